@@ -1,0 +1,285 @@
+/*
+ * resgpu: GB300 (sm_103a) implementation of the RS reservoir simulator's
+ * pressure hot path and of the MTJ sparse solver stack it calls.
+ *
+ * C ABI.  Plain pointers and sizes only; every call returns an rsg_status.
+ * Host buffers passed in are caller owned and only read or written during
+ * the call.  Device buffers are owned by the library and live behind the
+ * opaque handles.  One context owns one CUDA stream; handles created from a
+ * context must be used from one host thread at a time (MTJ solver objects
+ * are not re-entrant either: mtj/src/no/uib/cipr/matrix/sparse/BiCGstab.java:42-63).
+ * Destroy every handle created from a context before destroying the context.
+ *
+ * Reference interfaces replaced (paths relative to the RS/MTJ sources):
+ *   rsg_csr_*      sparse/CompRowMatrix.java:160-190 (construct), :300-372
+ *                  (mult/multAdd/transMult), :404-453 (add/zero)
+ *   rsg_solver_*   sparse/IterativeSolver.java:43-74 (solve),
+ *                  sparse/Preconditioner.java:42-63 (apply/setMatrix),
+ *                  sparse/DefaultIterationMonitor.java:72-156 (tolerances)
+ *   rsg_mesh_*     geometry/flux/TransmissibilityComputer.java:30-31
+ *                  (calculateTransmissibilities), numerics/LinearSolver.java:111-168
+ *                  (sparsity pattern)
+ *   rsg_sim_*      numerics/Discretisation.java:208-225 (solve(dt)),
+ *                  field/Field.java:69-96 (initialisation), :488-501
+ *                  (calculateSecondaries)
+ */
+#ifndef RSG_H
+#define RSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSG_ABI_VERSION 1
+#define RSG_MAX_COMPONENTS 8
+
+/* Status codes.  1..3 are MTJ's NotConvergedException.Reason values
+ * (sparse/IterativeSolverNotConvergedException.java:29-91). */
+typedef int32_t rsg_status;
+enum {
+  RSG_OK = 0,
+  RSG_NOT_CONVERGED_ITERATIONS = 1,
+  RSG_NOT_CONVERGED_DIVERGENCE = 2,
+  RSG_NOT_CONVERGED_BREAKDOWN = 3,
+  RSG_ZERO_PIVOT = 4,           /* sparse/ILU.java:105-107 */
+  RSG_MISSING_DIAGONAL = 5,     /* sparse/ILU.java:134-136 */
+  RSG_OUT_OF_PATTERN = 6,       /* sparse/CompRowMatrix.java:435 */
+  RSG_NONPOSITIVE_PRESSURE = 7, /* numerics/Discretisation.java:349-351 */
+  RSG_NEGATIVE_MOLES = 8,       /* numerics/Discretisation.java:800-812 */
+  RSG_BAD_ARG = 9,
+  RSG_CUDA_ERROR = 10,
+  RSG_TIMEOUT = 11,
+  RSG_UNSUPPORTED = 12,
+  RSG_NEWTON_NOT_CONVERGED = 13, /* numerics/Discretisation.java:327-329 */
+  RSG_SINGULAR = 14,             /* MatrixSingularException in MPFA / dense LU */
+  RSG_PHYSICS = 15               /* field/CV.java:496-500 and EOS data checks */
+};
+
+/* Krylov methods (numerics/LinearSolver.java:173-191) */
+enum { RSG_CG = 0, RSG_BICGSTAB = 1, RSG_GMRES = 2, RSG_FGMRES_MIXED = 3 };
+/* Preconditioners (numerics/LinearSolver.java:197-221) */
+enum { RSG_PC_NONE = 0, RSG_PC_DIAGONAL = 1, RSG_PC_ILU = 2, RSG_PC_SSOR = 3, RSG_PC_AMG = 4 };
+
+typedef struct rsg_ctx rsg_ctx;
+typedef struct rsg_csr rsg_csr;
+typedef struct rsg_solver rsg_solver;
+typedef struct rsg_mesh rsg_mesh;
+typedef struct rsg_sim rsg_sim;
+
+/* ------------------------------------------------------------ context -- */
+int32_t rsg_abi_version(void);
+const char* rsg_status_string(rsg_status s);
+/* Creates a context on CUDA device `device` (fails loudly with
+ * RSG_CUDA_ERROR when no sm_103 device is usable: there is no CPU path). */
+rsg_status rsg_context_create(int32_t device, rsg_ctx** out);
+rsg_status rsg_context_destroy(rsg_ctx* ctx);
+/* Last error message recorded on the context (empty if none). */
+const char* rsg_context_last_error(rsg_ctx* ctx);
+/* How the level-scheduled triangular sweeps run in this process:
+ * -1 not decided yet, 0 one launch per level, 1 one thread-block cluster
+ * walking all levels with hardware cluster barriers. */
+int32_t rsg_sweep_mode(void);
+/* Number of kernels this context has launched so far. */
+int64_t rsg_context_kernel_launches(rsg_ctx* ctx);
+/* Waits for all work queued on the context's stream. */
+rsg_status rsg_context_synchronize(rsg_ctx* ctx);
+/* Kernel-time accounting: when enabled, the library brackets its kernels
+ * with CUDA events on its own stream and accumulates per-kernel-family
+ * device time.  names: '\n'-separated family names written into buf. */
+rsg_status rsg_context_set_profiling(rsg_ctx* ctx, int32_t enabled);
+rsg_status rsg_context_profile_read(rsg_ctx* ctx, int32_t max_entries, double* ms, int64_t* launches,
+                                    char* names, int32_t names_len, int32_t* n_entries);
+rsg_status rsg_context_profile_reset(rsg_ctx* ctx);
+/* CUDA events on the context's stream for device-side timing: record into
+ * one of 64 slots, then read the elapsed milliseconds between two slots. */
+rsg_status rsg_context_timer_record(rsg_ctx* ctx, int32_t slot);
+rsg_status rsg_context_timer_elapsed(rsg_ctx* ctx, int32_t slot_a, int32_t slot_b, double* ms);
+/* Page-locked host memory for callers that stage inputs and results. */
+rsg_status rsg_host_alloc(size_t bytes, void** ptr);
+rsg_status rsg_host_free(void* ptr);
+
+/* ----------------------------------------------- CompRowMatrix (CSR) -- */
+/* Copies the pattern to the device.  Column indices must be sorted within
+ * each row (CompRowMatrix.construct sorts them). */
+rsg_status rsg_csr_create(rsg_ctx* ctx, int32_t n, int32_t nnz, const int32_t* row_ptr, const int32_t* col,
+                          rsg_csr** out);
+rsg_status rsg_csr_destroy(rsg_csr* A);
+rsg_status rsg_csr_set_values(rsg_csr* A, const double* values); /* host, nnz */
+rsg_status rsg_csr_get_values(rsg_csr* A, double* values);       /* host, nnz */
+/* y = A x  (CompRowMatrix.mult); host vectors of length n. */
+rsg_status rsg_csr_mult(rsg_csr* A, const double* x, double* y);
+/* y = alpha A x + y  (CompRowMatrix.multAdd) */
+rsg_status rsg_csr_mult_add(rsg_csr* A, double alpha, const double* x, double* y);
+/* y = A^T x  (CompRowMatrix.transMult) */
+rsg_status rsg_csr_trans_mult(rsg_csr* A, const double* x, double* y);
+/* Matrices.zeroRows(A, diagonal, rows) (mtj/src/no/uib/cipr/matrix/Matrices.java:631-652) */
+rsg_status rsg_csr_zero_rows(rsg_csr* A, double diagonal, int32_t nrows, const int32_t* rows);
+/* Device pointers of the CSR arrays (for callers that keep vectors on the GPU). */
+rsg_status rsg_csr_device_arrays(rsg_csr* A, const int32_t** row_ptr, const int32_t** col, double** values);
+
+/* ------------------------------ IterativeSolver + Preconditioner -------- */
+typedef struct {
+  int32_t iterations;    /* IterationMonitor.iterations() at exit */
+  int32_t reason;        /* rsg_status of the solve */
+  double residual;       /* last monitored residual norm */
+  double initial_residual;
+  int32_t inner_iterations; /* FP32 inner iterations (mixed precision only) */
+  int32_t refinements;      /* FP64 outer cycles (mixed precision only) */
+} rsg_solve_info;
+
+rsg_status rsg_solver_create(rsg_ctx* ctx, int32_t method, int32_t precond, rsg_solver** out);
+rsg_status rsg_solver_destroy(rsg_solver* s);
+/* DefaultIterationMonitor(maxIter, rtol, atol, dtol) */
+rsg_status rsg_solver_set_monitor(rsg_solver* s, double rtol, double atol, double dtol, int32_t max_iter);
+/* GMRES.setRestart (default 30) */
+rsg_status rsg_solver_set_restart(rsg_solver* s, int32_t restart);
+/* SSOR omegas (SSOR(F, reverse, omegaF, omegaR)) */
+rsg_status rsg_solver_set_ssor(rsg_solver* s, double omega_f, double omega_r, int32_t reverse);
+/* Preconditioner.setMatrix(A): ILU(0) factorisation / diagonal inversion. */
+rsg_status rsg_solver_setup(rsg_solver* s, rsg_csr* A);
+/* IterativeSolver.solve(A, b, x): x is the initial guess on entry and the
+ * solution on exit (host arrays of length n). */
+rsg_status rsg_solver_solve(rsg_solver* s, rsg_csr* A, const double* b, double* x, rsg_solve_info* info);
+/* Same with device-resident b and x (device pointers from this context). */
+rsg_status rsg_solver_solve_device(rsg_solver* s, rsg_csr* A, const double* d_b, double* d_x, rsg_solve_info* info);
+/* Preconditioner.apply(b, x) on host vectors (after rsg_solver_setup). */
+rsg_status rsg_precond_apply(rsg_solver* s, const double* b, double* x);
+/* Preconditioner.transApply(b, x) */
+rsg_status rsg_precond_trans_apply(rsg_solver* s, const double* b, double* x);
+/* Residual history of the last solve (monitor values in call order). */
+rsg_status rsg_solver_history(rsg_solver* s, int32_t max_len, double* out, int32_t* len);
+
+/* ------------------------------------------------- mesh + MPFA-O -------- */
+/* Structured hexahedral (dim 3) or quadrilateral (dim 2, nk = 0) mesh in
+ * RS's StructuredMeshGenerator numbering.  coords: 3 doubles per corner point
+ * in linear point order (i fastest), or NULL for the tensor grid built from
+ * (x0, y0, z0) and spacings (dx, dy, dz), dz < 0 as RS requires.
+ * perm: 6 doubles per element (xx, yy, zz, xy, xz, yz), RockDataParser's
+ * permx..permyz. */
+rsg_status rsg_mesh_create_structured(rsg_ctx* ctx, int32_t dim, int32_t ni, int32_t nj, int32_t nk,
+                                      const double* coords, double x0, double y0, double z0, double dx, double dy,
+                                      double dz, const double* perm, rsg_mesh** out);
+rsg_status rsg_mesh_destroy(rsg_mesh* m);
+/* O_MPFA.calculateTransmissibilities + Connection.setDarcyTransmissibilities,
+ * on the GPU.  continuity in (0, 1] (O_MPFA "Continuity" key). */
+rsg_status rsg_mesh_compute_mpfa(rsg_mesh* m, double continuity);
+/* counts[0] elements, [1] connections, [2] MD entries, [3] corner points,
+ * [4] pressure-pattern nnz (valid after MPFA) */
+rsg_status rsg_mesh_get_counts(rsg_mesh* m, int64_t* counts);
+/* centers: 3 per element; volumes: 1 per element (either may be NULL) */
+rsg_status rsg_mesh_get_geometry(rsg_mesh* m, double* centers, double* volumes);
+/* conn: 2 per connection (here, there) */
+rsg_status rsg_mesh_get_connections(rsg_mesh* m, int32_t* conn);
+/* MD lists: md_ptr (connections+1), md_elem and md_k (MD entries) */
+rsg_status rsg_mesh_get_transmissibilities(rsg_mesh* m, int32_t* md_ptr, int32_t* md_elem, double* md_k);
+/* which = 0: LinearSolver pattern (with diagonal); 1: PotentialCalculator
+ * pattern (without the explicit diagonal).  row_ptr: elements+1, col: nnz
+ * (query nnz first with col == NULL). */
+rsg_status rsg_mesh_get_pattern(rsg_mesh* m, int32_t which, int32_t* row_ptr, int32_t* col, int64_t* nnz);
+/* PotentialCalculator.discretizeFlux into a CSR created with pattern 1:
+ * A(here,k) += t_k, A(there,k) -= t_k (numerics/PotentialCalculator.java:319-333). */
+rsg_status rsg_mesh_assemble_potential(rsg_mesh* m, rsg_csr* A);
+
+/* -------------------------------------------- fluid / rock / sources --- */
+enum { RSG_FN_CONSTANT = 0, RSG_FN_TABLE = 1, RSG_FN_EVEN_TABLE = 2 };
+/* util/Function: ConstantValue, LookupTable (1-3D) or EvenLookupTable. */
+typedef struct {
+  int32_t kind;
+  int32_t dim;          /* number of arguments */
+  double value;         /* RSG_FN_CONSTANT */
+  int32_t n[3];         /* table points per axis */
+  const double* coord[3]; /* TABLE: n[d] sorted coordinates; EVEN: {min, max} */
+  const double* data;   /* n0*n1*n2 values, axis 0 fastest (LookupTable "data") */
+} rsg_function;
+
+/* BlackOilEquationOfState (fluid/BlackOilEquationOfState.java) on top of
+ * WaterEquationOfState (fluid/WaterEquationOfState.java).  Component 0 is
+ * water (fluid/Components.java:56-65). */
+typedef struct {
+  int32_t nc;
+  double molecular_weight[RSG_MAX_COMPONENTS];
+  int32_t group[RSG_MAX_COMPONENTS]; /* 0 water, 1 oil group, 2 gas group */
+  rsg_function water_density, water_viscosity, water_enthalpy; /* f(p, T) */
+  rsg_function bubble_point, dew_point;                        /* f(p, T) */
+  rsg_function oil_density, gas_density, oil_viscosity, gas_viscosity; /* f(p, C, T) */
+  rsg_function oil_enthalpy, gas_enthalpy;
+} rsg_blackoil;
+
+/* CoreyRockFluid (rock/CoreyRockFluid.java:41-82), phases water, oil, gas */
+typedef struct {
+  double Sr[3], n[3], ke[3];
+  double cw, cow, cg, cog, aw, aow, ag, aog;
+} rsg_corey;
+
+enum { RSG_SOURCE_FIXED = 0, RSG_SOURCE_REGULAR = 1 };
+/* field/Source.java: Fixed (locked cells) and Regular (mol/s per element) */
+typedef struct {
+  int32_t type;
+  int32_t num_elements;
+  const int32_t* elements;
+  double q[RSG_MAX_COMPONENTS];
+  double temperature;
+  double fraction[RSG_MAX_COMPONENTS];
+} rsg_source;
+
+/* field/InitialValues.java */
+typedef struct {
+  double datum_depth;
+  double datum_pressure;
+  rsg_function temperature;                     /* f(z) */
+  rsg_function fraction[RSG_MAX_COMPONENTS];   /* f(z) */
+} rsg_initial;
+
+/* numerics/RunSpec.java:133-251 (names kept) */
+typedef struct {
+  int32_t max_nonlinear_pressure_iterations; /* 10 */
+  double pressure_tolerance;                 /* 1e-6 */
+  int32_t linear_solver;                     /* RSG_BICGSTAB */
+  int32_t preconditioner;                    /* RSG_PC_ILU */
+  int32_t max_linear_iterations;             /* 5000 */
+  double relative_tolerance;                 /* 1e-50 */
+  double absolute_tolerance;                 /* 1e-12 */
+  double divergence_tolerance;               /* 1e5 */
+  int32_t truncate_negative_moles;           /* 0 */
+  int32_t newton_stop_rule;  /* 0: RS rule dp[0] < tol (Discretisation.java:324); 1: max |dp/p| < tol */
+  double omega, ax, ay;      /* BodyForces (field/Field.java:184-202) */
+  int32_t gmres_restart;     /* 30 */
+} rsg_runspec;
+
+typedef struct {
+  int32_t newton_iterations;
+  int32_t linear_iterations;   /* summed over the Newton iterations */
+  double dp_max;               /* last max |dp/p| */
+  double dp0;                  /* last correction of element 0 */
+  double mass_balance_error;   /* max over components, relative */
+  int32_t status;
+} rsg_step_info;
+
+/* Field construction + initialisation by local volume balance, on the GPU. */
+rsg_status rsg_sim_create(rsg_ctx* ctx, rsg_mesh* m, const rsg_blackoil* fluid, const rsg_corey* rockfluid,
+                          const double* porosity, const double* compaction, int32_t nsources,
+                          const rsg_source* sources, const rsg_initial* init, const rsg_runspec* spec,
+                          rsg_sim** out);
+rsg_status rsg_sim_destroy(rsg_sim* s);
+/* Discretisation.solve(dt): pressure Newton loop, explicit molar masses,
+ * secondaries.  On failure the state is left as the reference leaves it;
+ * rsg_sim_retract restores the state stored at the start of the step
+ * (Field.retract). */
+rsg_status rsg_sim_step(rsg_sim* s, double dt, rsg_step_info* info);
+rsg_status rsg_sim_retract(rsg_sim* s);
+/* p: n; N: nc*n (component major); S: 3*n (phase major) — any may be NULL */
+rsg_status rsg_sim_get_state(rsg_sim* s, double* p, double* N, double* S);
+rsg_status rsg_sim_set_state(rsg_sim* s, const double* p, const double* N);
+/* Last assembled pressure Jacobian (values in the pressure pattern order)
+ * and right-hand side, before the locked-row treatment. */
+rsg_status rsg_sim_get_jacobian(rsg_sim* s, double* values, double* rhs);
+/* Per-cell secondaries after the last update: R, dRdp (n each). */
+rsg_status rsg_sim_get_residual_volume(rsg_sim* s, double* R, double* dRdp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RSG_H */

@@ -1,0 +1,484 @@
+"""Python host binding of libresgpu (include/rsg.h), named after the
+reference interfaces it replaces:
+
+* ``CompRowMatrix``  - mtj sparse/CompRowMatrix (mult, multAdd, transMult, zeroRows)
+* ``CG``, ``BiCGstab``, ``GMRES`` - mtj sparse iterative solvers, each with a
+  preconditioner kind (``ILU``, ``SSOR``, ``DIAGONAL``, ``NONE``) and
+  DefaultIterationMonitor tolerances
+* ``Mesh``           - RS structured mesh + TransmissibilityComputer (O-MPFA)
+* ``Discretisation`` - RS Field + Discretisation.solve(dt)
+
+There is no CPU path: constructing a ``Context`` fails loudly when the CUDA
+library or a Blackwell GPU is missing.
+"""
+import ctypes as C
+import os
+import weakref
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libresgpu.so")
+_lib = None
+
+
+class RSGError(RuntimeError):
+    def __init__(self, status, msg=""):
+        super().__init__(f"{abi.STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class IterativeSolverNotConvergedException(RSGError):
+    """mtj sparse/IterativeSolverNotConvergedException: reason, residual, iterations."""
+
+    def __init__(self, status, msg, residual, iterations):
+        super().__init__(status, msg)
+        self.reason = {1: "Iterations", 2: "Divergence", 3: "Breakdown"}.get(status, "Other")
+        self.residual = residual
+        self.iterations = iterations
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() (there is no CPU fallback)")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    vp, i32, i64, d = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    P = C.POINTER
+    PP = lambda: P(vp)  # noqa: E731
+    sigs = {
+        "rsg_abi_version": (i32, []),
+        "rsg_sweep_mode": (i32, []),
+        "rsg_status_string": (C.c_char_p, [i32]),
+        "rsg_context_create": (i32, [i32, PP()]),
+        "rsg_context_destroy": (i32, [vp]),
+        "rsg_context_last_error": (C.c_char_p, [vp]),
+        "rsg_context_kernel_launches": (i64, [vp]),
+        "rsg_context_synchronize": (i32, [vp]),
+        "rsg_context_set_profiling": (i32, [vp, i32]),
+        "rsg_context_profile_read": (i32, [vp, i32, P(d), P(i64), C.c_char_p, i32, P(i32)]),
+        "rsg_context_profile_reset": (i32, [vp]),
+        "rsg_context_timer_record": (i32, [vp, i32]),
+        "rsg_context_timer_elapsed": (i32, [vp, i32, i32, P(d)]),
+        "rsg_host_alloc": (i32, [C.c_size_t, P(vp)]),
+        "rsg_host_free": (i32, [vp]),
+        "rsg_csr_create": (i32, [vp, i32, i32, P(i32), P(i32), PP()]),
+        "rsg_csr_destroy": (i32, [vp]),
+        "rsg_csr_set_values": (i32, [vp, P(d)]),
+        "rsg_csr_get_values": (i32, [vp, P(d)]),
+        "rsg_csr_mult": (i32, [vp, P(d), P(d)]),
+        "rsg_csr_mult_add": (i32, [vp, d, P(d), P(d)]),
+        "rsg_csr_trans_mult": (i32, [vp, P(d), P(d)]),
+        "rsg_csr_zero_rows": (i32, [vp, d, i32, P(i32)]),
+        "rsg_csr_device_arrays": (i32, [vp, P(vp), P(vp), P(vp)]),
+        "rsg_solver_create": (i32, [vp, i32, i32, PP()]),
+        "rsg_solver_destroy": (i32, [vp]),
+        "rsg_solver_set_monitor": (i32, [vp, d, d, d, i32]),
+        "rsg_solver_set_restart": (i32, [vp, i32]),
+        "rsg_solver_set_ssor": (i32, [vp, d, d, i32]),
+        "rsg_solver_setup": (i32, [vp, vp]),
+        "rsg_solver_solve": (i32, [vp, vp, P(d), P(d), P(abi.rsg_solve_info)]),
+        "rsg_solver_solve_device": (i32, [vp, vp, vp, vp, P(abi.rsg_solve_info)]),
+        "rsg_precond_apply": (i32, [vp, P(d), P(d)]),
+        "rsg_precond_trans_apply": (i32, [vp, P(d), P(d)]),
+        "rsg_solver_history": (i32, [vp, i32, P(d), P(i32)]),
+        "rsg_mesh_create_structured": (i32, [vp, i32, i32, i32, i32, P(d), d, d, d, d, d, d, P(d), PP()]),
+        "rsg_mesh_destroy": (i32, [vp]),
+        "rsg_mesh_compute_mpfa": (i32, [vp, d]),
+        "rsg_mesh_get_counts": (i32, [vp, P(i64)]),
+        "rsg_mesh_get_geometry": (i32, [vp, P(d), P(d)]),
+        "rsg_mesh_get_connections": (i32, [vp, P(i32)]),
+        "rsg_mesh_get_transmissibilities": (i32, [vp, P(i32), P(i32), P(d)]),
+        "rsg_mesh_get_pattern": (i32, [vp, i32, P(i32), P(i32), P(i64)]),
+        "rsg_mesh_assemble_potential": (i32, [vp, vp]),
+        "rsg_sim_create": (i32, [vp, vp, P(abi.rsg_blackoil), P(abi.rsg_corey), P(d), P(d), i32, P(abi.rsg_source),
+                                 P(abi.rsg_initial), P(abi.rsg_runspec), PP()]),
+        "rsg_sim_destroy": (i32, [vp]),
+        "rsg_sim_step": (i32, [vp, d, P(abi.rsg_step_info)]),
+        "rsg_sim_retract": (i32, [vp]),
+        "rsg_sim_get_state": (i32, [vp, P(d), P(d), P(d)]),
+        "rsg_sim_set_state": (i32, [vp, P(d), P(d)]),
+        "rsg_sim_get_jacobian": (i32, [vp, P(d), P(d)]),
+        "rsg_sim_get_residual_volume": (i32, [vp, P(d), P(d)]),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Context:
+    """One CUDA device and one stream (rsg_context_*)."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        st = lib().rsg_context_create(device, C.byref(h))
+        if st != 0:
+            raise RSGError(st, "rsg_context_create failed (a Blackwell GPU and libresgpu.so are required)")
+        self.h = h
+        # handles created from this context; destroyed before the context is
+        self.children = weakref.WeakSet()
+
+    def adopt(self, obj):
+        self.children.add(obj)
+
+    def check(self, st, what=""):
+        if st != 0:
+            raise RSGError(st, f"{what}: {lib().rsg_context_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            for child in list(getattr(self, "children", ())):
+                child.release()
+            lib().rsg_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def kernel_launches(self):
+        return lib().rsg_context_kernel_launches(self.h)
+
+    def synchronize(self):
+        self.check(lib().rsg_context_synchronize(self.h), "synchronize")
+
+    def set_profiling(self, on):
+        self.check(lib().rsg_context_set_profiling(self.h, int(on)), "set_profiling")
+
+    def profile_reset(self):
+        self.check(lib().rsg_context_profile_reset(self.h), "profile_reset")
+
+    def timer_record(self, slot):
+        self.check(lib().rsg_context_timer_record(self.h, slot), "timer_record")
+
+    def timer_elapsed_ms(self, a, b):
+        ms = C.c_double(0)
+        self.check(lib().rsg_context_timer_elapsed(self.h, a, b, C.byref(ms)), "timer_elapsed")
+        return ms.value
+
+    def profile(self):
+        ms = (C.c_double * 256)()
+        ln = (C.c_int64 * 256)()
+        names = C.create_string_buffer(16384)
+        k = C.c_int32(0)
+        self.check(lib().rsg_context_profile_read(self.h, 256, ms, ln, names, 16384, C.byref(k)), "profile_read")
+        keys = names.value.decode().split("\n")[: k.value]
+        return {keys[i]: (ms[i], ln[i]) for i in range(k.value)}
+
+
+class CompRowMatrix:
+    """mtj CompRowMatrix with the pattern resident on the GPU."""
+
+    def __init__(self, ctx, n, rowptr, col, values=None):
+        self.ctx = ctx
+        self.n = int(n)
+        self.rowptr = _i32(rowptr)
+        self.col = _i32(col)
+        h = C.c_void_p()
+        ctx.check(lib().rsg_csr_create(ctx.h, self.n, len(self.col), abi.iptr(self.rowptr), abi.iptr(self.col),
+                                       C.byref(h)), "rsg_csr_create")
+        self.h = h
+        ctx.adopt(self)
+        if values is not None:
+            self.set_values(values)
+
+    def release(self):
+        if getattr(self, "h", None):
+            if self.ctx.h is not None:
+                lib().rsg_csr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    @property
+    def nnz(self):
+        return len(self.col)
+
+    def set_values(self, values):
+        v = _f64(values)
+        assert len(v) == self.nnz
+        self.ctx.check(lib().rsg_csr_set_values(self.h, abi.dptr(v)), "set_values")
+
+    def get_values(self):
+        v = np.zeros(self.nnz)
+        self.ctx.check(lib().rsg_csr_get_values(self.h, abi.dptr(v)), "get_values")
+        return v
+
+    def mult(self, x):
+        x = _f64(x)
+        y = np.zeros(self.n)
+        self.ctx.check(lib().rsg_csr_mult(self.h, abi.dptr(x), abi.dptr(y)), "mult")
+        return y
+
+    def mult_add(self, alpha, x, y):
+        x = _f64(x)
+        y = _f64(y).copy()
+        self.ctx.check(lib().rsg_csr_mult_add(self.h, alpha, abi.dptr(x), abi.dptr(y)), "multAdd")
+        return y
+
+    def trans_mult(self, x):
+        x = _f64(x)
+        y = np.zeros(self.n)
+        self.ctx.check(lib().rsg_csr_trans_mult(self.h, abi.dptr(x), abi.dptr(y)), "transMult")
+        return y
+
+    def zero_rows(self, diagonal, rows):
+        r = _i32(rows)
+        self.ctx.check(lib().rsg_csr_zero_rows(self.h, diagonal, len(r), abi.iptr(r)), "zeroRows")
+
+
+class IterativeSolver:
+    """IterativeSolver + Preconditioner pair (rsg_solver_*)."""
+
+    method = None
+
+    def __init__(self, ctx, precond=abi.PC_ILU, rtol=1e-5, atol=1e-50, dtol=1e5, max_iter=100000, restart=None):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ctx.check(lib().rsg_solver_create(ctx.h, self.method, precond, C.byref(h)), "rsg_solver_create")
+        self.h = h
+        ctx.adopt(self)
+        self.set_monitor(rtol, atol, dtol, max_iter)
+        if restart is not None:
+            ctx.check(lib().rsg_solver_set_restart(self.h, restart), "setRestart")
+        self.last_info = None
+
+    def release(self):
+        if getattr(self, "h", None):
+            if self.ctx.h is not None:
+                lib().rsg_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def set_monitor(self, rtol, atol, dtol, max_iter):
+        self.ctx.check(lib().rsg_solver_set_monitor(self.h, rtol, atol, dtol, max_iter), "set_monitor")
+
+    def set_ssor(self, omega_f, omega_r, reverse=True):
+        self.ctx.check(lib().rsg_solver_set_ssor(self.h, omega_f, omega_r, int(reverse)), "set_ssor")
+
+    def set_matrix(self, A):
+        """Preconditioner.setMatrix(A)"""
+        self.ctx.check(lib().rsg_solver_setup(self.h, A.h), "setMatrix")
+
+    def solve(self, A, b, x0, raise_on_fail=True):
+        """IterativeSolver.solve(A, b, x): returns the new x."""
+        b = _f64(b)
+        x = _f64(x0).copy()
+        info = abi.rsg_solve_info()
+        st = lib().rsg_solver_solve(self.h, A.h, abi.dptr(b), abi.dptr(x), C.byref(info))
+        self.last_info = info
+        if st in (1, 2, 3) and raise_on_fail:
+            raise IterativeSolverNotConvergedException(st, lib().rsg_context_last_error(self.ctx.h).decode(),
+                                                       info.residual, info.iterations)
+        if st not in (0, 1, 2, 3):
+            self.ctx.check(st, "solve")
+        return x
+
+    def apply(self, b, x0=None, trans=False):
+        """Preconditioner.apply / transApply on host vectors."""
+        b = _f64(b)
+        x = np.zeros_like(b) if x0 is None else _f64(x0).copy()
+        f = lib().rsg_precond_trans_apply if trans else lib().rsg_precond_apply
+        self.ctx.check(f(self.h, abi.dptr(b), abi.dptr(x)), "apply")
+        return x
+
+    def history(self):
+        n = C.c_int32(0)
+        lib().rsg_solver_history(self.h, 0, abi.dptr(None), C.byref(n))
+        out = np.zeros(max(n.value, 1))
+        self.ctx.check(lib().rsg_solver_history(self.h, len(out), abi.dptr(out), C.byref(n)), "history")
+        return out[: n.value]
+
+
+class CG(IterativeSolver):
+    method = abi.CG
+
+
+class BiCGstab(IterativeSolver):
+    method = abi.BICGSTAB
+
+
+class GMRES(IterativeSolver):
+    method = abi.GMRES
+
+
+class Mesh:
+    """Structured RS mesh; compute_mpfa() = O_MPFA.calculateTransmissibilities."""
+
+    def __init__(self, ctx, dim, ni, nj, nk, perm, coords=None, x0=0.0, y0=0.0, z0=0.0, dx=1.0, dy=1.0, dz=-1.0):
+        self.ctx = ctx
+        self._perm = _f64(perm)
+        self._coords = _f64(coords) if coords is not None else None
+        h = C.c_void_p()
+        ctx.check(lib().rsg_mesh_create_structured(ctx.h, dim, ni, nj, nk, abi.dptr(self._coords), x0, y0, z0, dx,
+                                                   dy, dz, abi.dptr(self._perm), C.byref(h)), "mesh_create")
+        self.h = h
+        ctx.adopt(self)
+
+    def release(self):
+        if getattr(self, "h", None):
+            if self.ctx.h is not None:
+                lib().rsg_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def compute_mpfa(self, continuity=1.0):
+        self.ctx.check(lib().rsg_mesh_compute_mpfa(self.h, continuity), "compute_mpfa")
+
+    def counts(self):
+        c = (C.c_int64 * 5)()
+        self.ctx.check(lib().rsg_mesh_get_counts(self.h, c), "counts")
+        return dict(elements=c[0], connections=c[1], md=c[2], points=c[3], pattern_nnz=c[4])
+
+    def geometry(self):
+        k = self.counts()
+        centers = np.zeros((k["elements"], 3))
+        vols = np.zeros(k["elements"])
+        self.ctx.check(lib().rsg_mesh_get_geometry(self.h, abi.dptr(centers), abi.dptr(vols)), "geometry")
+        return centers, vols
+
+    def connections(self):
+        k = self.counts()
+        conn = np.zeros((k["connections"], 2), dtype=np.int32)
+        self.ctx.check(lib().rsg_mesh_get_connections(self.h, abi.iptr(conn)), "connections")
+        return conn
+
+    def transmissibilities(self):
+        k = self.counts()
+        ptr = np.zeros(k["connections"] + 1, dtype=np.int32)
+        el = np.zeros(k["md"], dtype=np.int32)
+        kk = np.zeros(k["md"])
+        self.ctx.check(lib().rsg_mesh_get_transmissibilities(self.h, abi.iptr(ptr), abi.iptr(el), abi.dptr(kk)),
+                       "transmissibilities")
+        return ptr, el, kk
+
+    def pattern(self, which=0):
+        nnz = C.c_int64(0)
+        self.ctx.check(lib().rsg_mesh_get_pattern(self.h, which, abi.iptr(None), abi.iptr(None), C.byref(nnz)),
+                       "pattern")
+        n = self.counts()["elements"]
+        rp = np.zeros(n + 1, dtype=np.int32)
+        col = np.zeros(nnz.value, dtype=np.int32)
+        self.ctx.check(lib().rsg_mesh_get_pattern(self.h, which, abi.iptr(rp), abi.iptr(col), C.byref(nnz)),
+                       "pattern")
+        return rp, col
+
+    def assemble_potential(self, A):
+        self.ctx.check(lib().rsg_mesh_assemble_potential(self.h, A.h), "assemble_potential")
+
+
+class Discretisation:
+    """RS Field + Discretisation on the GPU: step(dt) = Discretisation.solve(dt)."""
+
+    def __init__(self, ctx, mesh, fluid, corey, porosity, compaction, sources, init, spec):
+        self.ctx = ctx
+        self.mesh = mesh
+        self._keep = (fluid, corey, _f64(porosity), _f64(compaction), sources, init, spec)
+        h = C.c_void_p()
+        ctx.check(lib().rsg_sim_create(ctx.h, mesh.h, C.byref(fluid), C.byref(corey), abi.dptr(self._keep[2]),
+                                       abi.dptr(self._keep[3]), len(sources), sources, C.byref(init), C.byref(spec),
+                                       C.byref(h)), "sim_create")
+        self.h = h
+        ctx.adopt(self)
+        self.n = mesh.counts()["elements"]
+        self.nc = fluid.nc
+
+    def release(self):
+        if getattr(self, "h", None):
+            if self.ctx.h is not None:
+                lib().rsg_sim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def step(self, dt, raise_on_fail=True):
+        info = abi.rsg_step_info()
+        st = lib().rsg_sim_step(self.h, dt, C.byref(info))
+        if st != 0 and raise_on_fail:
+            self.ctx.check(st, "Discretisation.solve")
+        return info
+
+    def retract(self):
+        self.ctx.check(lib().rsg_sim_retract(self.h), "retract")
+
+    def state(self):
+        p = np.zeros(self.n)
+        N = np.zeros(self.nc * self.n)
+        S = np.zeros(3 * self.n)
+        self.ctx.check(lib().rsg_sim_get_state(self.h, abi.dptr(p), abi.dptr(N), abi.dptr(S)), "state")
+        return p, N.reshape(self.nc, self.n), S.reshape(3, self.n)
+
+    def set_state(self, p, N):
+        p = _f64(p)
+        N = _f64(N).reshape(-1)
+        self.ctx.check(lib().rsg_sim_set_state(self.h, abi.dptr(p), abi.dptr(N)), "set_state")
+
+    def enable_jacobian_capture(self):
+        st = lib().rsg_sim_get_jacobian(self.h, abi.dptr(None), abi.dptr(None))
+        return st
+
+    def jacobian(self, nnz):
+        v = np.zeros(nnz)
+        r = np.zeros(self.n)
+        self.ctx.check(lib().rsg_sim_get_jacobian(self.h, abi.dptr(v), abi.dptr(r)), "jacobian")
+        return v, r
+
+    def residual_volume(self):
+        R = np.zeros(self.n)
+        d = np.zeros(self.n)
+        self.ctx.check(lib().rsg_sim_get_residual_volume(self.h, abi.dptr(R), abi.dptr(d)), "residual_volume")
+        return R, d
+
+
+class PinnedArray:
+    """numpy float64 view of page-locked host memory (rsg_host_alloc)."""
+
+    def __init__(self, count):
+        p = C.c_void_p()
+        st = lib().rsg_host_alloc(max(1, count) * 8, C.byref(p))
+        if st != 0:
+            raise RSGError(st, "rsg_host_alloc")
+        self.p = p
+        self.array = np.ctypeslib.as_array((C.c_double * max(1, count)).from_address(p.value))[:count]
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            lib().rsg_host_free(self.p)
+            self.p = None

@@ -1,0 +1,98 @@
+// Sparse linear algebra on the GPU: CompRowMatrix storage (CSR plus a
+// SELL-32 copy for coalesced SpMV), deterministic reductions, level
+// scheduled triangular sweeps (ILU(0), SSOR) and the Krylov drivers.
+#pragma once
+#include <memory>
+
+#include "common.cuh"
+
+namespace rsg {
+
+constexpr int SELL_C = 32;
+
+// Level schedule of a triangular sweep, laid out as SELL-32 slices that never
+// straddle a level: slot (slice s, lane l, k) lives at base[s] + 32*k + l.
+struct SweepPlan {
+  int nlev = 0, nslices = 0;
+  std::vector<int> h_level_slices;  // nlev + 1 slice offsets
+  DeviceBuffer<int> level_slices, slice_base, slice_width, row, len, col, src;
+  DeviceBuffer<double> val;   // FP64 coefficients (gathered from CSR via src)
+  DeviceBuffer<float> valf;   // FP32 copy for the mixed-precision inner solver
+  DeviceBuffer<int> diag_src; // CSR position of each slot row's diagonal (upper sweeps)
+  DeviceBuffer<double> diag;  // diagonal per slot row (upper sweeps)
+  DeviceBuffer<float> diagf;
+  int max_rows_per_level = 0;
+};
+
+struct Csr {
+  Context* ctx = nullptr;
+  int n = 0, nnz = 0;
+  std::vector<int> h_rowptr, h_col;
+  DeviceBuffer<int> rowptr, col;
+  DeviceBuffer<double> val;
+  // SELL-32 copy used by SpMV
+  int nslices = 0;
+  int64_t sell_size = 0;
+  DeviceBuffer<int> slice_base, row_len, sell_col, sell_src;
+  DeviceBuffer<double> sell_val;
+  DeviceBuffer<float> sell_valf;
+  bool sell_dirty = true;
+  // diagonal positions (-1 if missing)
+  std::vector<int> h_diag;
+  DeviceBuffer<int> diag;
+  void build(Context* c, int n, int nnz, const int* rowptr, const int* col);
+  void refresh_sell();   // gathers CSR values into the SELL copy if stale
+  void refresh_sell_f32();
+};
+
+// Device-resident scalar state of one Krylov solve.
+struct KState {
+  double rho_1, rho_2, alpha, beta, omega, rho;
+  double residual, initR;
+  double rtol, atol, dtol;
+  double vscale;  // GMRES 1/H(i+1,i)
+  int iter, maxIter;
+  int status;     // 0 running, 1 converged, 2 converged on s (BiCGstab), negative: rsg_status failure
+  int first;
+  int hist_len, hist_cap;
+  int gm_i;       // GMRES inner index
+  int gm_exit;    // GMRES inner loop finished
+  int restart;
+};
+
+enum { KS_RUNNING = 0, KS_CONVERGED = 1, KS_CONVERGED_S = 2 };
+
+struct Precond {
+  virtual ~Precond() {}
+  virtual void setup(Csr& A) = 0;
+  // x := M^{-1} b (x may be read as the starting iterate, as SSOR does)
+  virtual void apply(const double* b, double* x, const int* active) = 0;
+  virtual void trans_apply(const double* b, double* x, const int* active) = 0;
+  // FP32 variant for the mixed-precision inner solver
+  virtual void apply_f32(const float* b, float* x, const int* active) {
+    throw Error(RSG_UNSUPPORTED, "preconditioner has no FP32 variant");
+  }
+};
+
+std::unique_ptr<Precond> make_precond(Context* ctx, int kind);
+
+// Krylov solver handle (defined in krylov.cu)
+struct Solver;
+struct SolverDeleter {
+  void operator()(Solver* s) const;
+};
+using SolverPtr = std::unique_ptr<Solver, SolverDeleter>;
+SolverPtr make_solver(Context* ctx, int method, int precond, double rtol, double atol, double dtol, int maxit,
+                      int restart);
+void solver_setup(Solver& s, Csr& A);
+void solver_solve(Solver& s, Csr& A, const double* b, double* x, rsg_solve_info* info);
+
+// Launches of BLAS-1 style kernels shared by the drivers.
+void launch_spmv(Context& ctx, Csr& A, const double* x, double* y, const int* active);
+void launch_spmv_f32(Context& ctx, Csr& A, const float* x, float* y, const int* active);
+
+}  // namespace rsg
+
+struct rsg_csr {
+  rsg::Csr m;
+};

@@ -1,0 +1,939 @@
+// Structured mesh geometry and MPFA-O transmissibilities on the GPU.
+//
+// Topology follows RS's StructuredMeshGenerator numbering in closed form
+// (rs/src/no/uib/cipr/rs/meshgen/structured/CartesianTopology3D.java:41-286,
+// CartesianTopology2D.java:38-228, NaturalIJKOrdering.java:57-104,
+// geometry/Topology.java:207-247): the interface and element lists of a
+// corner point come in the order RS's LinkedHashSets produce them, which
+// fixes the local numbering of each interaction region and therefore the
+// pivoting of its LU factorisation.
+//
+// Geometry restates HexCell/QuadCell/BilinearMap/TrilinearMap; MPFA-O
+// restates geometry/flux/O_MPFA.java:55-457 and MPFA.java:43-354 with the
+// dense LU of netlib dgesv (dgetf2 + dgetrs) and dgemm, one thread per corner
+// point.  Everything is compiled without fused multiply-add so each product
+// and sum rounds as the Java code does.
+#include <algorithm>
+#include <numeric>
+
+#include "mesh.cuh"
+
+namespace rsg {
+
+namespace {
+
+struct V3 {
+  double x, y, z;
+};
+__device__ __forceinline__ V3 vsub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 vadd(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 vmul(V3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V3 vcross(V3 a, V3 v) {
+  return {a.y * v.z - a.z * v.y, a.z * v.x - a.x * v.z, a.x * v.y - a.y * v.x};
+}
+__device__ __forceinline__ double vdot(V3 a, V3 v) { return a.x * v.x + a.y * v.y + a.z * v.z; }
+__device__ __forceinline__ double vnorm(V3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ double vcomp(V3 a, int c) { return c == 1 ? a.x : (c == 2 ? a.y : a.z); }
+__device__ __forceinline__ V3 ld3(const double* p, int64_t i) { return {p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
+__device__ __forceinline__ void st3(double* p, int64_t i, V3 v) {
+  p[3 * i] = v.x;
+  p[3 * i + 1] = v.y;
+  p[3 * i + 2] = v.z;
+}
+
+__host__ __device__ __forceinline__ int EL(const Grid& g, int i, int j, int k) { return i + j * g.ni + k * g.ni * g.nj; }
+__host__ __device__ __forceinline__ int PT(const Grid& g, int i, int j, int k) {
+  return i + j * g.npi + k * g.npi * g.npj;
+}
+__host__ __device__ __forceinline__ bool valid(const Grid& g, int i, int j, int k) {
+  if (i < 0 || i > g.ni - 1 || j < 0 || j > g.nj - 1) return false;
+  if (g.dim == 3) return k >= 0 && k <= g.nk - 1;
+  return k == 0;
+}
+__host__ __device__ __forceinline__ void el_ijk(const Grid& g, int e, int& i, int& j, int& k) {
+  i = e % g.ni;
+  j = (e / g.ni) % g.nj;
+  k = e / (g.ni * g.nj);
+}
+
+// Neighbour across face o of element (i,j,k); returns false on the boundary.
+__host__ __device__ bool face_neighbour(const Grid& g, int i, int j, int k, int o, int& ne, int& no) {
+  int di = 0, dj = 0, dk = 0, opp;
+  if (g.dim == 3) {
+    switch (o) {
+      case 0: dk = -1; opp = 1; break;
+      case 1: dk = 1; opp = 0; break;
+      case 2: dj = -1; opp = 3; break;
+      case 3: dj = 1; opp = 2; break;
+      case 4: di = -1; opp = 5; break;
+      default: di = 1; opp = 4; break;
+    }
+  } else {
+    switch (o) {
+      case 0: dj = -1; opp = 1; break;
+      case 1: dj = 1; opp = 0; break;
+      case 2: di = -1; opp = 3; break;
+      default: di = 1; opp = 2; break;
+    }
+  }
+  if (!valid(g, i + di, j + dj, k + dk)) return false;
+  ne = EL(g, i + di, j + dj, k + dk);
+  no = opp;
+  return true;
+}
+
+// Connection index of an interior face (CartesianTopology3D.getLinearConnection :104-130,
+// CartesianTopology2D :103-119); forward faces (odd o) are the "here" side.
+__host__ __device__ int face_connection(const Grid& g, int i, int j, int k, int o) {
+  if (!(o & 1)) {
+    int ne, no;
+    face_neighbour(g, i, j, k, o, ne, no);
+    int a, b, c;
+    el_ijk(g, ne, a, b, c);
+    i = a;
+    j = b;
+    k = c;
+    o = no;
+  }
+  const int ni = g.ni, nj = g.nj, nk = g.nk;
+  if (g.dim == 3) {
+    if (o == 1) return i + j * ni + k * ni * nj;
+    if (o == 3) return i + j * ni + k * ni * (nj - 1) + ni * nj * (nk - 1);
+    return i + j * (ni - 1) + k * (ni - 1) * nj + ni * (nj - 1) * nk + ni * nj * (nk - 1);
+  }
+  if (o == 1) return i + j * ni;
+  return i + j * (ni - 1) + ni * (nj - 1);
+}
+
+__host__ __device__ void elem_points(const Grid& g, int i, int j, int k, int* cp) {
+  if (g.dim == 3) {
+    cp[0] = PT(g, i, j, k);
+    cp[1] = cp[0] + 1;
+    cp[2] = PT(g, i, j + 1, k) + 1;
+    cp[3] = cp[2] - 1;
+    cp[4] = PT(g, i, j, k + 1);
+    cp[5] = cp[4] + 1;
+    cp[6] = PT(g, i, j + 1, k + 1) + 1;
+    cp[7] = cp[6] - 1;
+  } else {
+    cp[0] = PT(g, i, j, 0);
+    cp[1] = cp[0] + 1;
+    cp[2] = PT(g, i, j + 1, 0) + 1;
+    cp[3] = cp[2] - 1;
+  }
+}
+
+// getInterfacePoints (3D :267-286, 2D :213-228)
+__host__ __device__ int face_points(const Grid& g, const int* cp, int o, int* ip) {
+  if (g.dim == 3) {
+    const int t[6][4] = {{0, 1, 2, 3}, {7, 6, 5, 4}, {4, 5, 1, 0}, {6, 7, 3, 2}, {7, 4, 0, 3}, {5, 6, 2, 1}};
+    for (int a = 0; a < 4; ++a) ip[a] = cp[t[o][a]];
+    return 4;
+  }
+  const int t2[4][2] = {{1, 0}, {3, 2}, {0, 3}, {2, 1}};
+  ip[0] = cp[t2[o][0]];
+  ip[1] = cp[t2[o][1]];
+  return 2;
+}
+
+// Corner point topology: elements in NaturalIJKOrdering iteration order,
+// interfaces grouped by element in orientation order.
+struct PointTopo {
+  int ne, nf, nconn;
+  int el[8];
+  int eijk[8][3];
+  int face[24];     // global interface index
+  int fel[24];      // position of the owning element in el[]
+  int fo[24];       // orientation
+  int lidx[24];     // local connection index (intfMap)
+  char boundary[24];
+};
+
+__device__ void point_topology(const Grid& g, int p, PointTopo& t) {
+  const int pi = p % g.npi, pj = (p / g.npi) % g.npj, pk = p / (g.npi * g.npj);
+  t.ne = 0;
+  t.nf = 0;
+  const int nfe = g.dim == 3 ? 6 : 4;
+  for (int di = -1; di <= 0; ++di)
+    for (int dj = -1; dj <= 0; ++dj)
+      for (int dk = (g.dim == 3 ? -1 : 0); dk <= 0; ++dk) {
+        int i = pi + di, j = pj + dj, k = pk + dk;
+        if (!valid(g, i, j, k)) continue;
+        int a = t.ne++;
+        int e = EL(g, i, j, k);
+        t.el[a] = e;
+        t.eijk[a][0] = i;
+        t.eijk[a][1] = j;
+        t.eijk[a][2] = k;
+        int os[3], no = 0;
+        if (g.dim == 3) os[no++] = (pk == k) ? 0 : 1;
+        if (g.dim == 3) os[no++] = (pj == j) ? 2 : 3;
+        else os[no++] = (pj == j) ? 0 : 1;
+        if (g.dim == 3) os[no++] = (pi == i) ? 4 : 5;
+        else os[no++] = (pi == i) ? 2 : 3;
+        for (int q = 0; q < no; ++q) {
+          int f = t.nf++;
+          t.face[f] = e * nfe + os[q];
+          t.fel[f] = a;
+          t.fo[f] = os[q];
+          int ne_, no_;
+          t.boundary[f] = !face_neighbour(g, i, j, k, os[q], ne_, no_);
+        }
+      }
+  // createLocalInterfaceMap (O_MPFA.java:142-153)
+  t.nconn = 0;
+  for (int f = 0; f < t.nf; ++f) {
+    int idx = -1;
+    if (!t.boundary[f]) {
+      int a = t.fel[f];
+      int ne_, no_;
+      face_neighbour(g, t.eijk[a][0], t.eijk[a][1], t.eijk[a][2], t.fo[f], ne_, no_);
+      int nb = ne_ * nfe + no_;
+      for (int q = 0; q < f; ++q)
+        if (t.face[q] == nb) {
+          idx = t.lidx[q];
+          break;
+        }
+    }
+    t.lidx[f] = idx >= 0 ? idx : t.nconn++;
+  }
+}
+
+// ---------------------------------------------------------- geometry ----
+struct Bilin {
+  V3 p0, p1, p2, p3, normal;
+  double area;
+};
+__device__ Bilin bilinear(V3 a, V3 b, V3 c, V3 d) {
+  // BilinearMap.computeAreaNormal (:79-102)
+  Bilin m{a, b, c, d, {0, 0, 0}, 0};
+  V3 x1 = a, x2 = b, x3 = c, x4 = d;
+  V3 A = vcross(vsub(x2, x1), vsub(x3, x1));
+  V3 B = vcross(vsub(x2, x1), vsub(x4, x2));
+  V3 C = vcross(vsub(x4, x3), vsub(x3, x1));
+  V3 D = vcross(vsub(x4, x3), vsub(x4, x2));
+  V3 n = vmul(vadd(A, vadd(B, vadd(C, D))), .25);
+  double length = vnorm(n);
+  m.area = length;
+  m.normal = (length < 1.0e-9) ? V3{0, 0, 0} : vmul(n, 1.0 / length);
+  return m;
+}
+__device__ V3 bilin_point(const Bilin& m, double a, double b) {
+  double k0 = (1 - a) * (1 - b), k1 = a * (1 - b), k2 = (1 - a) * b, k3 = a * b;
+  return {k0 * m.p0.x + k1 * m.p1.x + k2 * m.p2.x + k3 * m.p3.x, k0 * m.p0.y + k1 * m.p1.y + k2 * m.p2.y + k3 * m.p3.y,
+          k0 * m.p0.z + k1 * m.p1.z + k2 * m.p2.z + k3 * m.p3.z};
+}
+
+__device__ double tri_coord(const V3* x, double a, double b, double c, int d) {
+  // TrilinearMap.getPoint (:41-64); x[0..7] = x1..x8
+  double v1 = vcomp(x[0], d), v2 = vcomp(x[1], d), v3 = vcomp(x[2], d), v4 = vcomp(x[3], d);
+  double v5 = vcomp(x[4], d), v6 = vcomp(x[5], d), v7 = vcomp(x[6], d), v8 = vcomp(x[7], d);
+  return c * (b * (a * v4 + (1 - a) * v3) + (1 - b) * (a * v2 + (1 - a) * v1)) +
+         (1 - c) * (b * (a * v8 + (1 - a) * v7) + (1 - b) * (a * v6 + (1 - a) * v5));
+}
+
+__device__ double tri_volume(const V3* x) {
+  // TrilinearMap.getVolume (:76-146) including the running sign flip
+  V3 r1 = x[2], r2 = x[3], r3 = x[0], r4 = x[1], r5 = x[6], r6 = x[7], r7 = x[4], r8 = x[5];
+  V3 C[2][2][2];
+  C[0][0][0] = r1;
+  C[1][0][0] = vsub(r2, r1);
+  C[0][1][0] = vsub(r3, r1);
+  C[0][0][1] = vsub(r5, r1);
+  C[1][1][0] = vsub(vadd(r4, r1), vadd(r3, r2));
+  C[0][1][1] = vsub(vadd(r7, r1), vadd(r5, r3));
+  C[1][0][1] = vsub(vadd(r6, r1), vadd(r5, r2));
+  C[1][1][1] = vsub(vadd(r8, vadd(r5, vadd(r3, r2))), vadd(r7, vadd(r6, vadd(r4, r1))));
+  const int perm[6][3] = {{1, 2, 3}, {1, 3, 2}, {2, 1, 3}, {2, 3, 1}, {3, 1, 2}, {3, 2, 1}};
+  double volume = 0.0;
+  for (int q = 0; q < 6; ++q) {
+    const int a = perm[q][0], b = perm[q][1], c = perm[q][2];
+    for (int pb = 0; pb <= 1; pb++)
+      for (int pc = 0; pc <= 1; pc++)
+        for (int qa = 0; qa <= 1; qa++)
+          for (int qc = 0; qc <= 1; qc++)
+            for (int ra = 0; ra <= 1; ra++)
+              for (int rb = 0; rb <= 1; rb++) {
+                double e = vcomp(C[1][pb][pc], a) * vcomp(C[qa][1][qc], b) * vcomp(C[ra][rb][1], c);
+                double d = (double)((qa + ra + 1) * (pb + rb + 1) * (pc + qc + 1));
+                volume += e / d;
+              }
+    int s = 0;
+    for (int i = 0; i < 3; i++)
+      for (int l = 0; l < i; l++)
+        if (perm[q][l] > i) s += 1;
+    volume = ((s & 1) ? -1.0 : 1.0) * volume;
+  }
+  return volume;
+}
+
+__global__ void k_geometry(Grid g, const double* __restrict__ pts, double* ecenter, double* evol, double* iarea,
+                           double* icenter, double* inormal) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel) return;
+  int i, j, k;
+  el_ijk(g, e, i, j, k);
+  int cp[8];
+  elem_points(g, i, j, k, cp);
+  if (g.dim == 3) {
+    // HexCell (:26-51): right-hand ordering -> volume/area ordering
+    V3 x[8] = {ld3(pts, cp[0]), ld3(pts, cp[1]), ld3(pts, cp[3]), ld3(pts, cp[2]),
+               ld3(pts, cp[4]), ld3(pts, cp[5]), ld3(pts, cp[7]), ld3(pts, cp[6])};
+    evol[e] = tri_volume(x);
+    st3(ecenter, e, V3{tri_coord(x, 0.5, 0.5, 0.5, 1), tri_coord(x, 0.5, 0.5, 0.5, 2), tri_coord(x, 0.5, 0.5, 0.5, 3)});
+    const int fidx[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 2, 4, 6}, {1, 3, 5, 7}};
+    const double scale[6] = {1.0, -1.0, -1.0, 1.0, 1.0, -1.0};
+    for (int o = 0; o < 6; ++o) {
+      Bilin b = bilinear(x[fidx[o][0]], x[fidx[o][1]], x[fidx[o][2]], x[fidx[o][3]]);
+      int64_t f = (int64_t)e * 6 + o;
+      iarea[f] = b.area;
+      st3(icenter, f, bilin_point(b, .5, .5));
+      st3(inormal, f, vmul(b.normal, scale[o]));
+    }
+  } else {
+    // QuadCell (:27-95)
+    V3 p0 = ld3(pts, cp[0]), p1 = ld3(pts, cp[1]), p2 = ld3(pts, cp[2]), p3 = ld3(pts, cp[3]);
+    Bilin b = bilinear(p0, p1, p3, p2);
+    st3(ecenter, e, bilin_point(b, .5, .5));
+    evol[e] = b.area;
+    V3 ends[4][2] = {{p0, p1}, {p2, p3}, {p3, p0}, {p1, p2}};
+    for (int o = 0; o < 4; ++o) {
+      V3 a = ends[o][0], c = ends[o][1];
+      double x_ = c.x - a.x, y_ = c.y - a.y;
+      V3 n{y_, -x_, 0};
+      n = vmul(n, 1 / vnorm(n));
+      int64_t f = (int64_t)e * 4 + o;
+      st3(inormal, f, n);
+      iarea[f] = vnorm(vsub(c, a));
+      st3(icenter, f, vmul(vadd(a, c), 0.5));
+    }
+  }
+}
+
+__global__ void k_connections(Grid g, int* conn) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel) return;
+  int i, j, k;
+  el_ijk(g, e, i, j, k);
+  const int nfe = g.dim == 3 ? 6 : 4;
+  for (int o = 1; o < nfe; o += 2) {
+    int ne, no;
+    if (!face_neighbour(g, i, j, k, o, ne, no)) continue;
+    int c = face_connection(g, i, j, k, o);
+    conn[2 * c] = e;
+    conn[2 * c + 1] = ne;
+  }
+}
+
+// ------------------------------------------------------------ dense LU ----
+// netlib dgesv: dgetf2 (idamax pivot, reciprocal scaling, dger update) then
+// dgetrs (dlaswp, unit-lower and non-unit-upper dtrsm with zero skips).
+__device__ int d_dgesv(int n, int nrhs, double* A, int lda, double* B, int ldb) {
+  int ipiv[12];
+  int info = 0;
+  for (int j = 0; j < n; ++j) {
+    int jp = j;
+    double amax = fabs(A[j + j * lda]);
+    for (int i = j + 1; i < n; ++i) {
+      double a = fabs(A[i + j * lda]);
+      if (a > amax) {
+        amax = a;
+        jp = i;
+      }
+    }
+    ipiv[j] = jp;
+    if (A[jp + j * lda] != 0.0) {
+      if (jp != j)
+        for (int c = 0; c < n; ++c) {
+          double t = A[j + c * lda];
+          A[j + c * lda] = A[jp + c * lda];
+          A[jp + c * lda] = t;
+        }
+      if (j < n - 1) {
+        double rp = 1.0 / A[j + j * lda];
+        for (int i = j + 1; i < n; ++i) A[i + j * lda] *= rp;
+      }
+    } else if (info == 0)
+      info = j + 1;
+    if (j < n - 1)
+      for (int c = j + 1; c < n; ++c) {
+        double yv = A[j + c * lda];
+        if (yv != 0.0) {
+          double temp = -1.0 * yv;
+          for (int i = j + 1; i < n; ++i) A[i + c * lda] += A[i + j * lda] * temp;
+        }
+      }
+  }
+  if (info) return info;
+  for (int j = 0; j < n; ++j)
+    if (ipiv[j] != j)
+      for (int c = 0; c < nrhs; ++c) {
+        double t = B[j + c * ldb];
+        B[j + c * ldb] = B[ipiv[j] + c * ldb];
+        B[ipiv[j] + c * ldb] = t;
+      }
+  for (int c = 0; c < nrhs; ++c) {
+    double* bc = B + c * ldb;
+    for (int k = 0; k < n; ++k)
+      if (bc[k] != 0.0)
+        for (int i = k + 1; i < n; ++i) bc[i] -= bc[k] * A[i + k * lda];
+    for (int k = n - 1; k >= 0; --k)
+      if (bc[k] != 0.0) {
+        bc[k] = bc[k] / A[k + k * lda];
+        for (int i = 0; i < k; ++i) bc[i] -= bc[k] * A[i + k * lda];
+      }
+  }
+  return 0;
+}
+
+constexpr int TLD = 12;  // leading dimension of the per-point T store
+constexpr int TSZ = 96;  // 12 local connections x 8 elements
+
+// MPFA.calculateNormalArea (:314-354) for the face at position f of point p
+__device__ V3 normal_area(const Grid& g, const PointTopo& t, int f, int p, const double* pts, const double* inormal,
+                          const double* iarea) {
+  const int face = t.face[f];
+  if (g.dim == 2) return vmul(ld3(inormal, face), -iarea[face] / 2);
+  int cp[8], ip[4];
+  const int a = t.fel[f];
+  elem_points(g, t.eijk[a][0], t.eijk[a][1], t.eijk[a][2], cp);
+  face_points(g, cp, t.fo[f], ip);
+  int i = 0;
+  for (int q = 0; q < 4; ++q)
+    if (ip[q] == p) {
+      i = q;
+      break;
+    }
+  V3 x1 = ld3(pts, ip[i]);
+  V3 x2 = ld3(pts, ip[i == 0 ? 3 : (i - 1) % 4]);
+  V3 x3 = ld3(pts, ip[(i + 1) % 4]);
+  V3 x4 = ld3(pts, ip[(i + 2) % 4]);
+  V3 v21 = vsub(x2, x1), v31 = vsub(x3, x1), v42 = vsub(x4, x2), v43 = vsub(x4, x3);
+  V3 n1 = vmul(vcross(v21, v31), 9);
+  V3 n2 = vmul(vcross(v21, v42), 3);
+  V3 n3 = vmul(vcross(v43, v31), 3);
+  V3 n4 = vcross(v43, v42);
+  return vmul(vadd(vadd(vadd(n1, n2), n3), n4), 1. / 64.);
+}
+
+// OmethodInteractionRegion.calculateT (O_MPFA.java:193-239) per corner point;
+// stores T = C (A\B) - D (column major, ld 12) and flags singular regions.
+__global__ void __launch_bounds__(128) k_mpfa_point(Grid g, const double* __restrict__ pts,
+                                                    const double* __restrict__ perm, const double* __restrict__ ecenter,
+                                                    const double* __restrict__ icenter,
+                                                    const double* __restrict__ inormal,
+                                                    const double* __restrict__ iarea, double continuity,
+                                                    double* __restrict__ Tstore, int* flag) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  PointTopo t;
+  point_topology(g, p, t);
+  const int nc = t.nconn, ne = t.ne;
+  double A[TLD * TLD], B[TLD * 8], C[TLD * TLD], D[TLD * 8];
+  for (int q = 0; q < TLD * TLD; ++q) A[q] = C[q] = 0;
+  for (int q = 0; q < TLD * 8; ++q) B[q] = D[q] = 0;
+  const V3 corner = ld3(pts, p);
+  const int per = g.dim == 3 ? 3 : 2;  // interfaces of one element at the point
+  for (int a = 0; a < ne; ++a) {
+    const int el = t.el[a];
+    const int f0 = a * per;  // faces of element a occupy positions f0..f0+per-1
+    const int n = per + 1;
+    double Ab[16], Psi[16];
+    for (int q = 0; q < 16; ++q) Ab[q] = Psi[q] = 0;
+    V3 ec = ld3(ecenter, el);
+    Ab[0] = 1;
+    Ab[0 + 1 * n] = ec.x;
+    Ab[0 + 2 * n] = ec.y;
+    if (n == 4) Ab[0 + 3 * n] = ec.z;
+    for (int i = 0; i < per; ++i) {
+      V3 cp = ld3(icenter, t.face[f0 + i]);
+      if (continuity != 1)
+        cp = {(cp.x - corner.x) * continuity + corner.x, (cp.y - corner.y) * continuity + corner.y,
+              (cp.z - corner.z) * continuity + corner.z};
+      Ab[(i + 1)] = 1;
+      Ab[(i + 1) + 1 * n] = cp.x;
+      Ab[(i + 1) + 2 * n] = cp.y;
+      if (n == 4) Ab[(i + 1) + 3 * n] = cp.z;
+    }
+    for (int i = 0; i < n; ++i) Psi[i + i * n] = 1;
+    if (d_dgesv(n, n, Ab, n, Psi, n) != 0) {
+      atomicCAS(flag, 0, 1);
+      return;
+    }
+    V3 grad[4];
+    for (int i = 0; i < n; ++i) grad[i] = {Psi[1 + i * n], Psi[2 + i * n], n == 4 ? Psi[3 + i * n] : 0.0};
+    const double* K = perm + 6 * (int64_t)el;
+    const double kxx = K[0], kyy = K[1], kzz = K[2], kxy = K[3], kxz = K[4], kyz = K[5];
+    V3 Kn[3];
+    for (int i = 0; i < per; ++i) {
+      V3 v = normal_area(g, t, f0 + i, p, pts, inormal, iarea);
+      Kn[i] = {kxx * v.x + kxy * v.y + kxz * v.z, kxy * v.x + kyy * v.y + kyz * v.z, kxz * v.x + kyz * v.y + kzz * v.z};
+    }
+    // assembleElementContribution (O_MPFA.java:422-457)
+    for (int i = 0; i < per; ++i) {
+      double f = vdot(Kn[i], grad[0]);
+      const int fi = f0 + i;
+      const int is = t.lidx[fi];
+      const bool isHere = t.boundary[fi] ? true : (t.fo[fi] & 1);
+      B[is + a * TLD] += -f;
+      if (isHere) D[is + a * TLD] += -f;
+      for (int j = 1; j < per + 1; j++) {
+        f = vdot(Kn[i], grad[j]);
+        const int js = t.lidx[f0 + j - 1];
+        A[is + js * TLD] += f;
+        if (isHere) C[is + js * TLD] += f;
+      }
+    }
+  }
+  // T = C * (A \ B) - D (MPFA.java:43-54)
+  if (d_dgesv(nc, ne, A, TLD, B, TLD) != 0) {
+    atomicCAS(flag, 0, 2);
+    return;
+  }
+  double* T = Tstore + (int64_t)p * TSZ;
+  for (int j = 0; j < ne; ++j)
+    for (int i = 0; i < nc; ++i) {
+      double acc = D[i + j * TLD] * -1;
+      T[i + j * TLD] = acc;
+    }
+  for (int j = 0; j < ne; ++j)
+    for (int l = 0; l < nc; ++l) {
+      double bl = B[l + j * TLD];
+      if (bl != 0.0) {
+        double temp = 1.0 * bl;
+        for (int i = 0; i < nc; ++i) T[i + j * TLD] += temp * C[i + l * TLD];
+      }
+    }
+}
+
+// storeTransmissibilities (O_MPFA.java:88-112) gathered per connection over
+// its corner points in ascending point order, then Connection.check
+// (geometry/Connection.java:80-107).
+__global__ void k_mpfa_gather(Grid g, int maxmd, const double* __restrict__ Tstore, const int* __restrict__ conn,
+                              int* md_len, int* md_elem, double* md_k, int* flag) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nconn) return;
+  const int here = conn[2 * c], there = conn[2 * c + 1];
+  int i, j, k;
+  el_ijk(g, here, i, j, k);
+  const int nfe = g.dim == 3 ? 6 : 4;
+  int o = -1;
+  for (int q = 1; q < nfe; q += 2) {
+    int ne, no;
+    if (face_neighbour(g, i, j, k, q, ne, no) && ne == there) {
+      o = q;
+      break;
+    }
+  }
+  const int fh = here * nfe + o;
+  int cp[8], ip[4];
+  elem_points(g, i, j, k, cp);
+  const int np = face_points(g, cp, o, ip);
+  // ascending point order
+  for (int a = 1; a < np; ++a)
+    for (int b = a; b > 0 && ip[b] < ip[b - 1]; --b) {
+      int tmp = ip[b];
+      ip[b] = ip[b - 1];
+      ip[b - 1] = tmp;
+    }
+  int el[18];
+  double kk[18];
+  int n = 0;
+  PointTopo t;
+  for (int a = 0; a < np; ++a) {
+    const int p = ip[a];
+    point_topology(g, p, t);
+    int li = -1;
+    for (int f = 0; f < t.nf; ++f)
+      if (t.face[f] == fh) {
+        li = t.lidx[f];
+        break;
+      }
+    if (li < 0 || li >= TLD) {
+      atomicCAS(flag, 0, 5);
+      return;
+    }
+    const double* T = Tstore + (int64_t)p * TSZ;
+    for (int e = 0; e < t.ne; ++e) {
+      double tk = T[li + e * TLD];
+      bool found = false;
+      for (int q = 0; q < n; ++q)
+        if (el[q] == t.el[e]) {
+          found = true;
+          kk[q] += tk;
+          break;
+        }
+      if (!found && tk != 0) {
+        if (n >= maxmd) {
+          atomicCAS(flag, 0, 3);
+          return;
+        }
+        el[n] = t.el[e];
+        kk[n] = tk;
+        n++;
+      }
+    }
+  }
+  double sum = 0;
+  bool hasHere = false, hasThere = false;
+  for (int q = 0; q < n; ++q) {
+    sum += kk[q];
+    hasHere |= el[q] == here;
+    hasThere |= el[q] == there;
+  }
+  if (fabs(sum) > 1.0e-6 || !hasHere || !hasThere) atomicCAS(flag, 0, 4);
+  md_len[c] = n;
+  for (int q = 0; q < n; ++q) {
+    md_elem[(int64_t)c * maxmd + q] = el[q];
+    md_k[(int64_t)c * maxmd + q] = kk[q] * 1.0;  // connection multiplier (1 on structured grids)
+  }
+}
+
+__global__ void k_md_compact(int nconn, int maxmd, const int* __restrict__ ptr, const int* __restrict__ el_in,
+                             const double* __restrict__ k_in, int* el_out, double* k_out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nconn) return;
+  for (int q = ptr[c]; q < ptr[c + 1]; ++q) {
+    el_out[q] = el_in[(int64_t)c * maxmd + (q - ptr[c])];
+    k_out[q] = k_in[(int64_t)c * maxmd + (q - ptr[c])];
+  }
+}
+
+// cell -> incident connections, ascending
+__global__ void k_cell_conns(Grid g, int* cptr_fixed /* nel * 6 */, int* ccount) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.nel) return;
+  int i, j, k;
+  el_ijk(g, e, i, j, k);
+  const int nfe = g.dim == 3 ? 6 : 4;
+  int cs[6], n = 0;
+  for (int o = 0; o < nfe; ++o) {
+    int ne, no;
+    if (!face_neighbour(g, i, j, k, o, ne, no)) continue;
+    int c = face_connection(g, i, j, k, o);
+    // side flag in the sign bit region: store c*2 + (here ? 0 : 1)
+    cs[n++] = 2 * c + ((o & 1) ? 0 : 1);
+  }
+  for (int a = 1; a < n; ++a)
+    for (int b = a; b > 0 && cs[b] < cs[b - 1]; --b) {
+      int tmp = cs[b];
+      cs[b] = cs[b - 1];
+      cs[b - 1] = tmp;
+    }
+  for (int a = 0; a < 6; ++a) cptr_fixed[(int64_t)e * 6 + a] = a < n ? cs[a] : -1;
+  ccount[e] = n;
+}
+
+// Row pattern: diagonal (optional) plus MD elements of incident connections.
+template <bool FILL>
+__global__ void k_rows(int nel, int with_diag, const int* __restrict__ cc, const int* __restrict__ ccount,
+                       const int* __restrict__ md_ptr, const int* __restrict__ md_el, int* row_len,
+                       const int* __restrict__ row_ptr, int* col) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  int buf[128];
+  int n = 0;
+  if (with_diag) buf[n++] = e;
+  for (int a = 0; a < ccount[e]; ++a) {
+    int c = cc[(int64_t)e * 6 + a] >> 1;
+    for (int q = md_ptr[c]; q < md_ptr[c + 1] && n < 128; ++q) buf[n++] = md_el[q];
+  }
+  for (int a = 1; a < n; ++a)
+    for (int b = a; b > 0 && buf[b] < buf[b - 1]; --b) {
+      int tmp = buf[b];
+      buf[b] = buf[b - 1];
+      buf[b - 1] = tmp;
+    }
+  int m = 0;
+  for (int a = 0; a < n; ++a)
+    if (a == 0 || buf[a] != buf[a - 1]) {
+      if (FILL) col[row_ptr[e] + m] = buf[a];
+      m++;
+    }
+  if (!FILL) row_len[e] = m;
+}
+
+__device__ int bsearch_pos(const int* col, int lo, int hi, int key) {
+  hi -= 1;
+  while (lo <= hi) {
+    int mid = (lo + hi) >> 1;
+    int v = col[mid];
+    if (v < key) lo = mid + 1;
+    else if (v > key) hi = mid - 1;
+    else return mid;
+  }
+  return -1;
+}
+
+__global__ void k_md_pos(int nconn, const int* __restrict__ conn, const int* __restrict__ md_ptr,
+                         const int* __restrict__ md_el, const int* __restrict__ rp, const int* __restrict__ col,
+                         int* pos_here, int* pos_there) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nconn) return;
+  int h = conn[2 * c], t = conn[2 * c + 1];
+  for (int q = md_ptr[c]; q < md_ptr[c + 1]; ++q) {
+    pos_here[q] = bsearch_pos(col, rp[h], rp[h + 1], md_el[q]);
+    pos_there[q] = bsearch_pos(col, rp[t], rp[t + 1], md_el[q]);
+  }
+}
+
+// PotentialCalculator.discretizeFlux, gathered per row in connection order.
+__global__ void k_potential_rows(int nel, const int* __restrict__ cc, const int* __restrict__ ccount,
+                                 const int* __restrict__ md_ptr, const int* __restrict__ md_el,
+                                 const double* __restrict__ md_k, const int* __restrict__ rp,
+                                 const int* __restrict__ col, double* val) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  for (int q = rp[e]; q < rp[e + 1]; ++q) val[q] = 0;
+  for (int a = 0; a < ccount[e]; ++a) {
+    int code = cc[(int64_t)e * 6 + a];
+    int c = code >> 1;
+    bool here = !(code & 1);
+    for (int q = md_ptr[c]; q < md_ptr[c + 1]; ++q) {
+      int pos = bsearch_pos(col, rp[e], rp[e + 1], md_el[q]);
+      if (pos >= 0) val[pos] += here ? md_k[q] : -md_k[q];
+    }
+  }
+}
+
+}  // namespace
+
+static void make_grid(Grid& g, int dim, int ni, int nj, int nk) {
+  g.dim = dim;
+  g.ni = ni;
+  g.nj = nj;
+  g.nk = dim == 3 ? nk : 0;
+  g.npi = ni + 1;
+  g.npj = nj + 1;
+  g.npk = dim == 3 ? nk + 1 : 1;
+  g.npts = g.npi * g.npj * g.npk;
+  g.nel = dim == 3 ? ni * nj * nk : ni * nj;
+  g.nfacepe = dim == 3 ? 6 : 4;
+  g.nintf = g.nel * g.nfacepe;
+  g.nconn = dim == 3 ? 3 * ni * nj * nk - ni * nj - ni * nk - nj * nk : 2 * ni * nj - ni - nj;
+}
+
+static void scan_lengths(const std::vector<int>& len, std::vector<int>& ptr) {
+  ptr.assign(len.size() + 1, 0);
+  for (size_t i = 0; i < len.size(); ++i) ptr[i + 1] = ptr[i] + len[i];
+}
+
+void Mesh::build_patterns() {
+  Context& c = *ctx;
+  const int n = g.nel;
+  DeviceBuffer<int> cc((size_t)n * 6), ccount(n);
+  RSG_LAUNCH(c, "cell_conns", k_cell_conns, blocks_for(n, 256), 256, 0, g, cc.get(), ccount.get());
+  DeviceBuffer<int> len(n);
+  auto one = [&](int with_diag, std::vector<int>& hrow, std::vector<int>& hcol, DeviceBuffer<int>& drow,
+                 DeviceBuffer<int>& dcol) {
+    RSG_LAUNCH(c, "pattern_rows", k_rows<false>, blocks_for(n, 128), 128, 0, n, with_diag, cc.get(), ccount.get(),
+               md_ptr.get(), md_elem.get(), len.get(), (const int*)nullptr, (int*)nullptr);
+    std::vector<int> hl(n);
+    RSG_CUDA(cudaMemcpyAsync(hl.data(), len.get(), sizeof(int) * n, cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    scan_lengths(hl, hrow);
+    drow.resize(n + 1);
+    dcol.resize(std::max(hrow[n], 1));
+    RSG_CUDA(cudaMemcpyAsync(drow.get(), hrow.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, c.stream));
+    RSG_LAUNCH(c, "pattern_rows", k_rows<true>, blocks_for(n, 128), 128, 0, n, with_diag, cc.get(), ccount.get(),
+               md_ptr.get(), md_elem.get(), len.get(), drow.get(), dcol.get());
+    hcol.resize(hrow[n]);
+    RSG_CUDA(cudaMemcpyAsync(hcol.data(), dcol.get(), sizeof(int) * hrow[n], cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+  };
+  DeviceBuffer<int> prow, pcol, qrow, qcol;
+  one(1, h_prow, h_pcol, prow, pcol);
+  one(0, h_qrow, h_qcol, qrow, qcol);
+  md_pos_here.resize(std::max<int64_t>(nmd, 1));
+  md_pos_there.resize(std::max<int64_t>(nmd, 1));
+  RSG_LAUNCH(c, "md_pos", k_md_pos, blocks_for(g.nconn, 128), 128, 0, g.nconn, conn.get(), md_ptr.get(),
+             md_elem.get(), prow.get(), pcol.get(), md_pos_here.get(), md_pos_there.get());
+  cell_conn_ptr = std::move(ccount);
+  cell_conn = std::move(cc);
+  c.sync();
+}
+
+}  // namespace rsg
+
+using rsg::guarded;
+
+extern "C" {
+
+rsg_status rsg_mesh_create_structured(rsg_ctx* ctx, int32_t dim, int32_t ni, int32_t nj, int32_t nk,
+                                      const double* coords, double x0, double y0, double z0, double dx, double dy,
+                                      double dz, const double* perm, rsg_mesh** out) {
+  if (!ctx || !out || !perm) return RSG_BAD_ARG;
+  if ((dim != 2 && dim != 3) || ni <= 0 || nj <= 0 || (dim == 3 && nk <= 0)) return RSG_BAD_ARG;
+  *out = nullptr;
+  rsg_mesh* h = new rsg_mesh();
+  rsg_status st = guarded(&ctx->c, [&] {
+    rsg::Mesh& m = h->m;
+    m.ctx = &ctx->c;
+    rsg::make_grid(m.g, dim, ni, nj, nk);
+    const rsg::Grid& g = m.g;
+    if ((int64_t)g.nel * 6 > INT32_MAX) throw rsg::Error(RSG_UNSUPPORTED, "grid too large");
+    m.maxmd = dim == 3 ? 18 : 6;
+    std::vector<double> p((size_t)g.npts * 3);
+    if (coords) std::copy(coords, coords + p.size(), p.begin());
+    else
+      for (int k = 0; k < g.npk; ++k)
+        for (int j = 0; j < g.npj; ++j)
+          for (int i = 0; i < g.npi; ++i) {
+            double x = x0, y = y0, z = (dim == 3) ? z0 : 0.0;
+            for (int a = 0; a < i; ++a) x += dx;
+            for (int a = 0; a < j; ++a) y += dy;
+            if (dim == 3)
+              for (int a = 0; a < k; ++a) z += dz;
+            size_t q = (size_t)i + (size_t)j * g.npi + (size_t)k * g.npi * g.npj;
+            p[3 * q] = x;
+            p[3 * q + 1] = y;
+            p[3 * q + 2] = z;
+          }
+    rsg::Context& c = ctx->c;
+    m.pts.resize(p.size());
+    m.perm.resize((size_t)g.nel * 6);
+    RSG_CUDA(cudaMemcpyAsync(m.pts.get(), p.data(), sizeof(double) * p.size(), cudaMemcpyHostToDevice, c.stream));
+    RSG_CUDA(cudaMemcpyAsync(m.perm.get(), perm, sizeof(double) * g.nel * 6, cudaMemcpyHostToDevice, c.stream));
+    m.ecenter.resize((size_t)g.nel * 3);
+    m.evol.resize(g.nel);
+    m.iarea.resize(g.nintf);
+    m.icenter.resize((size_t)g.nintf * 3);
+    m.inormal.resize((size_t)g.nintf * 3);
+    m.conn.resize((size_t)g.nconn * 2);
+    RSG_LAUNCH(c, "geometry", rsg::k_geometry, rsg::blocks_for(g.nel, 128), 128, 0, g, m.pts.get(), m.ecenter.get(),
+               m.evol.get(), m.iarea.get(), m.icenter.get(), m.inormal.get());
+    RSG_LAUNCH(c, "connections", rsg::k_connections, rsg::blocks_for(g.nel, 256), 256, 0, g, m.conn.get());
+    m.h_conn.resize((size_t)g.nconn * 2);
+    RSG_CUDA(cudaMemcpyAsync(m.h_conn.data(), m.conn.get(), sizeof(int) * m.h_conn.size(), cudaMemcpyDeviceToHost,
+                             c.stream));
+    c.sync();
+  });
+  if (st != RSG_OK) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return RSG_OK;
+}
+
+rsg_status rsg_mesh_destroy(rsg_mesh* m) {
+  if (!m) return RSG_BAD_ARG;
+  if (m->m.ctx) cudaStreamSynchronize(m->m.ctx->stream);
+  delete m;
+  return RSG_OK;
+}
+
+rsg_status rsg_mesh_compute_mpfa(rsg_mesh* mh, double continuity) {
+  if (!mh) return RSG_BAD_ARG;
+  if (continuity > 1 || continuity <= 0) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  return guarded(m.ctx, [&] {
+    rsg::Context& c = *m.ctx;
+    const rsg::Grid& g = m.g;
+    rsg::DeviceBuffer<double> T((size_t)g.npts * rsg::TSZ);
+    rsg::DeviceBuffer<int> flag(1), mdlen(g.nconn), mdel((size_t)g.nconn * m.maxmd);
+    rsg::DeviceBuffer<double> mdk((size_t)g.nconn * m.maxmd);
+    RSG_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), c.stream));
+    RSG_LAUNCH(c, "mpfa_point", rsg::k_mpfa_point, rsg::blocks_for(g.npts, 128), 128, 0, g, m.pts.get(), m.perm.get(),
+               m.ecenter.get(), m.icenter.get(), m.inormal.get(), m.iarea.get(), continuity, T.get(), flag.get());
+    RSG_LAUNCH(c, "mpfa_gather", rsg::k_mpfa_gather, rsg::blocks_for(g.nconn, 128), 128, 0, g, m.maxmd, T.get(),
+               m.conn.get(), mdlen.get(), mdel.get(), mdk.get(), flag.get());
+    int hf = 0;
+    std::vector<int> hl(g.nconn);
+    RSG_CUDA(cudaMemcpyAsync(&hf, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    RSG_CUDA(cudaMemcpyAsync(hl.data(), mdlen.get(), sizeof(int) * g.nconn, cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    if (hf == 1) throw rsg::Error(RSG_SINGULAR, "Severe grid distortion (singular basis system)");
+    if (hf == 2) throw rsg::Error(RSG_SINGULAR, "Conductivity tensor does not appear to be symmetrical, positive definite");
+    if (hf == 3) throw rsg::Error(RSG_BAD_ARG, "too many transmissibilities on a connection");
+    if (hf == 4) throw rsg::Error(RSG_BAD_ARG, "Transmissibilities on a connection fail the consistency check");
+    if (hf == 5) throw rsg::Error(RSG_BAD_ARG, "interaction region lookup failed");
+    rsg::scan_lengths(hl, m.h_md_ptr);
+    m.nmd = m.h_md_ptr[g.nconn];
+    m.md_ptr.resize(g.nconn + 1);
+    m.md_elem.resize(std::max<int64_t>(m.nmd, 1));
+    m.md_k.resize(std::max<int64_t>(m.nmd, 1));
+    RSG_CUDA(cudaMemcpyAsync(m.md_ptr.get(), m.h_md_ptr.data(), sizeof(int) * (g.nconn + 1), cudaMemcpyHostToDevice,
+                             c.stream));
+    RSG_LAUNCH(c, "md_compact", rsg::k_md_compact, rsg::blocks_for(g.nconn, 256), 256, 0, g.nconn, m.maxmd,
+               m.md_ptr.get(), mdel.get(), mdk.get(), m.md_elem.get(), m.md_k.get());
+    m.h_md_elem.resize(m.nmd);
+    RSG_CUDA(cudaMemcpyAsync(m.h_md_elem.data(), m.md_elem.get(), sizeof(int) * m.nmd, cudaMemcpyDeviceToHost,
+                             c.stream));
+    c.sync();
+    m.have_md = true;
+    m.build_patterns();
+  });
+}
+
+rsg_status rsg_mesh_get_counts(rsg_mesh* mh, int64_t* counts) {
+  if (!mh || !counts) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  counts[0] = m.g.nel;
+  counts[1] = m.g.nconn;
+  counts[2] = m.nmd;
+  counts[3] = m.g.npts;
+  counts[4] = m.h_pcol.size();
+  return RSG_OK;
+}
+
+rsg_status rsg_mesh_get_geometry(rsg_mesh* mh, double* centers, double* volumes) {
+  if (!mh) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  return guarded(m.ctx, [&] {
+    if (centers)
+      RSG_CUDA(cudaMemcpyAsync(centers, m.ecenter.get(), sizeof(double) * 3 * m.g.nel, cudaMemcpyDeviceToHost,
+                               m.ctx->stream));
+    if (volumes)
+      RSG_CUDA(cudaMemcpyAsync(volumes, m.evol.get(), sizeof(double) * m.g.nel, cudaMemcpyDeviceToHost, m.ctx->stream));
+    m.ctx->sync();
+  });
+}
+
+rsg_status rsg_mesh_get_connections(rsg_mesh* mh, int32_t* conn) {
+  if (!mh || !conn) return RSG_BAD_ARG;
+  std::copy(mh->m.h_conn.begin(), mh->m.h_conn.end(), conn);
+  return RSG_OK;
+}
+
+rsg_status rsg_mesh_get_transmissibilities(rsg_mesh* mh, int32_t* md_ptr, int32_t* md_elem, double* md_k) {
+  if (!mh) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  if (!m.have_md) return RSG_BAD_ARG;
+  return guarded(m.ctx, [&] {
+    if (md_ptr) std::copy(m.h_md_ptr.begin(), m.h_md_ptr.end(), md_ptr);
+    if (md_elem) std::copy(m.h_md_elem.begin(), m.h_md_elem.end(), md_elem);
+    if (md_k)
+      RSG_CUDA(cudaMemcpyAsync(md_k, m.md_k.get(), sizeof(double) * m.nmd, cudaMemcpyDeviceToHost, m.ctx->stream));
+    m.ctx->sync();
+  });
+}
+
+rsg_status rsg_mesh_get_pattern(rsg_mesh* mh, int32_t which, int32_t* row_ptr, int32_t* col, int64_t* nnz) {
+  if (!mh || (which != 0 && which != 1)) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  if (!m.have_md) return RSG_BAD_ARG;
+  const auto& r = which == 0 ? m.h_prow : m.h_qrow;
+  const auto& c = which == 0 ? m.h_pcol : m.h_qcol;
+  if (nnz) *nnz = (int64_t)c.size();
+  if (row_ptr) std::copy(r.begin(), r.end(), row_ptr);
+  if (col) std::copy(c.begin(), c.end(), col);
+  return RSG_OK;
+}
+
+rsg_status rsg_mesh_assemble_potential(rsg_mesh* mh, rsg_csr* A) {
+  if (!mh || !A) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  if (!m.have_md) return RSG_BAD_ARG;
+  return guarded(m.ctx, [&] {
+    if (A->m.n != m.g.nel || A->m.h_col != m.h_qcol)
+      throw rsg::Error(RSG_OUT_OF_PATTERN, "matrix does not have the potential pattern of this mesh");
+    RSG_LAUNCH(*m.ctx, "potential_rows", rsg::k_potential_rows, rsg::blocks_for(m.g.nel, 128), 128, 0, m.g.nel,
+               m.cell_conn.get(), m.cell_conn_ptr.get(), m.md_ptr.get(), m.md_elem.get(), m.md_k.get(),
+               A->m.rowptr.get(), A->m.col.get(), A->m.val.get());
+    A->m.sell_dirty = true;
+    m.ctx->sync();
+  });
+}
+
+}  // extern "C"

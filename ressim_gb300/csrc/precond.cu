@@ -1,0 +1,635 @@
+// Preconditioners: ILU(0) (mtj/src/no/uib/cipr/matrix/sparse/ILU.java:54-140
+// with UnitLowerCompRowMatrix.java:48-86 and UpperCompRowMatrix.java:48-90),
+// SSOR (sparse/SSOR.java:126-194) and the diagonal preconditioner
+// (sparse/DiagonalPreconditioner.java:44-78).
+//
+// The sequential sweeps are level scheduled: rows are grouped by the depth
+// of their dependency chain, every row is computed by one thread that sums
+// its entries in CSR order (so each row's arithmetic equals the Java loop),
+// and one thread-block cluster walks the levels with a hardware cluster
+// barrier between them.  Coefficients are stored per level as SELL-32 slices
+// so the loads of a warp are contiguous.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
+#include "linalg.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace rsg {
+
+enum SweepKind { SW_ILU_LOWER = 0, SW_ILU_UPPER = 1, SW_SSOR_FWD = 2, SW_SSOR_BWD = 3, SW_ILU_LOWER_T = 4 };
+
+template <typename T>
+struct SweepArgs {
+  int nlev;
+  const int* level_slices;
+  const int* slice_base;
+  const int* row;
+  const int* len;
+  const int* col;
+  const T* val;
+  const T* diag;
+  const T* b;
+  T* x;   // output / in-place vector
+  T* xx;  // SSOR half iterate
+  T omega;
+  const int* active;
+};
+
+__device__ __forceinline__ double ld_l2(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_l2(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ void st_l2(double* p, double v) { __stcg(p, v); }
+__device__ __forceinline__ void st_l2(float* p, float v) { __stcg(p, v); }
+
+template <int KIND, typename T>
+__device__ __forceinline__ void sweep_row(const SweepArgs<T>& a, int slot, int row, int s) {
+  const int base = a.slice_base[s] + (slot & 31);
+  const int len = a.len[slot];
+  T sum = 0;
+  if (KIND == SW_SSOR_FWD || KIND == SW_SSOR_BWD) {
+    // sigma over the full row without the diagonal, CSR order; lower
+    // columns read the half iterate xx, upper columns read x.
+#pragma unroll 4
+    for (int k = 0; k < len; ++k) {
+      int q = base + 32 * k;
+      int c = a.col[q];
+      T v = (c < row) ? ld_l2(a.xx + c) : ld_l2(a.x + c);
+      sum += a.val[q] * v;
+    }
+    T d = a.diag[slot];
+    T sigma = (a.b[row] - sum) / d;
+    if (KIND == SW_SSOR_FWD) {
+      T xo = ld_l2(a.x + row);
+      st_l2(a.xx + row, xo + a.omega * (sigma - xo));
+    } else {
+      T xh = ld_l2(a.xx + row);
+      st_l2(a.x + row, xh + a.omega * (sigma - xh));
+    }
+    return;
+  }
+#pragma unroll 4
+  for (int k = 0; k < len; ++k) {
+    int q = base + 32 * k;
+    sum += a.val[q] * ld_l2(a.x + a.col[q]);
+  }
+  if (KIND == SW_ILU_LOWER) st_l2(a.x + row, a.b[row] - sum);
+  else st_l2(a.x + row, (a.b[row] - sum) / a.diag[slot]);
+}
+
+// One cluster walks all levels.  Every CTA of the cluster evaluates the same
+// early-exit test, so either all of them reach each barrier or none does.
+template <int KIND, typename T>
+__global__ void __launch_bounds__(512) k_sweep_cluster(SweepArgs<T> a) {
+  if (a.active && *a.active != 0) return;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int wpc = blockDim.x >> 5;
+  const int gwarp = (int)cluster.block_rank() * wpc + (threadIdx.x >> 5);
+  const int nwarps = (int)cluster.num_blocks() * wpc;
+  const int lane = threadIdx.x & 31;
+  for (int l = 0; l < a.nlev; ++l) {
+    const int s1 = a.level_slices[l + 1];
+    for (int s = a.level_slices[l] + gwarp; s < s1; s += nwarps) {
+      const int slot = s * 32 + lane;
+      const int row = a.row[slot];
+      if (row >= 0) sweep_row<KIND, T>(a, slot, row, s);
+    }
+    cluster.sync();
+  }
+}
+
+// Fallback: one launch per level.
+template <int KIND, typename T>
+__global__ void k_sweep_level(SweepArgs<T> a, int l) {
+  if (a.active && *a.active != 0) return;
+  const int s = a.level_slices[l] + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (s >= a.level_slices[l + 1]) return;
+  const int slot = s * 32 + (threadIdx.x & 31);
+  const int row = a.row[slot];
+  if (row >= 0) sweep_row<KIND, T>(a, slot, row, s);
+}
+
+// ILU(0) factorisation, one thread per row, rows of a level in parallel.
+// Row k reads only rows of earlier levels (its lower neighbours), which are
+// final once the barrier of their level has passed.
+struct FactorArgs {
+  int nlev;
+  const int* level_slices;
+  const int* row;
+  const int* rowptr;
+  const int* col;
+  const int* diag;
+  double* data;
+  int* flag;  // first zero-pivot row + 1
+};
+
+__device__ __forceinline__ void factor_row(const FactorArgs& a, int k) {
+  const int r0 = a.rowptr[k], r1 = a.rowptr[k + 1], dk = a.diag[k];
+  for (int i = r0; i < dk; ++i) {
+    const int index = a.col[i];
+    const double LUii = ld_l2(a.data + a.diag[index]);
+    if (LUii == 0) atomicCAS(a.flag, 0, i + 1);
+    const double LUki = ld_l2(a.data + i) / LUii;
+    st_l2(a.data + i, LUki);
+    const int j1 = a.rowptr[index + 1];
+    int l = r0 + 1;
+    for (int j = a.diag[index] + 1; j < j1; ++j) {
+      const int cj = a.col[j];
+      while (l < r1 && a.col[l] < cj) l++;
+      if (l < r1 && a.col[l] == cj) st_l2(a.data + l, ld_l2(a.data + l) - LUki * ld_l2(a.data + j));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(512) k_factor_cluster(FactorArgs a) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int nthreads = (int)cluster.num_blocks() * blockDim.x;
+  const int t = (int)cluster.block_rank() * blockDim.x + threadIdx.x;
+  for (int l = 0; l < a.nlev; ++l) {
+    const int r0 = a.level_slices[l] * 32, r1 = a.level_slices[l + 1] * 32;
+    for (int slot = r0 + t; slot < r1; slot += nthreads) {
+      const int k = a.row[slot];
+      if (k >= 0) factor_row(a, k);
+    }
+    cluster.sync();
+  }
+}
+
+__global__ void k_factor_level(FactorArgs a, int l) {
+  const int slot = a.level_slices[l] * 32 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= a.level_slices[l + 1] * 32) return;
+  const int k = a.row[slot];
+  if (k >= 0) factor_row(a, k);
+}
+
+template <typename T>
+__global__ void k_plan_gather(int64_t size, const int* __restrict__ src, const double* __restrict__ v,
+                              T* __restrict__ out) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= size) return;
+  int s = src[q];
+  out[q] = s >= 0 ? (T)v[s] : (T)0;
+}
+
+__global__ void k_copy(int64_t n, const double* __restrict__ a, double* __restrict__ b) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+__global__ void k_invdiag(int n, const int* __restrict__ diag, const double* __restrict__ val, double* inv,
+                          float* invf, int* flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double d = diag[i] >= 0 ? val[diag[i]] : 0.0;
+  if (d == 0) atomicCAS(flag, 0, i + 1);
+  inv[i] = 1 / d;
+  invf[i] = (float)(1 / d);
+}
+
+template <typename T>
+__global__ void k_diag_apply(int n, const T* __restrict__ inv, const T* __restrict__ b, T* __restrict__ x,
+                             const int* active) {
+  if (active && *active != 0) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = b[i] * inv[i];
+}
+
+// ------------------------------------------------------------ planning ----
+// entries: 0 lower part, 1 upper part, 2 full row without the diagonal.
+// upper_levels: schedule by dependencies on higher rows (backward sweeps).
+static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, bool with_diag) {
+  const int n = A.n;
+  const auto& rp = A.h_rowptr;
+  const auto& cl = A.h_col;
+  const auto& dg = A.h_diag;
+  std::vector<int> lev(n, 0);
+  if (!upper_levels) {
+    for (int i = 0; i < n; ++i) {
+      int L = 0;
+      for (int q = rp[i]; q < rp[i + 1] && cl[q] < i; ++q) L = std::max(L, lev[cl[q]] + 1);
+      lev[i] = L;
+    }
+  } else {
+    for (int i = n - 1; i >= 0; --i) {
+      int L = 0;
+      for (int q = rp[i + 1] - 1; q >= rp[i] && cl[q] > i; --q) L = std::max(L, lev[cl[q]] + 1);
+      lev[i] = L;
+    }
+  }
+  int nlev = 0;
+  for (int i = 0; i < n; ++i) nlev = std::max(nlev, lev[i] + 1);
+  std::vector<int> cnt(nlev + 1, 0);
+  for (int i = 0; i < n; ++i) cnt[lev[i] + 1]++;
+  for (int l = 0; l < nlev; ++l) cnt[l + 1] += cnt[l];
+  std::vector<int> order(n), fill(cnt.begin(), cnt.end() - 1);
+  for (int i = 0; i < n; ++i) order[fill[lev[i]]++] = i;  // ascending row within a level
+  // slices per level
+  std::vector<int> level_slices(nlev + 1, 0);
+  for (int l = 0; l < nlev; ++l) {
+    int rows = cnt[l + 1] - cnt[l];
+    level_slices[l + 1] = level_slices[l] + (rows + 31) / 32;
+    P.max_rows_per_level = std::max(P.max_rows_per_level, rows);
+  }
+  const int ns = level_slices[nlev];
+  std::vector<int> row((size_t)ns * 32, -1), len((size_t)ns * 32, 0), base(ns + 1, 0), width(ns, 0);
+  auto row_entries = [&](int r, int& b0, int& b1, int& c0, int& c1) {
+    // returns up to two ranges [b0,b1) and [c0,c1) of CSR positions
+    b0 = b1 = c0 = c1 = rp[r];
+    int d = dg[r];
+    if (entries == 0) {
+      b0 = rp[r];
+      b1 = d;
+    } else if (entries == 1) {
+      b0 = d + 1;
+      b1 = rp[r + 1];
+    } else {
+      b0 = rp[r];
+      b1 = d;
+      c0 = d + 1;
+      c1 = rp[r + 1];
+    }
+  };
+  for (int l = 0; l < nlev; ++l) {
+    for (int t = 0; t < cnt[l + 1] - cnt[l]; ++t) {
+      int s = level_slices[l] + t / 32, lane = t % 32;
+      int r = order[cnt[l] + t];
+      row[(size_t)s * 32 + lane] = r;
+      int b0, b1, c0, c1;
+      row_entries(r, b0, b1, c0, c1);
+      int L = (b1 - b0) + (c1 - c0);
+      len[(size_t)s * 32 + lane] = L;
+      width[s] = std::max(width[s], L);
+    }
+  }
+  int64_t pos = 0;
+  for (int s = 0; s < ns; ++s) {
+    base[s] = (int)pos;
+    pos += (int64_t)width[s] * 32;
+  }
+  base[ns] = (int)pos;
+  if (pos > INT32_MAX) throw Error(RSG_UNSUPPORTED, "matrix too large for 32-bit sweep offsets");
+  std::vector<int> col(std::max<int64_t>(pos, 1), 0), src(std::max<int64_t>(pos, 1), -1);
+  std::vector<int> dsrc((size_t)ns * 32, -1);
+  for (int s = 0; s < ns; ++s)
+    for (int lane = 0; lane < 32; ++lane) {
+      int r = row[(size_t)s * 32 + lane];
+      if (r < 0) continue;
+      dsrc[(size_t)s * 32 + lane] = dg[r];
+      int b0, b1, c0, c1;
+      row_entries(r, b0, b1, c0, c1);
+      int k = 0;
+      for (int q = b0; q < b1; ++q, ++k) {
+        col[base[s] + 32 * k + lane] = cl[q];
+        src[base[s] + 32 * k + lane] = q;
+      }
+      for (int q = c0; q < c1; ++q, ++k) {
+        col[base[s] + 32 * k + lane] = cl[q];
+        src[base[s] + 32 * k + lane] = q;
+      }
+    }
+  Context& ctx = *A.ctx;
+  P.nlev = nlev;
+  P.nslices = ns;
+  P.h_level_slices = level_slices;
+  P.level_slices.resize(nlev + 1);
+  P.slice_base.resize(ns + 1);
+  P.row.resize((size_t)ns * 32 + 1);
+  P.len.resize((size_t)ns * 32 + 1);
+  P.col.resize(col.size());
+  P.src.resize(src.size());
+  P.val.resize(col.size());
+  P.valf.resize(col.size());
+  auto up = [&](auto& dst, const auto& v) {
+    RSG_CUDA(cudaMemcpyAsync(dst.get(), v.data(), sizeof(v[0]) * v.size(), cudaMemcpyHostToDevice, ctx.stream));
+  };
+  up(P.level_slices, level_slices);
+  up(P.slice_base, base);
+  up(P.row, row);
+  up(P.len, len);
+  up(P.col, col);
+  up(P.src, src);
+  if (with_diag) {
+    P.diag_src.resize(dsrc.size());
+    P.diag.resize(dsrc.size());
+    P.diagf.resize(dsrc.size());
+    up(P.diag_src, dsrc);
+  }
+  ctx.sync();
+}
+
+static void plan_values(Context& ctx, SweepPlan& P, const double* csr_vals, bool with_diag, bool f32) {
+  int64_t size = (int64_t)P.src.size();
+  RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<double>, blocks_for(size, 256), 256, 0, size, P.src.get(), csr_vals,
+             P.val.get());
+  if (f32)
+    RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<float>, blocks_for(size, 256), 256, 0, size, P.src.get(), csr_vals,
+               P.valf.get());
+  if (with_diag) {
+    int64_t ds = (int64_t)P.diag_src.size();
+    RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<double>, blocks_for(ds, 256), 256, 0, ds, P.diag_src.get(),
+               csr_vals, P.diag.get());
+    if (f32)
+      RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<float>, blocks_for(ds, 256), 256, 0, ds, P.diag_src.get(),
+                 csr_vals, P.diagf.get());
+  }
+}
+
+// Cluster launch of a level walk; falls back to one launch per level when
+// clusters of the requested size cannot be scheduled.
+static int g_cluster_ok = -1;  // probed once per process
+
+template <typename Kernel, typename Args>
+static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Args& args) {
+  int& cluster_ok = g_cluster_ok;
+  const int threads = 512;
+  if (cluster_ok < 0) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctx.cluster_size);
+    cfg.blockDim = dim3(threads);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ctx.cluster_size;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, (const void*)kern, &cfg);
+    cluster_ok = (e == cudaSuccess && nclusters >= 1) ? 1 : 0;
+    cudaGetLastError();
+  }
+  if (!cluster_ok) return false;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctx.cluster_size);
+  cfg.blockDim = dim3(threads);
+  cfg.stream = ctx.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ctx.cluster_size;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  LaunchScope scope(ctx, name);
+  RSG_CUDA(cudaLaunchKernelEx(&cfg, kern, args));
+  return true;
+}
+
+template <int KIND, typename T>
+static void run_sweep(Context& ctx, const char* name, const SweepPlan& P, const T* val, const T* diag, const T* b,
+                      T* x, T* xx, T omega, const int* active) {
+  SweepArgs<T> a{P.nlev, P.level_slices.get(), P.slice_base.get(), P.row.get(), P.len.get(), P.col.get(), val, diag,
+                 b, x, xx, omega, active};
+  if (launch_cluster(ctx, name, k_sweep_cluster<KIND, T>, a)) return;
+  for (int l = 0; l < P.nlev; ++l) {
+    int slices = P.h_level_slices[l + 1] - P.h_level_slices[l];
+    RSG_LAUNCH(ctx, name, (k_sweep_level<KIND, T>), blocks_for(slices, 8), 256, 0, a, l);
+  }
+}
+
+// ------------------------------------------------------------------ ILU ----
+struct ILUPrecond : Precond {
+  Context* ctx;
+  Csr* A = nullptr;
+  SweepPlan Lp, Up;
+  DeviceBuffer<double> LU, y;
+  DeviceBuffer<float> yf;
+  DeviceBuffer<int> flag;
+  const int* pattern_id = nullptr;
+  explicit ILUPrecond(Context* c) : ctx(c) {}
+
+  void analyse(Csr& M) {
+    const auto& rp = M.h_rowptr;
+    const auto& cl = M.h_col;
+    for (int k = 0; k < M.n; ++k)
+      if (M.h_diag[k] < 0)
+        throw Error(RSG_MISSING_DIAGONAL, "Missing diagonal entry on row " + std::to_string(k + 1));
+    // ILU.java:113-120 reads colind[l] one past the end of row k when the
+    // scan of row k runs off its end; that read can update row k+1 or run
+    // off the array.  Such patterns are rejected rather than reproduced.
+    for (int k = 1; k < M.n; ++k) {
+      const int r1 = rp[k + 1];
+      const int maxc = cl[r1 - 1];
+      for (int i = rp[k]; i < M.h_diag[k]; ++i) {
+        int index = cl[i];
+        if (cl[rp[index + 1] - 1] <= maxc) continue;
+        for (int j = M.h_diag[index] + 1; j < rp[index + 1]; ++j)
+          if (cl[j] > maxc) {
+            if (r1 >= M.nnz || cl[r1] == cl[j])
+              throw Error(RSG_UNSUPPORTED, "ILU(0) pattern reaches past the end of row " + std::to_string(k + 1));
+          }
+      }
+    }
+    build_plan(M, Lp, false, 0, false);
+    build_plan(M, Up, true, 1, true);
+    LU.resize(std::max(M.nnz, 1));
+    y.resize(M.n);
+    yf.resize(M.n);
+    flag.resize(1);
+  }
+
+  void setup(Csr& M) override {
+    if (A != &M || pattern_id != M.rowptr.get()) {
+      analyse(M);
+      A = &M;
+      pattern_id = M.rowptr.get();
+    }
+    // LU.set(A) then factor() (ILU.java:80-125)
+    RSG_LAUNCH(*ctx, "ilu_copy", k_copy, blocks_for(M.nnz, 256), 256, 0, (int64_t)M.nnz, M.val.get(), LU.get());
+    RSG_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), ctx->stream));
+    FactorArgs fa{Lp.nlev, Lp.level_slices.get(), Lp.row.get(), M.rowptr.get(), M.col.get(), M.diag.get(), LU.get(),
+                  flag.get()};
+    if (!launch_cluster(*ctx, "ilu_factor", k_factor_cluster, fa)) {
+      for (int l = 0; l < Lp.nlev; ++l) {
+        int slots = (Lp.h_level_slices[l + 1] - Lp.h_level_slices[l]) * 32;
+        RSG_LAUNCH(*ctx, "ilu_factor", k_factor_level, blocks_for(slots, 256), 256, 0, fa, l);
+      }
+    }
+    int h = 0;
+    RSG_CUDA(cudaMemcpyAsync(&h, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    if (h) throw Error(RSG_ZERO_PIVOT, "Zero pivot encountered on row " + std::to_string(h));
+    plan_values(*ctx, Lp, LU.get(), false, true);
+    plan_values(*ctx, Up, LU.get(), true, true);
+  }
+
+  void apply(const double* b, double* x, const int* active) override {
+    // L.solve(b, y); U.solve(y, x)
+    run_sweep<SW_ILU_LOWER, double>(*ctx, "ilu_lower", Lp, Lp.val.get(), nullptr, b, y.get(), nullptr, 0.0, active);
+    run_sweep<SW_ILU_UPPER, double>(*ctx, "ilu_upper", Up, Up.val.get(), Up.diag.get(), y.get(), x, nullptr, 0.0,
+                                    active);
+  }
+  void apply_f32(const float* b, float* x, const int* active) override {
+    run_sweep<SW_ILU_LOWER, float>(*ctx, "ilu_lower_f32", Lp, Lp.valf.get(), nullptr, b, yf.get(), nullptr, 0.0f,
+                                   active);
+    run_sweep<SW_ILU_UPPER, float>(*ctx, "ilu_upper_f32", Up, Up.valf.get(), Up.diagf.get(), yf.get(), x, nullptr,
+                                   0.0f, active);
+  }
+  void trans_apply(const double* b, double* x, const int* active) override;
+};
+
+// transApply (ILU.java:72-78) via column-oriented sweeps over the transpose;
+// built lazily on first use.
+struct TransPlan {
+  Csr At;
+  DeviceBuffer<int> tsrc;
+  SweepPlan Lt, Ut;
+  bool built = false;
+};
+static std::map<const ILUPrecond*, std::unique_ptr<TransPlan>> g_trans;
+
+__global__ void k_gather_vals(int64_t n, const int* __restrict__ src, const double* __restrict__ v,
+                              double* __restrict__ out) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) out[q] = v[src[q]];
+}
+
+// U^T y = b: row i of U^T holds column i of U; y_i = (b_i - sum_{j<i} U_ji y_j) / U_ii.
+// L^T x = y: x_i = y_i - sum_{j>i} L_ji x_j.
+// The Java transSolve loops (UpperCompRowMatrix.java:69-90,
+// UnitLowerCompRowMatrix.java:69-86) subtract the same products in row
+// order of U and L; the transposed gather subtracts them in the same order.
+void ILUPrecond::trans_apply(const double* b, double* x, const int* active) {
+  auto& tp = g_trans[this];
+  if (!tp) tp.reset(new TransPlan());
+  TransPlan& T = *tp;
+  Csr& M = *A;
+  if (!T.built) {
+    std::vector<int> tptr(M.n + 1, 0), tcol(M.nnz), tsrc(M.nnz);
+    for (int q = 0; q < M.nnz; ++q) tptr[M.h_col[q] + 1]++;
+    for (int c = 0; c < M.n; ++c) tptr[c + 1] += tptr[c];
+    std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+    for (int r = 0; r < M.n; ++r)
+      for (int q = M.h_rowptr[r]; q < M.h_rowptr[r + 1]; ++q) {
+        int c = M.h_col[q];
+        tcol[fill[c]] = r;
+        tsrc[fill[c]] = q;
+        fill[c]++;
+      }
+    T.At.build(ctx, M.n, M.nnz, tptr.data(), tcol.data());
+    T.tsrc.resize(M.nnz);
+    RSG_CUDA(cudaMemcpyAsync(T.tsrc.get(), tsrc.data(), sizeof(int) * M.nnz, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->sync();
+    // U^T is lower triangular (its strictly lower part = U's strictly upper
+    // part, transposed); L^T is upper triangular.
+    build_plan(T.At, T.Ut, false, 0, true);
+    build_plan(T.At, T.Lt, true, 1, false);
+    T.built = true;
+  }
+  RSG_LAUNCH(*ctx, "ilu_trans_gather", k_gather_vals, blocks_for(M.nnz, 256), 256, 0, (int64_t)M.nnz, T.tsrc.get(),
+             LU.get(), T.At.val.get());
+  plan_values(*ctx, T.Ut, T.At.val.get(), true, false);
+  plan_values(*ctx, T.Lt, T.At.val.get(), false, false);
+  run_sweep<SW_ILU_UPPER, double>(*ctx, "ilu_trans_upper", T.Ut, T.Ut.val.get(), T.Ut.diag.get(), b, y.get(), nullptr,
+                                  0.0, active);
+  run_sweep<SW_ILU_LOWER, double>(*ctx, "ilu_trans_lower", T.Lt, T.Lt.val.get(), nullptr, y.get(), x, nullptr, 0.0,
+                                  active);
+}
+
+// --------------------------------------------------------------- SSOR ----
+struct SSORPrecond : Precond {
+  Context* ctx;
+  Csr* A = nullptr;
+  const int* pattern_id = nullptr;
+  SweepPlan Fp, Bp;
+  DeviceBuffer<double> xx;
+  double omegaF = 1, omegaR = 1;
+  bool reverse = true;
+  explicit SSORPrecond(Context* c) : ctx(c) {}
+  void setup(Csr& M) override {
+    if (A != &M || pattern_id != M.rowptr.get()) {
+      for (int k = 0; k < M.n; ++k)
+        if (M.h_diag[k] < 0) throw Error(RSG_MISSING_DIAGONAL, "Missing diagonal on row " + std::to_string(k + 1));
+      build_plan(M, Fp, false, 2, true);
+      build_plan(M, Bp, true, 2, true);
+      xx.resize(M.n);
+      A = &M;
+      pattern_id = M.rowptr.get();
+    }
+    plan_values(*ctx, Fp, M.val.get(), true, false);
+    plan_values(*ctx, Bp, M.val.get(), true, false);
+  }
+  void apply(const double* b, double* x, const int* active) override {
+    // SSOR.java:143-194; x holds the starting iterate
+    run_sweep<SW_SSOR_FWD, double>(*ctx, "ssor_fwd", Fp, Fp.val.get(), Fp.diag.get(), b, x, xx.get(), omegaF, active);
+    if (!reverse) {
+      RSG_LAUNCH(*ctx, "ssor_copy", k_copy, blocks_for(A->n, 256), 256, 0, (int64_t)A->n, xx.get(), x);
+      return;
+    }
+    run_sweep<SW_SSOR_BWD, double>(*ctx, "ssor_bwd", Bp, Bp.val.get(), Bp.diag.get(), b, x, xx.get(), omegaR, active);
+  }
+  void trans_apply(const double* b, double* x, const int* active) override { apply(b, x, active); }
+};
+
+// ----------------------------------------------------------- diagonal ----
+struct DiagPrecond : Precond {
+  Context* ctx;
+  int n = 0;
+  DeviceBuffer<double> inv;
+  DeviceBuffer<float> invf;
+  DeviceBuffer<int> flag;
+  explicit DiagPrecond(Context* c) : ctx(c) {}
+  void setup(Csr& M) override {
+    n = M.n;
+    inv.resize(n);
+    invf.resize(n);
+    flag.resize(1);
+    RSG_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), ctx->stream));
+    RSG_LAUNCH(*ctx, "diag_setup", k_invdiag, blocks_for(n, 256), 256, 0, n, M.diag.get(), M.val.get(), inv.get(),
+               invf.get(), flag.get());
+    int h = 0;
+    RSG_CUDA(cudaMemcpyAsync(&h, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    if (h) throw Error(RSG_ZERO_PIVOT, "Zero diagonal on row " + std::to_string(h));
+  }
+  void apply(const double* b, double* x, const int* active) override {
+    RSG_LAUNCH(*ctx, "diag_apply", k_diag_apply<double>, blocks_for(n, 256), 256, 0, n, inv.get(), b, x, active);
+  }
+  void apply_f32(const float* b, float* x, const int* active) override {
+    RSG_LAUNCH(*ctx, "diag_apply_f32", k_diag_apply<float>, blocks_for(n, 256), 256, 0, n, invf.get(), b, x, active);
+  }
+  void trans_apply(const double* b, double* x, const int* active) override { apply(b, x, active); }
+};
+
+struct IdentityPrecond : Precond {
+  Context* ctx;
+  int n = 0;
+  explicit IdentityPrecond(Context* c) : ctx(c) {}
+  void setup(Csr& M) override { n = M.n; }
+  void apply(const double* b, double* x, const int* active) override {
+    RSG_LAUNCH(*ctx, "copy", k_copy, blocks_for(n, 256), 256, 0, (int64_t)n, b, x);
+  }
+  void apply_f32(const float* b, float* x, const int* active) override {
+    RSG_CUDA(cudaMemcpyAsync(x, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  void trans_apply(const double* b, double* x, const int* active) override { apply(b, x, active); }
+};
+
+std::unique_ptr<Precond> make_precond(Context* ctx, int kind) {
+  switch (kind) {
+    case RSG_PC_NONE: return std::unique_ptr<Precond>(new IdentityPrecond(ctx));
+    case RSG_PC_DIAGONAL: return std::unique_ptr<Precond>(new DiagPrecond(ctx));
+    case RSG_PC_ILU: return std::unique_ptr<Precond>(new ILUPrecond(ctx));
+    case RSG_PC_SSOR: return std::unique_ptr<Precond>(new SSORPrecond(ctx));
+  }
+  throw Error(RSG_UNSUPPORTED, "preconditioner not implemented");
+}
+
+void set_ssor_params(Precond* p, double wf, double wr, int reverse) {
+  auto* s = dynamic_cast<SSORPrecond*>(p);
+  if (!s) throw Error(RSG_BAD_ARG, "solver does not use SSOR");
+  if (wf < 0 || wf > 2 || wr < 0 || wr > 2) throw Error(RSG_BAD_ARG, "omega must be between 0 and 2");
+  s->omegaF = wf;
+  s->omegaR = wr;
+  s->reverse = reverse != 0;
+}
+
+void release_trans_plan(const Precond* p) {
+  auto* ilu = dynamic_cast<const ILUPrecond*>(p);
+  if (ilu) g_trans.erase(ilu);
+}
+
+}  // namespace rsg
+
+extern "C" int32_t rsg_sweep_mode(void) { return rsg::g_cluster_ok; }

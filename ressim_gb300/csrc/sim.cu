@@ -1,0 +1,1340 @@
+// RS pressure step on the GPU: per-cell property chain (field/CV.java:375-550
+// with fluid/WaterEquationOfState.java:71-129, fluid/BlackOilEquationOfState.java:168-547,
+// rock/CoreyRockFluid.java:84-141, util/LookupTable.java:202-430), per-connection
+// Darcy fluxes (field/CS.java:94-170), the pressure Jacobian
+// (numerics/Discretisation.java:365-561), LinearSolver.solve
+// (numerics/LinearSolver.java:244-294), the pressure update and Newton test
+// (Discretisation.java:280-359), and the explicit molar-mass update
+// (Discretisation.java:769-919).  Field initialisation by local volume
+// balance (field/Field.java:260-447) runs one thread per cell.
+//
+// Every sum that RS accumulates over connections is gathered per row in
+// ascending connection order, so the assembled Jacobian, residual and mass
+// changes equal the sequential Java loops without atomics.
+#include <algorithm>
+#include <cmath>
+
+#include "mesh.cuh"
+
+namespace rsg {
+
+namespace {
+
+constexpr double G_ACC = 9.81;  // util/Constants.java:18
+constexpr int NCM = RSG_MAX_COMPONENTS;
+
+struct DFunc {
+  int kind, dim;
+  double value;
+  int n[3];
+  const double* coord[3];
+  double offset[3], delta[3];
+  const double* data;
+};
+
+__device__ int f_index(const DFunc& f, int d, double x) {
+  if (f.kind == RSG_FN_EVEN_TABLE) {
+    // EvenLookupTable.getIndex (:164-174)
+    int index = (int)((x - f.offset[d]) / f.delta[d]);
+    if (index < 0) index = 0;
+    else if (index > f.n[d] - 2) index = f.n[d] - 2;
+    return index;
+  }
+  const double* c = f.coord[d];
+  const int len = f.n[d];
+  if (x <= c[0]) return 0;
+  if (x >= c[len - 2]) return len - 2;
+  int begin = 0, end = len - 1;
+  while (begin <= end) {
+    int mid = (end + begin) / 2;
+    if (c[mid] < x) begin = mid + 1;
+    else end = mid - 1;
+  }
+  return begin - 1;
+}
+
+__device__ double f_weight(const DFunc& f, int d, int index, double x) {
+  double mn = f.coord[d][index], mx = f.coord[d][index + 1];
+  if (x <= mn) return 0;
+  if (x >= mx) return 1;
+  return (x - mn) / (mx - mn);
+}
+
+// LookupTable.evaluate (:217-357); nd = -1 value, else partial derivative
+__device__ double f_eval(const DFunc& f, int nd, const double* x) {
+  if (f.kind == RSG_FN_CONSTANT) return nd < 0 ? f.value : 0.0;
+  if (nd >= 0 && !(x[nd] >= f.coord[nd][0] && x[nd] <= f.coord[nd][f.n[nd] - 1])) return 0;
+  const double* D = f.data;
+  const int nx = f.n[0], ny = f.n[1];
+  if (f.dim == 1) {
+    int xi = f_index(f, 0, x[0]);
+    double xw = f_weight(f, 0, xi, x[0]);
+    double phi1, phi2;
+    if (nd == -1) {
+      phi1 = 1 - xw;
+      phi2 = xw;
+    } else {
+      double dl = f.coord[0][xi + 1] - f.coord[0][xi];
+      phi1 = -1 / dl;
+      phi2 = 1 / dl;
+    }
+    return phi1 * D[xi] + phi2 * D[xi + 1];
+  }
+  if (f.dim == 2) {
+    int xi = f_index(f, 0, x[0]), yi = f_index(f, 1, x[1]);
+    double xw = f_weight(f, 0, xi, x[0]), yw = f_weight(f, 1, yi, x[1]);
+    double phi1, phi2, phi3, phi4, dl;
+    if (nd == -1) {
+      phi1 = (1 - xw) * (1 - yw);
+      phi2 = xw * (1 - yw);
+      phi3 = (1 - xw) * yw;
+      phi4 = xw * yw;
+    } else if (nd == 0) {
+      dl = f.coord[0][xi + 1] - f.coord[0][xi];
+      phi1 = (-1 + yw) / dl;
+      phi2 = (1 - yw) / dl;
+      phi3 = -yw / dl;
+      phi4 = yw / dl;
+    } else {
+      dl = f.coord[1][yi + 1] - f.coord[1][yi];
+      phi1 = (-1 + xw) / dl;
+      phi2 = -xw / dl;
+      phi3 = (1 - xw) / dl;
+      phi4 = xw / dl;
+    }
+    return phi1 * D[xi + yi * nx] + phi2 * D[xi + 1 + yi * nx] + phi3 * D[xi + (yi + 1) * nx] +
+           phi4 * D[xi + 1 + (yi + 1) * nx];
+  }
+  int xi = f_index(f, 0, x[0]), yi = f_index(f, 1, x[1]), zi = f_index(f, 2, x[2]);
+  double xw = f_weight(f, 0, xi, x[0]), yw = f_weight(f, 1, yi, x[1]), zw = f_weight(f, 2, zi, x[2]);
+  double p1, p2, p3, p4, p5, p6, p7, p8, dl;
+  if (nd == -1) {
+    p1 = (1 - xw) * (1 - yw) * (1 - zw);
+    p2 = xw * (1 - yw) * (1 - zw);
+    p3 = (1 - xw) * yw * (1 - zw);
+    p4 = xw * yw * (1 - zw);
+    p5 = (1 - xw) * (1 - yw) * zw;
+    p6 = xw * (1 - yw) * zw;
+    p7 = (1 - xw) * yw * zw;
+    p8 = xw * yw * zw;
+  } else if (nd == 0) {
+    dl = f.coord[0][xi + 1] - f.coord[0][xi];
+    p1 = -(1 - yw) * (1 - zw) / dl;
+    p2 = (1 - yw) * (1 - zw) / dl;
+    p3 = -yw * (1 - zw) / dl;
+    p4 = yw * (1 - zw) / dl;
+    p5 = -(1 - yw) * zw / dl;
+    p6 = (1 - yw) * zw / dl;
+    p7 = -yw * zw / dl;
+    p8 = yw * zw / dl;
+  } else if (nd == 1) {
+    dl = f.coord[1][yi + 1] - f.coord[1][yi];
+    p1 = -(1 - xw) * (1 - zw) / dl;
+    p2 = -xw * (1 - zw) / dl;
+    p3 = (1 - xw) * (1 - zw) / dl;
+    p4 = xw * (1 - zw) / dl;
+    p5 = -(1 - xw) * zw / dl;
+    p6 = -xw * zw / dl;
+    p7 = (1 - xw) * zw / dl;
+    p8 = xw * zw / dl;
+  } else {
+    dl = f.coord[2][zi + 1] - f.coord[2][zi];
+    p1 = -(1 - xw) * (1 - yw) / dl;
+    p2 = -xw * (1 - yw) / dl;
+    p3 = -(1 - xw) * yw / dl;
+    p4 = -xw * yw / dl;
+    p5 = (1 - xw) * (1 - yw) / dl;
+    p6 = xw * (1 - yw) / dl;
+    p7 = (1 - xw) * yw / dl;
+    p8 = xw * yw / dl;
+  }
+  const int sxy = nx * ny;
+  auto d3 = [&](int a, int b, int c) { return D[a + b * nx + c * sxy]; };
+  return p1 * d3(xi, yi, zi) + p2 * d3(xi + 1, yi, zi) + p3 * d3(xi, yi + 1, zi) + p4 * d3(xi + 1, yi + 1, zi) +
+         p5 * d3(xi, yi, zi + 1) + p6 * d3(xi + 1, yi, zi + 1) + p7 * d3(xi, yi + 1, zi + 1) +
+         p8 * d3(xi + 1, yi + 1, zi + 1);
+}
+
+struct DFluid {
+  int nc, ngO, ngG;
+  int O[NCM], G[NCM];
+  double Mw[NCM];
+  DFunc wden, wvis, went, bub, dew, oden, gden, ovis, gvis, oent, gent;
+};
+
+struct DCorey {
+  double Sr[3], n[3], ke[3], cw, cow, cg, cog, aw, aow, ag, aog;
+};
+
+// Per-phase EOS record (EquationOfStateData)
+struct Phase {
+  bool present;
+  double V, xi, dVdp, dVdT, h, dhdT, mu;
+  double N[NCM], dVdN[NCM];
+};
+
+__device__ void phase_clear(Phase& e, int nc) {
+  e.present = false;
+  e.V = e.xi = e.dVdp = e.dVdT = e.h = e.dhdT = e.mu = 0;
+  for (int i = 0; i < nc; ++i) e.N[i] = e.dVdN[i] = 0;
+}
+
+__device__ double mole_fraction(const double* N, int nc, int nu) {
+  double NT = 0;
+  for (int i = 0; i < nc; ++i) NT += N[i];
+  return NT > 0 ? N[nu] / NT : 0;
+}
+
+// Flags raised by the property chain (first one wins)
+enum { FL_NONE = 0, FL_DRDP = 1, FL_DENSITY = 2, FL_WATER_DERIV = 3, FL_BLACKOIL_CHECK = 4, FL_ENTHALPY = 5, FL_PATTERN = 6 };
+
+__device__ void blackoil_state(const DFluid& fl, double p, const double* N, double T, Phase* ph, int* flag) {
+  const int nc = fl.nc;
+  double pT[2] = {p, T};
+  {
+    Phase& w = ph[0];
+    double Nw = N[0];
+    if (Nw > 0) {
+      w.present = true;
+      double xiw = f_eval(fl.wden, -1, pT);
+      double Vw = Nw / xiw;
+      if (xiw <= 0) atomicCAS(flag, 0, FL_DENSITY);
+      w.xi = xiw;
+      w.V = Vw;
+      w.N[0] = Nw;
+      double dxiw_dp = f_eval(fl.wden, 0, pT);
+      double dxiw_dT = f_eval(fl.wden, 1, pT);
+      if (dxiw_dp < 0) atomicCAS(flag, 0, FL_WATER_DERIV);
+      w.dVdp = -(Vw / xiw) * dxiw_dp;
+      w.dVdT = -(Vw / xiw) * dxiw_dT;
+      w.dVdN[0] = 1 / xiw;
+      double hw = f_eval(fl.went, -1, pT);
+      w.h = hw * xiw;
+      double dhw_dT = f_eval(fl.went, 1, pT);
+      w.dhdT = dhw_dT * xiw + hw * dxiw_dT;
+      w.mu = f_eval(fl.wvis, -1, pT);
+    } else
+      phase_clear(w, nc);
+  }
+  Phase& oil = ph[1];
+  Phase& gas = ph[2];
+  double No = 0, Ng = 0;
+  for (int a = 0; a < fl.ngO; ++a) No += N[fl.O[a]];
+  for (int a = 0; a < fl.ngG; ++a) Ng += N[fl.G[a]];
+  double NHC = No + Ng;
+  double Nt = 0;
+  for (int i = 0; i < nc; ++i) Nt += N[i];
+  auto inverse_group = [&](double Nop, double Ngp, Phase& e) {
+    double Co = No / Nt, Cg = Ng / Nt;
+    if (Co > 0)
+      for (int a = 0; a < fl.ngO; ++a) e.N[fl.O[a]] = mole_fraction(N, nc, fl.O[a]) * Nop / Co;
+    if (Cg > 0)
+      for (int a = 0; a < fl.ngG; ++a) e.N[fl.G[a]] = mole_fraction(N, nc, fl.G[a]) * Ngp / Cg;
+  };
+  auto enthalpy = [&](double C, double dCdT, double xi, double dxidT, double dxidC, const DFunc& fn, Phase& e) {
+    double x[3] = {p, C, T};
+    double hbar = f_eval(fn, -1, x);
+    if (hbar * xi < 0) atomicCAS(flag, 0, FL_ENTHALPY);
+    e.h = hbar * xi;
+    double dhbar_dT = f_eval(fn, 2, x);
+    double dhbar_dC = 0;
+    if (dCdT != 0) dhbar_dC = f_eval(fn, 1, x);
+    e.dhdT = (dhbar_dT + dhbar_dC * dCdT) * xi + hbar * (dxidT + dxidC * dCdT);
+  };
+  if (NHC < 1e-300) {
+    phase_clear(oil, nc);
+    phase_clear(gas, nc);
+    return;
+  }
+  double Cb = 0, Cd = 0;
+  double Zo = No / NHC, Zg = Ng / NHC;
+  if (Zg <= (Cb = f_eval(fl.bub, -1, pT))) {
+    oil.present = true;
+    phase_clear(gas, nc);
+    inverse_group(No, Ng, oil);
+    double Cgo = Ng / NHC;
+    double x[3] = {p, Cgo, T};
+    double xio = f_eval(fl.oden, -1, x);
+    double Vo = (No + Ng) / xio;
+    if (xio <= 0) atomicCAS(flag, 0, FL_DENSITY);
+    oil.xi = xio;
+    oil.V = Vo;
+    double dxio_dp = f_eval(fl.oden, 0, x), dxio_dC = f_eval(fl.oden, 1, x), dxio_dT = f_eval(fl.oden, 2, x);
+    double dCgo_dNo = -Cgo / NHC;
+    double dCgo_dNg = (1 - Cgo) / NHC;
+    double Vo_xio = Vo / xio;
+    oil.dVdp = -Vo_xio * dxio_dp;
+    oil.dVdT = -Vo_xio * dxio_dT;
+    double dVodNo = (1 / xio) - Vo_xio * dxio_dC * dCgo_dNo;
+    double dVodNg = (1 / xio) - Vo_xio * dxio_dC * dCgo_dNg;
+    for (int a = 0; a < fl.ngO; ++a) oil.dVdN[fl.O[a]] = dVodNo;
+    for (int a = 0; a < fl.ngG; ++a) oil.dVdN[fl.G[a]] = dVodNg;
+    enthalpy(1, 0, xio, dxio_dT, dxio_dC, fl.oent, oil);
+    oil.mu = f_eval(fl.ovis, -1, x);
+  } else if (Zo <= (Cd = f_eval(fl.dew, -1, pT))) {
+    phase_clear(oil, nc);
+    gas.present = true;
+    inverse_group(No, Ng, gas);
+    double Cog = No / NHC;
+    double x[3] = {p, Cog, T};
+    double xig = f_eval(fl.gden, -1, x);
+    double Vg = (No + Ng) / xig;
+    if (xig <= 0) atomicCAS(flag, 0, FL_DENSITY);
+    gas.xi = xig;
+    gas.V = Vg;
+    double dxig_dp = f_eval(fl.gden, 0, x), dxig_dC = f_eval(fl.gden, 1, x), dxig_dT = f_eval(fl.gden, 2, x);
+    double dCgo_dNo = -(1 - Cog) / NHC;
+    double dCgo_dNg = -Cog / NHC;
+    double Vg_xig = Vg / xig;
+    gas.dVdp = -Vg_xig * dxig_dp;
+    gas.dVdT = -Vg_xig * dxig_dT;
+    double dVgdNo = (1 / xig) - Vg_xig * dxig_dC * dCgo_dNo;
+    double dVgdNg = (1 / xig) - Vg_xig * dxig_dC * dCgo_dNg;
+    for (int a = 0; a < fl.ngO; ++a) gas.dVdN[fl.O[a]] = dVgdNo;
+    for (int a = 0; a < fl.ngG; ++a) gas.dVdN[fl.G[a]] = dVgdNg;
+    enthalpy(1, 0, xig, dxig_dT, dxig_dC, fl.gent, gas);
+    gas.mu = f_eval(fl.gvis, -1, x);
+  } else {
+    oil.present = true;
+    gas.present = true;
+    double Cgo = Cb, Cog = Cd;
+    double L = (Cog - Zo) / (Cog - (1 - Cgo));
+    double Noo = L * NHC * (1 - Cgo);
+    double Ngo = L * NHC * Cgo;
+    double Nog = (1 - L) * NHC * Cog;
+    double Ngg = (1 - L) * NHC * (1 - Cog);
+    inverse_group(Noo, Ngo, oil);
+    inverse_group(Nog, Ngg, gas);
+    double xo[3] = {p, Cgo, T}, xg[3] = {p, Cog, T};
+    double xio = f_eval(fl.oden, -1, xo);
+    double xig = f_eval(fl.gden, -1, xg);
+    double Vo = (Noo + Ngo) / xio;
+    double Vg = (Nog + Ngg) / xig;
+    oil.xi = xio;
+    gas.xi = xig;
+    oil.V = Vo;
+    gas.V = Vg;
+    double dCgo_dp = f_eval(fl.bub, 0, pT), dCog_dp = f_eval(fl.dew, 0, pT);
+    double dCgo_dT = f_eval(fl.bub, 1, pT), dCog_dT = f_eval(fl.dew, 1, pT);
+    double dLdp = (1 / (Cog - (1 - Cgo))) * ((1 - L) * dCog_dp - L * (dCgo_dp));
+    double dLdT = (1 / (Cog - (1 - Cgo))) * ((1 - L) * dCog_dT - L * (dCgo_dT));
+    double dLdNo = (1 / (Cog - (1 - Cgo))) * ((Zo - 1) / NHC);
+    double dLdNg = (1 / (Cog - (1 - Cgo))) * (Zo / NHC);
+    double dxio_dp = f_eval(fl.oden, 0, xo), dxio_dC = f_eval(fl.oden, 1, xo), dxio_dT = f_eval(fl.oden, 2, xo);
+    double dxig_dp = f_eval(fl.gden, 0, xg), dxig_dC = f_eval(fl.gden, 1, xg), dxig_dT = f_eval(fl.gden, 2, xg);
+    double dVodp = (Vo / L) * dLdp - (Vo / xio) * (dxio_dp + dxio_dC * dCgo_dp);
+    double dVgdp = -(Vg / (1 - L)) * dLdp - (Vg / xig) * (dxig_dp + dxig_dC * dCog_dp);
+    double dVodT = (Vo / L) * dLdT - (Vo / xio) * (dxio_dT + dxio_dC * dCgo_dT);
+    double dVgdT = -(Vg / (1 - L)) * dLdT - (Vg / xig) * (dxig_dT + dxig_dC * dCog_dT);
+    double dVodNo = (1 / xio) * (dLdNo * NHC + L);
+    double dVodNg = (1 / xio) * (dLdNg * NHC + L);
+    double dVgdNo = (1 / xig) * (-dLdNo * NHC + (1 - L));
+    double dVgdNg = (1 / xig) * (-dLdNg * NHC + (1 - L));
+    oil.dVdp = dVodp;
+    oil.dVdT = dVodT;
+    gas.dVdp = dVgdp;
+    gas.dVdT = dVgdT;
+    for (int a = 0; a < fl.ngO; ++a) {
+      oil.dVdN[fl.O[a]] = dVodNo;
+      gas.dVdN[fl.O[a]] = dVgdNo;
+    }
+    for (int a = 0; a < fl.ngG; ++a) {
+      oil.dVdN[fl.G[a]] = dVodNg;
+      gas.dVdN[fl.G[a]] = dVgdNg;
+    }
+    if (Cog - (1 - Cgo) > 0 || (1 - L) * dCog_dp - L * dCgo_dp > 0 || dVodp + dVgdp > 0 || dVodNo + dVgdNo <= 0 ||
+        dVodNg + dVgdNg <= 0)
+      atomicCAS(flag, 0, FL_BLACKOIL_CHECK);
+    enthalpy(Cgo, dCgo_dT, xio, dxio_dT, dxio_dC, fl.oent, oil);
+    enthalpy(Cog, dCog_dT, xig, dxig_dT, dxig_dC, fl.gent, gas);
+    oil.mu = f_eval(fl.ovis, -1, xo);
+    gas.mu = f_eval(fl.gvis, -1, xg);
+  }
+}
+
+// Math.pow as HotSpot evaluates it for an exponent of exactly 2 (x * x);
+// other exponents use CUDA's pow (within 2 ulp).
+__device__ __forceinline__ double jpow(double x, double y) { return y == 2.0 ? x * x : pow(x, y); }
+
+__device__ double eff_sat(const DCorey& c, int ph, double S) {
+  double Se = S;
+  Se -= c.Sr[ph];
+  double denom = 1;
+  for (int q = 0; q < 3; ++q) denom -= c.Sr[q];
+  Se /= denom;
+  return Se;
+}
+
+// Persistent per-cell phase records: kept across calls the way the Java CV
+// objects keep theirs (entries that a branch does not set keep old values).
+struct CellOut {
+  double S[3], rho[3], lambda[3], Cxi[NCM][3];
+  double R, dRdp, dRdN[NCM], pcow, pcgo, phi;
+  int present;
+};
+
+struct SimDev {
+  int n, nc, nconn;
+  DFluid fl;
+  DCorey co;
+  const double* phi0;
+  const double* cr;
+  const double* vol;
+  const double* bf;  // body force per cell
+  // primary
+  double* p;
+  double* p0;
+  double* T;
+  double* N;  // nc x n
+  // phase records persisted between calls (nc x 3 x n for N and dVdN)
+  double* phN;
+  double* phdVdN;
+  // secondaries
+  double* S;       // 3 x n
+  double* rho;     // 3 x n
+  double* lambda;  // 3 x n
+  double* Cxi;     // nc x 3 x n
+  double* xi;      // 3 x n
+  double* R;
+  double* dRdp;
+  double* dRdN;    // nc x n
+  double* pcow;
+  double* pcgo;
+  int* present;    // bit mask per cell
+  int* flag;
+};
+
+// CV.calculateSecondaries on one cell; reads p, p0, T, N and the persisted
+// phase records, writes all secondaries.
+__device__ void cv_cell(const SimDev& d, int i, double p, double p0, double T, const double* N) {
+  const int nc = d.nc, n = d.n;
+  Phase ph[3];
+  for (int a = 0; a < 3; ++a) {
+    ph[a].present = (d.present[i] >> a) & 1;
+    ph[a].V = ph[a].xi = ph[a].dVdp = ph[a].dVdT = ph[a].h = ph[a].dhdT = ph[a].mu = 0;
+    for (int nu = 0; nu < nc; ++nu) {
+      ph[a].N[nu] = d.phN[((int64_t)nu * 3 + a) * n + i];
+      ph[a].dVdN[nu] = d.phdVdN[((int64_t)nu * 3 + a) * n + i];
+    }
+  }
+  blackoil_state(d.fl, p, N, T, ph, d.flag);
+  const double V = d.vol[i];
+  // calculateFluidProperties: rho = kg / V_l for present phases
+  double rho[3];
+  for (int a = 0; a < 3; ++a) {
+    if (!ph[a].present) {
+      rho[a] = 0;
+      continue;
+    }
+    double kg = 0;
+    for (int nu = 0; nu < nc; ++nu) kg += d.fl.Mw[nu] * ph[a].N[nu];
+    rho[a] = kg / ph[a].V;
+  }
+  // calculateRockProperties
+  const double c = d.cr[i];
+  const double dpp = p - p0;
+  const double phi = d.phi0[i] * (1 + c * dpp + c * c * dpp * dpp / 2);
+  double Vf = 0;
+  for (int a = 0; a < 3; ++a) Vf += ph[a].V;
+  double S[3];
+  for (int a = 0; a < 3; ++a) S[a] = ph[a].V / Vf;
+  // Corey relative permeability and capillary pressures
+  double kr[3];
+  for (int a = 0; a < 3; ++a) kr[a] = d.co.ke[a] * jpow(eff_sat(d.co, a, S[a]), d.co.n[a]);
+  double pcow = 0, pcgo = 0;
+  {
+    double Sw = eff_sat(d.co, 0, S[0]), So = eff_sat(d.co, 1, S[1]);
+    if (Sw > 0) pcow += d.co.cw / jpow(Sw, d.co.aw);
+    if (So > 0) pcow -= d.co.cow / jpow(So, d.co.aow);
+    double Sg = eff_sat(d.co, 2, S[2]);
+    if (Sg > 0) pcgo += d.co.cg / jpow(Sg, d.co.ag);
+    if (So > 0) pcgo -= d.co.cog / jpow(So, d.co.aog);
+  }
+  // calculateResidualVolume
+  double Vp = phi * V;
+  double R = Vp;
+  double dRdp = c * Vp;
+  double dRdN[NCM];
+  for (int nu = 0; nu < nc; ++nu) dRdN[nu] = 0;
+  for (int a = 0; a < 3; ++a) {
+    R -= ph[a].V;
+    dRdp -= ph[a].dVdp;
+    for (int nu = 0; nu < nc; ++nu) dRdN[nu] -= ph[a].dVdN[nu];
+  }
+  if (dRdp <= 0) atomicCAS(d.flag, 0, FL_DRDP);
+  // mobilities
+  int mask = 0;
+  for (int a = 0; a < 3; ++a) {
+    double lam = 0;
+    if (ph[a].mu != 0) lam = kr[a] / ph[a].mu;
+    d.S[(int64_t)a * n + i] = S[a];
+    d.rho[(int64_t)a * n + i] = rho[a];
+    d.lambda[(int64_t)a * n + i] = lam;
+    d.xi[(int64_t)a * n + i] = ph[a].xi;
+    for (int nu = 0; nu < nc; ++nu) {
+      d.Cxi[((int64_t)nu * 3 + a) * n + i] = mole_fraction(ph[a].N, nc, nu) * ph[a].xi;
+      d.phN[((int64_t)nu * 3 + a) * n + i] = ph[a].N[nu];
+      d.phdVdN[((int64_t)nu * 3 + a) * n + i] = ph[a].dVdN[nu];
+    }
+    if (ph[a].present) mask |= 1 << a;
+  }
+  d.present[i] = mask;
+  d.R[i] = R;
+  d.dRdp[i] = dRdp;
+  for (int nu = 0; nu < nc; ++nu) d.dRdN[(int64_t)nu * n + i] = dRdN[nu];
+  d.pcow[i] = pcow;
+  d.pcgo[i] = pcgo;
+}
+
+__global__ void k_cv(SimDev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  double N[NCM];
+  for (int nu = 0; nu < d.nc; ++nu) N[nu] = d.N[(int64_t)nu * d.n + i];
+  cv_cell(d, i, d.p[i], d.p0[i], d.T[i], N);
+}
+
+__device__ __forceinline__ double phase_pressure(const SimDev& d, int e, int ph) {
+  double p = d.p[e];
+  return ph == 0 ? p - d.pcow[e] : (ph == 1 ? p : p + d.pcgo[e]);
+}
+
+struct ConnDev {
+  const int* conn;
+  const int* md_ptr;
+  const int* md_el;
+  const double* md_k;
+  double* rho_cs;  // 3 x nconn
+  double* u;       // 3 x nconn
+  int* up;         // 3 x nconn
+};
+
+// CS.calculateSecondaries (field/CS.java:94-155)
+__global__ void k_cs(SimDev d, ConnDev c) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.nconn) return;
+  const int h = c.conn[2 * q], t = c.conn[2 * q + 1];
+  const int nc_ = d.nconn;
+  double rho[3];
+  for (int a = 0; a < 3; ++a) {
+    rho[a] = 0;
+    double Sh = d.S[(int64_t)a * d.n + h], St = d.S[(int64_t)a * d.n + t];
+    double S = Sh + St;
+    double av = (Sh * d.rho[(int64_t)a * d.n + h] + St * d.rho[(int64_t)a * d.n + t]) / S;
+    if (!isnan(av)) rho[a] = av;
+    c.rho_cs[(int64_t)a * nc_ + q] = rho[a];
+  }
+  for (int a = 0; a < 3; ++a) {
+    double D = 0;
+    for (int m = c.md_ptr[q]; m < c.md_ptr[q + 1]; ++m) {
+      int ek = c.md_el[m];
+      double psi = phase_pressure(d, ek, a) + rho[a] * d.bf[ek];
+      D += c.md_k[m] * psi;
+    }
+    int up = (D > 0) ? h : t;
+    c.up[(int64_t)a * nc_ + q] = up;
+    c.u[(int64_t)a * nc_ + q] = d.lambda[(int64_t)a * d.n + up] * D;
+  }
+}
+
+// assemblePressureJacobianFlux per connection (Discretisation.java:459-561)
+__global__ void k_flux_conn(SimDev d, ConnDev c, double* Jh, double* Jt, double* rh, double* rt) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.nconn) return;
+  const int i = c.conn[2 * q], j = c.conn[2 * q + 1];
+  const int n = d.n, nc = d.nc, ncn = d.nconn;
+  double dRh[NCM], dRt[NCM];
+  for (int nu = 0; nu < nc; ++nu) {
+    dRh[nu] = d.dRdN[(int64_t)nu * n + i];
+    dRt[nu] = d.dRdN[(int64_t)nu * n + j];
+  }
+  int up[3];
+  bool pres[3];
+  double rho[3];
+  for (int a = 0; a < 3; ++a) {
+    up[a] = c.up[(int64_t)a * ncn + q];
+    pres[a] = (d.present[up[a]] >> a) & 1;
+    rho[a] = c.rho_cs[(int64_t)a * ncn + q];
+  }
+  double ri = 0, rj = 0;
+  for (int m = c.md_ptr[q]; m < c.md_ptr[q + 1]; ++m) {
+    const int ik = c.md_el[m];
+    const double tk = c.md_k[m];
+    const double b = d.bf[ik];
+    double Ji = 0, Jj = 0;
+    for (int a = 0; a < 3; ++a) {
+      if (!pres[a]) continue;
+      double psi = phase_pressure(d, ik, a) + rho[a] * b;
+      const double lam = d.lambda[(int64_t)a * n + up[a]];
+      for (int nu = 0; nu < nc; ++nu) {
+        double phaseCompMob = d.Cxi[((int64_t)nu * 3 + a) * n + up[a]] * lam;
+        double dNdt = -phaseCompMob * tk * psi;
+        double d2Ndtp = -phaseCompMob * tk;
+        ri += dRh[nu] * dNdt;
+        rj += -dRt[nu] * dNdt;
+        Ji += dRh[nu] * d2Ndtp;
+        Jj += -dRt[nu] * d2Ndtp;
+      }
+    }
+    Jh[m] = Ji;
+    Jt[m] = Jj;
+  }
+  rh[q] = ri;
+  rt[q] = rj;
+}
+
+struct AsmDev {
+  const int* cc;      // incident connections (2c + side), 6 per cell
+  const int* ccount;
+  const int* md_ptr;
+  const int* pos_here;
+  const int* pos_there;
+  const int* rowptr;
+  const int* diag;
+  const int* src_ptr;  // regular sources per cell
+  const int* src_id;
+  const double* src_q;  // nsrc x NCM
+  const int* locked;
+  const double* p_prev;
+  const double* R_prev;
+};
+
+// Row gather of the Jacobian and residual, then LinearSolver.solve's
+// sign change and locked rows (numerics/LinearSolver.java:246-260).
+__global__ void k_assemble_rows(SimDev d, AsmDev a, const double* Jh, const double* Jt, const double* rh,
+                                const double* rt, double dt, double* val, double* b, double* rawJ, double* rawB) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.n) return;
+  const int r0 = a.rowptr[e], r1 = a.rowptr[e + 1];
+  for (int q = r0; q < r1; ++q) val[q] = 0;
+  double be = 0;
+  for (int k = 0; k < a.ccount[e]; ++k) {
+    const int code = a.cc[(int64_t)e * 6 + k];
+    const int c = code >> 1;
+    const bool here = !(code & 1);
+    if (here) {
+      for (int m = a.md_ptr[c]; m < a.md_ptr[c + 1]; ++m) {
+        const int pos = a.pos_here[m];
+        if (pos >= r0 && pos < r1) val[pos] += Jh[m];
+        else atomicCAS(d.flag, 0, FL_PATTERN);
+      }
+      be += rh[c];
+    } else {
+      for (int m = a.md_ptr[c]; m < a.md_ptr[c + 1]; ++m) {
+        const int pos = a.pos_there[m];
+        if (pos >= r0 && pos < r1) val[pos] += Jt[m];
+        else atomicCAS(d.flag, 0, FL_PATTERN);
+      }
+      be += rt[c];
+    }
+  }
+  // assemblePressureJacobianDiagonal
+  const double dpp = d.p[e] - a.p_prev[e];
+  const double dRdp = d.dRdp[e];
+  be += (a.R_prev[e] + dRdp * dpp) / dt;
+  val[a.diag[e]] += dRdp / dt;
+  // assemblePressureRegularSource
+  for (int s = a.src_ptr[e]; s < a.src_ptr[e + 1]; ++s) {
+    const double* q = a.src_q + (int64_t)a.src_id[s] * NCM;
+    for (int nu = 0; nu < d.nc; ++nu) be += d.dRdN[(int64_t)nu * d.n + e] * q[nu];
+  }
+  if (rawJ) {
+    for (int q = r0; q < r1; ++q) rawJ[q] = val[q];
+  }
+  be *= -1;
+  if (rawB) rawB[e] = be;
+  if (a.locked[e]) {
+    for (int q = r0; q < r1; ++q) val[q] = (q == a.diag[e]) ? 1.0 : 0.0;
+    be = 0;
+  }
+  b[e] = be;
+}
+
+// PressureNewtonRaphson.updatePressure (:340-359): p += dp, max |dp/p_prev|
+__global__ void k_update_pressure(SimDev d, double* dp, const int* locked, const double* p_prev,
+                                  unsigned long long* dpmax_bits, int* bad_row, double* dp0) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  if (locked[i]) dp[i] = 0;  // LinearSolver.solve: x[locked] = 0
+  double dpi = dp[i];
+  double pn = d.p[i] + dpi;
+  if (pn <= 0) atomicMin(bad_row, i + 1);
+  d.p[i] = pn;
+  double r = fabs(dpi / p_prev[i]);
+  atomicMax(dpmax_bits, (unsigned long long)__double_as_longlong(r));
+  if (i == 0) *dp0 = dpi;
+}
+
+// MolarMassExplicit.calculateMolarMassFlux per connection
+__global__ void k_molar_conn(SimDev d, ConnDev c, double* cf) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.nconn) return;
+  const int n = d.n, nc = d.nc, ncn = d.nconn;
+  double flux[NCM];
+  for (int nu = 0; nu < nc; ++nu) flux[nu] = 0;
+  for (int a = 0; a < 3; ++a) {
+    int up = c.up[(int64_t)a * ncn + q];
+    if (!((d.present[up] >> a) & 1)) continue;
+    double D = c.u[(int64_t)a * ncn + q];
+    for (int nu = 0; nu < nc; ++nu) flux[nu] += d.Cxi[((int64_t)nu * 3 + a) * n + up] * D;
+  }
+  for (int nu = 0; nu < nc; ++nu) cf[(int64_t)nu * ncn + q] = flux[nu];
+}
+
+// dN gather, sources, locks, update with the negative-moles test
+__global__ void k_molar_cells(SimDev d, AsmDev a, const double* cf, double dt, const double* N_prev, int truncate,
+                              int* bad_row, double* dN_out) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.n) return;
+  const int n = d.n, nc = d.nc, ncn = d.nconn;
+  double dN[NCM];
+  for (int nu = 0; nu < nc; ++nu) dN[nu] = 0;
+  for (int k = 0; k < a.ccount[e]; ++k) {
+    const int code = a.cc[(int64_t)e * 6 + k];
+    const int c = code >> 1;
+    const bool here = !(code & 1);
+    for (int nu = 0; nu < nc; ++nu) {
+      double f = cf[(int64_t)nu * ncn + c];
+      if (here) dN[nu] -= dt * f;
+      else dN[nu] += dt * f;
+    }
+  }
+  for (int s = a.src_ptr[e]; s < a.src_ptr[e + 1]; ++s) {
+    const double* q = a.src_q + (int64_t)a.src_id[s] * NCM;
+    for (int nu = 0; nu < nc; ++nu) dN[nu] += dt * q[nu];
+  }
+  for (int nu = 0; nu < nc; ++nu) dN_out[(int64_t)nu * n + e] = dN[nu];
+  if (a.locked[e])
+    for (int nu = 0; nu < nc; ++nu) dN[nu] = 0;
+  for (int nu = 0; nu < nc; ++nu) {
+    double Nold = N_prev[(int64_t)nu * n + e];
+    double Nnew = Nold + dN[nu];
+    if (Nnew < 0) {
+      if (truncate) Nnew = 0;
+      else atomicMin(bad_row, e + 1);
+    }
+    d.N[(int64_t)nu * n + e] = Nnew;
+  }
+}
+
+// Field.volumeBalance (field/Field.java:390-447) per cell
+struct InitDev {
+  double datum_depth, datum_pressure;
+  DFunc temperature;
+  DFunc frac[NCM];
+  const double* zc;     // cell centre z
+  const int* fixed_id;  // fixed source per cell (-1 none); the last one listed wins
+  const double* fixed_T;
+  const double* fixed_C;  // nsrc x NCM, normalised
+};
+
+__device__ void volume_balance(const SimDev& d, const InitDev& in, int i, const double* C, double p, double T) {
+  const int nc = d.nc, n = d.n;
+  double N[NCM];
+  for (int nu = 0; nu < nc; ++nu) N[nu] = 1 * C[nu];
+  double dz = in.zc[i] - in.datum_depth;
+  double p0 = p;
+  cv_cell(d, i, p, p0, T, N);
+  int iters = 0;
+  do {
+    double dRdNt = 0;
+    for (int nu = 0; nu < nc; ++nu) dRdNt += d.dRdN[(int64_t)nu * n + i] * C[nu];
+    if (dRdNt == 0) {
+      atomicCAS(d.flag, 0, FL_DRDP);
+      return;
+    }
+    double Nt = 0;
+    for (int nu = 0; nu < nc; ++nu) Nt += N[nu];
+    double dNt = -d.R[i] / dRdNt;
+    double alpha = 1;
+    for (int h = 0; h < 2100 && Nt + alpha * dNt < 0; ++h) alpha /= 2;
+    Nt += alpha * dNt;
+    for (int nu = 0; nu < nc; ++nu) N[nu] = Nt * C[nu];
+    double pp = in.datum_pressure;
+    for (int a = 0; a < 3; ++a) pp -= G_ACC * d.rho[(int64_t)a * n + i] * d.S[(int64_t)a * n + i] * dz;
+    p = pp;
+    p0 = pp;
+    cv_cell(d, i, p, p0, T, N);
+    iters++;
+  } while (iters < 3 || (fabs(d.R[i]) > 1.0e-9 && iters < 50));
+  d.p[i] = p;
+  d.p0[i] = p0;
+  d.T[i] = T;
+  for (int nu = 0; nu < nc; ++nu) d.N[(int64_t)nu * n + i] = N[nu];
+}
+
+__global__ void k_init(SimDev d, InitDev in) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const int nc = d.nc;
+  double z = in.zc[i];
+  double C[NCM];
+  double sum = 0;
+  double T = f_eval(in.temperature, -1, &z);
+  for (int nu = 0; nu < nc; ++nu) {
+    C[nu] = f_eval(in.frac[nu], -1, &z);
+    sum += C[nu];
+  }
+  if (sum == 0) {
+    C[0] = 1;
+    sum = 1;
+  }
+  for (int nu = 0; nu < nc; ++nu) C[nu] /= sum;
+  volume_balance(d, in, i, C, in.datum_pressure, T);
+  int f = in.fixed_id[i];
+  if (f >= 0) {
+    double Cf[NCM];
+    for (int nu = 0; nu < nc; ++nu) Cf[nu] = in.fixed_C[(int64_t)f * NCM + nu];
+    volume_balance(d, in, i, Cf, in.datum_pressure, in.fixed_T[f]);
+  }
+}
+
+__global__ void k_copy(int64_t n, const double* __restrict__ a, double* __restrict__ b) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+__global__ void k_zero(int64_t n, double* __restrict__ a) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = 0;
+}
+
+// deterministic per-block partial sums of dN (mass balance diagnostic)
+__global__ void k_sum_blocks(int64_t n, const double* __restrict__ a, double* part) {
+  __shared__ double sh[256];
+  double s = 0;
+  for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) s += a[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------
+struct HostFunc {
+  DFunc d{};
+  DeviceBuffer<double> coord[3], data;
+};
+
+static void upload_func(Context& ctx, const rsg_function& f, HostFunc& h) {
+  h.d.kind = f.kind;
+  h.d.dim = f.dim;
+  h.d.value = f.value;
+  if (f.kind == RSG_FN_CONSTANT) return;
+  if (f.kind != RSG_FN_TABLE && f.kind != RSG_FN_EVEN_TABLE) throw Error(RSG_BAD_ARG, "unknown function kind");
+  if (f.dim < 1 || f.dim > 3) throw Error(RSG_BAD_ARG, "table dimension must be 1..3");
+  size_t total = 1;
+  for (int d = 0; d < f.dim; ++d) {
+    if (f.n[d] < 2) throw Error(RSG_BAD_ARG, "table needs two points per axis");
+    h.d.n[d] = f.n[d];
+    total *= (size_t)f.n[d];
+    std::vector<double> c(f.n[d]);
+    if (f.kind == RSG_FN_TABLE) {
+      for (int j = 0; j < f.n[d]; ++j) c[j] = f.coord[d][j];
+      for (int j = 1; j < f.n[d]; ++j)
+        if (c[j] <= c[j - 1]) throw Error(RSG_BAD_ARG, "table coordinates must be increasing");
+    } else {
+      h.d.offset[d] = f.coord[d][0];
+      h.d.delta[d] = (f.coord[d][1] - h.d.offset[d]) / (f.n[d] - 1);
+      c[0] = h.d.offset[d];
+      for (int j = 1; j < f.n[d]; ++j) c[j] = c[j - 1] + h.d.delta[d];
+    }
+    h.coord[d].resize(c.size());
+    RSG_CUDA(cudaMemcpyAsync(h.coord[d].get(), c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice, ctx.stream));
+    h.d.coord[d] = h.coord[d].get();
+  }
+  h.data.resize(total);
+  RSG_CUDA(cudaMemcpyAsync(h.data.get(), f.data, sizeof(double) * total, cudaMemcpyHostToDevice, ctx.stream));
+  h.d.data = h.data.get();
+  ctx.sync();
+}
+
+static double fmin_out(const rsg_function& f) {
+  if (f.kind == RSG_FN_CONSTANT) return f.value;
+  size_t total = 1;
+  for (int d = 0; d < f.dim; ++d) total *= (size_t)f.n[d];
+  return *std::min_element(f.data, f.data + total);
+}
+static double fmax_out(const rsg_function& f) {
+  if (f.kind == RSG_FN_CONSTANT) return f.value;
+  size_t total = 1;
+  for (int d = 0; d < f.dim; ++d) total *= (size_t)f.n[d];
+  return *std::max_element(f.data, f.data + total);
+}
+
+struct Sim {
+  Context* ctx;
+  Mesh* mesh;
+  rsg_runspec spec;
+  int n, nc, nconn;
+  HostFunc funcs[11];
+  HostFunc initT, initC[NCM];
+  DFluid fl{};
+  DCorey co{};
+  DeviceBuffer<double> phi0, cr, bf, zc;
+  DeviceBuffer<double> p, p0, T, N, phN, phdVdN, S, rho, lambda, Cxi, xi, R, dRdp, dRdN, pcow, pcgo;
+  DeviceBuffer<int> present, flag, locked, src_ptr, src_id, bad_row, fixed_id;
+  DeviceBuffer<double> src_q, fixed_T, fixed_C;
+  DeviceBuffer<double> rho_cs, u, Jh, Jt, rh, rt, cf, dNbuf, part;
+  DeviceBuffer<int> up;
+  DeviceBuffer<double> p_prev, p0_prev, T_prev, R_prev, N_prev, dp, b;
+  DeviceBuffer<double> rawJ, rawB;
+  DeviceBuffer<unsigned long long> dpmax_bits;
+  DeviceBuffer<double> dp0;
+  rsg_csr A;
+  SolverPtr solver;
+  std::vector<double> h_src_total;  // dt-independent sum of regular source rates per component
+  bool keep_jacobian = false;
+
+  SimDev dev() {
+    SimDev d;
+    d.n = n;
+    d.nc = nc;
+    d.nconn = nconn;
+    d.fl = fl;
+    d.co = co;
+    d.phi0 = phi0.get();
+    d.cr = cr.get();
+    d.vol = mesh->evol.get();
+    d.bf = bf.get();
+    d.p = p.get();
+    d.p0 = p0.get();
+    d.T = T.get();
+    d.N = N.get();
+    d.phN = phN.get();
+    d.phdVdN = phdVdN.get();
+    d.S = S.get();
+    d.rho = rho.get();
+    d.lambda = lambda.get();
+    d.Cxi = Cxi.get();
+    d.xi = xi.get();
+    d.R = R.get();
+    d.dRdp = dRdp.get();
+    d.dRdN = dRdN.get();
+    d.pcow = pcow.get();
+    d.pcgo = pcgo.get();
+    d.present = present.get();
+    d.flag = flag.get();
+    return d;
+  }
+  ConnDev cdev() {
+    return ConnDev{mesh->conn.get(), mesh->md_ptr.get(), mesh->md_elem.get(), mesh->md_k.get(),
+                   rho_cs.get(),     u.get(),            up.get()};
+  }
+  AsmDev adev() {
+    return AsmDev{mesh->cell_conn.get(), mesh->cell_conn_ptr.get(), mesh->md_ptr.get(), mesh->md_pos_here.get(),
+                  mesh->md_pos_there.get(), A.m.rowptr.get(), A.m.diag.get(), src_ptr.get(), src_id.get(),
+                  src_q.get(), locked.get(), p_prev.get(), R_prev.get()};
+  }
+
+  void check_flag() {
+    int h = 0;
+    RSG_CUDA(cudaMemcpyAsync(&h, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    if (h == FL_DRDP) throw Error(RSG_PHYSICS, "dR/dp must be positive (check PVT data or datum depth/pressure)");
+    if (h) throw Error(RSG_PHYSICS, "equation-of-state data check failed (code " + std::to_string(h) + ")");
+  }
+
+  void secondaries() {
+    SimDev d = dev();
+    RSG_LAUNCH(*ctx, "cv", k_cv, blocks_for(n, 128), 128, 0, d);
+    RSG_LAUNCH(*ctx, "cs", k_cs, blocks_for(nconn, 128), 128, 0, d, cdev());
+  }
+
+  void copy(const DeviceBuffer<double>& a, DeviceBuffer<double>& b, int64_t count) {
+    RSG_LAUNCH(*ctx, "copy", k_copy, blocks_for(count, 256), 256, 0, count, a.get(), b.get());
+  }
+
+  void store_state() {
+    copy(p, p_prev, n);
+    copy(p0, p0_prev, n);
+    copy(T, T_prev, n);
+    copy(R, R_prev, n);
+    copy(N, N_prev, (int64_t)nc * n);
+  }
+
+  void step(double dt, rsg_step_info* info) {
+    if (!(dt > 0)) throw Error(RSG_BAD_ARG, "time step must be positive");
+    store_state();
+    int its = 0, lin = 0;
+    double dpMax = 0, dp0h = 0;
+    const bool ref_rule = spec.newton_stop_rule == 0;
+    for (;;) {
+      SimDev d = dev();
+      RSG_LAUNCH(*ctx, "flux_conn", k_flux_conn, blocks_for(nconn, 128), 128, 0, d, cdev(), Jh.get(), Jt.get(),
+                 rh.get(), rt.get());
+      RSG_LAUNCH(*ctx, "assemble_rows", k_assemble_rows, blocks_for(n, 128), 128, 0, d, adev(), Jh.get(), Jt.get(),
+                 rh.get(), rt.get(), dt, A.m.val.get(), b.get(), keep_jacobian ? rawJ.get() : nullptr,
+                 keep_jacobian ? rawB.get() : nullptr);
+      A.m.sell_dirty = true;
+      RSG_LAUNCH(*ctx, "zero", k_zero, blocks_for(n, 256), 256, 0, (int64_t)n, dp.get());
+      rsg_solve_info si{};
+      solver_setup(*solver, A.m);
+      solver_solve(*solver, A.m, b.get(), dp.get(), &si);
+      lin += si.iterations;
+      RSG_CUDA(cudaMemsetAsync(dpmax_bits.get(), 0, sizeof(unsigned long long), ctx->stream));
+      int big = INT32_MAX;
+      RSG_CUDA(cudaMemcpyAsync(bad_row.get(), &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+      RSG_LAUNCH(*ctx, "update_pressure", k_update_pressure, blocks_for(n, 256), 256, 0, d, dp.get(), locked.get(),
+                 p_prev.get(), dpmax_bits.get(), bad_row.get(), dp0.get());
+      secondaries();
+      unsigned long long bits = 0;
+      int bad = 0;
+      RSG_CUDA(cudaMemcpyAsync(&bits, dpmax_bits.get(), sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+      RSG_CUDA(cudaMemcpyAsync(&dp0h, dp0.get(), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      RSG_CUDA(cudaMemcpyAsync(&bad, bad_row.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      ctx->sync();
+      std::memcpy(&dpMax, &bits, sizeof(double));
+      if (bad != INT32_MAX)
+        throw Error(RSG_NONPOSITIVE_PRESSURE, "Non-positive pressure in element " + std::to_string(bad));
+      check_flag();
+      ++its;
+      bool conv = ref_rule ? (dp0h < spec.pressure_tolerance) : (dpMax < spec.pressure_tolerance);
+      if (conv) break;
+      if (its >= spec.max_nonlinear_pressure_iterations)
+        throw Error(RSG_NEWTON_NOT_CONVERGED, "Nonlinear pressure solver failed to converge");
+    }
+    // MolarMassExplicit.solve
+    SimDev d = dev();
+    RSG_LAUNCH(*ctx, "molar_conn", k_molar_conn, blocks_for(nconn, 128), 128, 0, d, cdev(), cf.get());
+    int big = INT32_MAX;
+    RSG_CUDA(cudaMemcpyAsync(bad_row.get(), &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    RSG_LAUNCH(*ctx, "molar_cells", k_molar_cells, blocks_for(n, 128), 128, 0, d, adev(), cf.get(), dt, N_prev.get(),
+               spec.truncate_negative_moles, bad_row.get(), dNbuf.get());
+    int bad = 0;
+    RSG_CUDA(cudaMemcpyAsync(&bad, bad_row.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    if (bad != INT32_MAX) throw Error(RSG_NEGATIVE_MOLES, "Negative number of moles in element " + std::to_string(bad));
+    secondaries();
+    if (info) {
+      info->newton_iterations = its;
+      info->linear_iterations = lin;
+      info->dp_max = dpMax;
+      info->dp0 = dp0h;
+      info->status = RSG_OK;
+      info->mass_balance_error = mass_balance(dt);
+    }
+    check_flag();
+  }
+
+  double mass_balance(double dt) {
+    // |sum_i dN_i - dt * sum(sources)| / sum_i N_i per component, worst one
+    const int nb = 256;
+    part.resize((size_t)2 * nb);
+    std::vector<double> hp(2 * nb);
+    double worst = 0;
+    for (int nu = 0; nu < nc; ++nu) {
+      RSG_LAUNCH(*ctx, "sum_blocks", k_sum_blocks, nb, 256, 0, (int64_t)n, dNbuf.get() + (int64_t)nu * n, part.get());
+      RSG_LAUNCH(*ctx, "sum_blocks", k_sum_blocks, nb, 256, 0, (int64_t)n, N_prev.get() + (int64_t)nu * n,
+                 part.get() + nb);
+      RSG_CUDA(cudaMemcpyAsync(hp.data(), part.get(), sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, ctx->stream));
+      ctx->sync();
+      double s = 0, tot = 0;
+      for (int q = 0; q < nb; ++q) {
+        s += hp[q];
+        tot += hp[nb + q];
+      }
+      s -= dt * h_src_total[nu];
+      if (tot > 0) worst = std::max(worst, std::fabs(s) / tot);
+    }
+    return worst;
+  }
+
+  void retract() {
+    copy(p_prev, p, n);
+    copy(T_prev, T, n);
+    copy(N_prev, N, (int64_t)nc * n);
+    secondaries();
+    ctx->sync();
+  }
+};
+
+}  // namespace rsg
+
+struct rsg_sim {
+  std::unique_ptr<rsg::Sim> s;
+};
+
+using rsg::guarded;
+
+extern "C" {
+
+rsg_status rsg_sim_create(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_blackoil* fluid, const rsg_corey* rf,
+                          const double* porosity, const double* compaction, int32_t nsources,
+                          const rsg_source* sources, const rsg_initial* init, const rsg_runspec* spec, rsg_sim** out) {
+  if (!ctx || !mesh || !fluid || !rf || !porosity || !compaction || !init || !spec || !out) return RSG_BAD_ARG;
+  if (nsources < 0 || (nsources > 0 && !sources)) return RSG_BAD_ARG;
+  if (!mesh->m.have_md) return RSG_BAD_ARG;
+  *out = nullptr;
+  rsg_sim* h = new rsg_sim();
+  rsg_status st = guarded(&ctx->c, [&] {
+    using namespace rsg;
+    h->s.reset(new Sim());
+    Sim& S = *h->s;
+    Context& c = ctx->c;
+    S.ctx = &c;
+    S.mesh = &mesh->m;
+    S.spec = *spec;
+    S.n = mesh->m.g.nel;
+    S.nconn = mesh->m.g.nconn;
+    S.nc = fluid->nc;
+    const int n = S.n, nc = S.nc;
+    if (nc < 1 || nc > RSG_MAX_COMPONENTS) throw Error(RSG_BAD_ARG, "component count");
+    // fluid (BlackOilEquationOfState constructor checks)
+    const rsg_function* fs[11] = {&fluid->water_density, &fluid->water_viscosity, &fluid->water_enthalpy,
+                                  &fluid->bubble_point,  &fluid->dew_point,       &fluid->oil_density,
+                                  &fluid->gas_density,   &fluid->oil_viscosity,   &fluid->gas_viscosity,
+                                  &fluid->oil_enthalpy,  &fluid->gas_enthalpy};
+    for (int q = 0; q < 11; ++q) upload_func(c, *fs[q], S.funcs[q]);
+    if (fmin_out(fluid->water_density) <= 0 || fmin_out(fluid->water_viscosity) <= 0 ||
+        fmin_out(fluid->oil_density) <= 0 || fmin_out(fluid->gas_density) <= 0 ||
+        fmin_out(fluid->oil_viscosity) <= 0 || fmin_out(fluid->gas_viscosity) <= 0)
+      throw Error(RSG_BAD_ARG, "densities and viscosities must be positive");
+    if (fmin_out(fluid->bubble_point) < 0 || fmax_out(fluid->bubble_point) > 1 || fmin_out(fluid->dew_point) < 0 ||
+        fmax_out(fluid->dew_point) > 1)
+      throw Error(RSG_BAD_ARG, "bubble/dew point curves must be in [0,1]");
+    DFluid& fl = S.fl;
+    fl.nc = nc;
+    fl.ngO = fl.ngG = 0;
+    for (int i = 0; i < nc; ++i) {
+      fl.Mw[i] = fluid->molecular_weight[i];
+      if (i == 0 && fluid->group[i] != 0) throw Error(RSG_BAD_ARG, "The water component may not be grouped");
+      if (i > 0 && fluid->group[i] == 1) fl.O[fl.ngO++] = i;
+      else if (i > 0 && fluid->group[i] == 2) fl.G[fl.ngG++] = i;
+      else if (i > 0) throw Error(RSG_BAD_ARG, "component has not been grouped");
+    }
+    DFunc* dst[11] = {&fl.wden, &fl.wvis, &fl.went, &fl.bub, &fl.dew, &fl.oden,
+                      &fl.gden, &fl.ovis, &fl.gvis, &fl.oent, &fl.gent};
+    for (int q = 0; q < 11; ++q) *dst[q] = S.funcs[q].d;
+    for (int a = 0; a < 3; ++a) {
+      S.co.Sr[a] = rf->Sr[a];
+      S.co.n[a] = rf->n[a];
+      S.co.ke[a] = rf->ke[a];
+    }
+    S.co.cw = rf->cw;
+    S.co.cow = rf->cow;
+    S.co.cg = rf->cg;
+    S.co.cog = rf->cog;
+    S.co.aw = rf->aw;
+    S.co.aow = rf->aow;
+    S.co.ag = rf->ag;
+    S.co.aog = rf->aog;
+    for (int i = 0; i < n; ++i)
+      if (porosity[i] < 0 || porosity[i] > 1 || compaction[i] < 0) throw Error(RSG_BAD_ARG, "rock data out of range");
+    auto up = [&](DeviceBuffer<double>& dbuf, const double* hsrc, size_t count) {
+      dbuf.resize(count);
+      RSG_CUDA(cudaMemcpyAsync(dbuf.get(), hsrc, sizeof(double) * count, cudaMemcpyHostToDevice, c.stream));
+    };
+    up(S.phi0, porosity, n);
+    up(S.cr, compaction, n);
+    // body force and centre z
+    std::vector<double> centers((size_t)3 * n);
+    RSG_CUDA(cudaMemcpyAsync(centers.data(), mesh->m.ecenter.get(), sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
+                             c.stream));
+    c.sync();
+    std::vector<double> bfh(n), zh(n);
+    for (int i = 0; i < n; ++i) {
+      double x = centers[3 * i], y = centers[3 * i + 1], z = centers[3 * i + 2];
+      double distance = (spec->ax - x) * (spec->ax - x) + (spec->ay - y) * (spec->ay - y);
+      bfh[i] = G_ACC * z - (spec->omega * spec->omega / 2) * distance;
+      zh[i] = z;
+    }
+    up(S.bf, bfh.data(), n);
+    up(S.zc, zh.data(), n);
+    // state buffers
+    for (auto* b : {&S.p, &S.p0, &S.T, &S.R, &S.dRdp, &S.pcow, &S.pcgo, &S.p_prev, &S.p0_prev, &S.T_prev, &S.R_prev,
+                    &S.dp, &S.b})
+      b->resize(n);
+    S.N.resize((size_t)nc * n);
+    S.N_prev.resize((size_t)nc * n);
+    S.dRdN.resize((size_t)nc * n);
+    S.dNbuf.resize((size_t)nc * n);
+    S.phN.resize((size_t)nc * 3 * n);
+    S.phdVdN.resize((size_t)nc * 3 * n);
+    S.Cxi.resize((size_t)nc * 3 * n);
+    for (auto* b : {&S.S, &S.rho, &S.lambda, &S.xi}) b->resize((size_t)3 * n);
+    RSG_CUDA(cudaMemsetAsync(S.phN.get(), 0, sizeof(double) * S.phN.size(), c.stream));
+    RSG_CUDA(cudaMemsetAsync(S.phdVdN.get(), 0, sizeof(double) * S.phdVdN.size(), c.stream));
+    S.present.resize(n);
+    RSG_CUDA(cudaMemsetAsync(S.present.get(), 0, sizeof(int) * n, c.stream));
+    S.flag.resize(1);
+    RSG_CUDA(cudaMemsetAsync(S.flag.get(), 0, sizeof(int), c.stream));
+    S.bad_row.resize(1);
+    S.dpmax_bits.resize(1);
+    S.dp0.resize(1);
+    const int64_t nmd = mesh->m.nmd;
+    S.rho_cs.resize((size_t)3 * S.nconn);
+    S.u.resize((size_t)3 * S.nconn);
+    S.up.resize((size_t)3 * S.nconn);
+    S.Jh.resize(std::max<int64_t>(nmd, 1));
+    S.Jt.resize(std::max<int64_t>(nmd, 1));
+    S.rh.resize(S.nconn);
+    S.rt.resize(S.nconn);
+    S.cf.resize((size_t)nc * S.nconn);
+    // sources
+    std::vector<std::vector<int>> cell_src(n);
+    std::vector<double> q((size_t)std::max(nsources, 1) * RSG_MAX_COMPONENTS, 0.0);
+    std::vector<int> lockh(n, 0), fixed(n, -1);
+    std::vector<double> fT(std::max(nsources, 1), 0.0), fC((size_t)std::max(nsources, 1) * RSG_MAX_COMPONENTS, 0.0);
+    S.h_src_total.assign(nc, 0.0);
+    for (int s = 0; s < nsources; ++s) {
+      const rsg_source& src = sources[s];
+      if (src.num_elements < 0 || (src.num_elements > 0 && !src.elements)) throw Error(RSG_BAD_ARG, "source elements");
+      for (int a = 0; a < src.num_elements; ++a)
+        if (src.elements[a] < 0 || src.elements[a] >= n) throw Error(RSG_BAD_ARG, "source element out of range");
+      if (src.type == RSG_SOURCE_REGULAR) {
+        for (int nu = 0; nu < nc; ++nu) {
+          if (src.q[nu] < 0) throw Error(RSG_BAD_ARG, "Mass source cannot be negative");
+          q[(size_t)s * RSG_MAX_COMPONENTS + nu] = src.q[nu];
+          S.h_src_total[nu] += src.q[nu] * src.num_elements;
+        }
+        for (int a = 0; a < src.num_elements; ++a) cell_src[src.elements[a]].push_back(s);
+      } else if (src.type == RSG_SOURCE_FIXED) {
+        double C[RSG_MAX_COMPONENTS], sum = 0;
+        for (int nu = 0; nu < nc; ++nu) {
+          if (src.fraction[nu] < 0) throw Error(RSG_BAD_ARG, "Fraction of component cannot be negative");
+          C[nu] = src.fraction[nu];
+          sum += C[nu];
+        }
+        if (sum == 0) {
+          C[0] = 1;
+          sum = 1;
+        }
+        for (int nu = 0; nu < nc; ++nu) fC[(size_t)s * RSG_MAX_COMPONENTS + nu] = C[nu] / sum;
+        if (src.temperature < 0) throw Error(RSG_BAD_ARG, "Temperature cannot be negative");
+        fT[s] = src.temperature;
+        for (int a = 0; a < src.num_elements; ++a) {
+          lockh[src.elements[a]] = 1;
+          fixed[src.elements[a]] = s;
+        }
+      } else
+        throw Error(RSG_UNSUPPORTED, "source type not supported (outlet sources are broken in RS)");
+    }
+    std::vector<int> sptr(n + 1, 0), sid;
+    for (int i = 0; i < n; ++i) {
+      sptr[i + 1] = sptr[i] + (int)cell_src[i].size();
+      for (int s : cell_src[i]) sid.push_back(s);
+    }
+    if (sid.empty()) sid.push_back(0);
+    S.src_ptr.resize(n + 1);
+    S.src_id.resize(sid.size());
+    S.locked.resize(n);
+    S.fixed_id.resize(n);
+    RSG_CUDA(cudaMemcpyAsync(S.src_ptr.get(), sptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, c.stream));
+    RSG_CUDA(cudaMemcpyAsync(S.src_id.get(), sid.data(), sizeof(int) * sid.size(), cudaMemcpyHostToDevice, c.stream));
+    RSG_CUDA(cudaMemcpyAsync(S.locked.get(), lockh.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
+    RSG_CUDA(cudaMemcpyAsync(S.fixed_id.get(), fixed.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
+    up(S.src_q, q.data(), q.size());
+    up(S.fixed_T, fT.data(), fT.size());
+    up(S.fixed_C, fC.data(), fC.size());
+    // initial values (field/InitialValues.java)
+    if (init->datum_pressure <= 0) throw Error(RSG_BAD_ARG, "Datum pressure must be positive");
+    upload_func(c, init->temperature, S.initT);
+    for (int nu = 0; nu < nc; ++nu) upload_func(c, init->fraction[nu], S.initC[nu]);
+    InitDev in{};
+    in.datum_depth = init->datum_depth;
+    in.datum_pressure = init->datum_pressure;
+    in.temperature = S.initT.d;
+    for (int nu = 0; nu < nc; ++nu) in.frac[nu] = S.initC[nu].d;
+    in.zc = S.zc.get();
+    in.fixed_id = S.fixed_id.get();
+    in.fixed_T = S.fixed_T.get();
+    in.fixed_C = S.fixed_C.get();
+    RSG_LAUNCH(c, "init_volume_balance", k_init, blocks_for(n, 64), 64, 0, S.dev(), in);
+    S.secondaries();
+    S.check_flag();
+    // LinearSolver(runSpec, mesh, locked)
+    S.A.m.build(&c, n, (int)mesh->m.h_pcol.size(), mesh->m.h_prow.data(), mesh->m.h_pcol.data());
+    for (int i = 0; i < n; ++i)
+      if (S.A.m.h_diag[i] < 0) throw Error(RSG_MISSING_DIAGONAL, "pressure pattern lacks a diagonal");
+    S.solver = make_solver(&c, spec->linear_solver, spec->preconditioner, spec->relative_tolerance,
+                                   spec->absolute_tolerance, spec->divergence_tolerance, spec->max_linear_iterations,
+                                   spec->gmres_restart > 0 ? spec->gmres_restart : 30);
+    c.sync();
+  });
+  if (st != RSG_OK) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return RSG_OK;
+}
+
+rsg_status rsg_sim_destroy(rsg_sim* s) {
+  if (!s) return RSG_BAD_ARG;
+  if (s->s) cudaStreamSynchronize(s->s->ctx->stream);
+  delete s;
+  return RSG_OK;
+}
+
+rsg_status rsg_sim_step(rsg_sim* s, double dt, rsg_step_info* info) {
+  if (!s) return RSG_BAD_ARG;
+  rsg_status st = guarded(s->s->ctx, [&] { s->s->step(dt, info); });
+  if (info && st != RSG_OK) info->status = st;
+  return st;
+}
+
+rsg_status rsg_sim_retract(rsg_sim* s) {
+  if (!s) return RSG_BAD_ARG;
+  return guarded(s->s->ctx, [&] { s->s->retract(); });
+}
+
+rsg_status rsg_sim_get_state(rsg_sim* s, double* p, double* N, double* S) {
+  if (!s) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    if (p) RSG_CUDA(cudaMemcpyAsync(p, m.p.get(), sizeof(double) * m.n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    if (N)
+      RSG_CUDA(cudaMemcpyAsync(N, m.N.get(), sizeof(double) * m.nc * m.n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    if (S) RSG_CUDA(cudaMemcpyAsync(S, m.S.get(), sizeof(double) * 3 * m.n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    m.ctx->sync();
+  });
+}
+
+rsg_status rsg_sim_set_state(rsg_sim* s, const double* p, const double* N) {
+  if (!s) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    if (p) RSG_CUDA(cudaMemcpyAsync(m.p.get(), p, sizeof(double) * m.n, cudaMemcpyHostToDevice, m.ctx->stream));
+    if (N)
+      RSG_CUDA(cudaMemcpyAsync(m.N.get(), N, sizeof(double) * m.nc * m.n, cudaMemcpyHostToDevice, m.ctx->stream));
+    m.secondaries();
+    m.check_flag();
+  });
+}
+
+rsg_status rsg_sim_get_jacobian(rsg_sim* s, double* values, double* rhs) {
+  if (!s) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    if (!m.keep_jacobian) {
+      m.keep_jacobian = true;
+      m.rawJ.resize(std::max(m.A.m.nnz, 1));
+      m.rawB.resize(m.n);
+      throw rsg::Error(RSG_BAD_ARG, "Jacobian capture enabled; it is available after the next step");
+    }
+    if (values)
+      RSG_CUDA(cudaMemcpyAsync(values, m.rawJ.get(), sizeof(double) * m.A.m.nnz, cudaMemcpyDeviceToHost,
+                               m.ctx->stream));
+    if (rhs) RSG_CUDA(cudaMemcpyAsync(rhs, m.rawB.get(), sizeof(double) * m.n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    m.ctx->sync();
+  });
+}
+
+rsg_status rsg_sim_get_residual_volume(rsg_sim* s, double* R, double* dRdp) {
+  if (!s) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    if (R) RSG_CUDA(cudaMemcpyAsync(R, m.R.get(), sizeof(double) * m.n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    if (dRdp)
+      RSG_CUDA(cudaMemcpyAsync(dRdp, m.dRdp.get(), sizeof(double) * m.n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    m.ctx->sync();
+  });
+}
+
+}  // extern "C"

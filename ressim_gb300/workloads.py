@@ -1,0 +1,235 @@
+"""Seeded synthetic inputs for the RS pressure path.
+
+The reference publishes no datasets for these cases; every input is generated
+here from a seed with numpy's PCG64 so that the GPU library and the CPU
+oracle consume identical bytes:
+
+* ``grf``: stationary Gaussian random field with squared-exponential
+  covariance, sampled by FFT circulant embedding on a 2x padded torus;
+* ``potential_case``: 2D single-phase incompressible potential problem
+  (MPFA-O, full anisotropic tensor, Dirichlet columns, injector/producer);
+* ``two_phase_case``: 3D oil/water black-oil problem on a perturbed hexahedral
+  grid with a lognormal permeability field and a five-spot well pattern.
+
+Units are SI as in RS (Pa, m^2, Pa*s, K, mol).
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+MILLIDARCY = 9.869233e-16  # m^2
+BAR = 1.0e5  # Pa
+CENTIPOISE = 1.0e-3  # Pa*s
+
+
+def rng(seed):
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def grf(shape, corr_len, mean, std, seed):
+    """Gaussian random field on a grid of `shape` cells (1 to 3 axes)."""
+    g = rng(seed)
+    pad = [2 * s for s in shape]
+    axes = [np.minimum(np.arange(p), p - np.arange(p)).astype(np.float64) for p in pad]
+    mesh = np.meshgrid(*axes, indexing="ij")
+    h2 = sum(m * m for m in mesh)
+    cov = (std * std) * np.exp(-h2 / (corr_len * corr_len))
+    lam = np.fft.fftn(cov).real
+    lam = np.maximum(lam, 0.0)
+    eps = g.standard_normal(pad) + 1j * g.standard_normal(pad)
+    y = np.fft.fftn(np.sqrt(lam / lam.size) * eps)
+    field = y.real[tuple(slice(0, s) for s in shape)]
+    return mean + field
+
+
+def _cells_ijk_to_linear(field_ijk):
+    """RS numbers cells i fastest (NaturalIJKOrdering.getLinear)."""
+    return np.ascontiguousarray(field_ijk.transpose(*reversed(range(field_ijk.ndim))).reshape(-1))
+
+
+# --------------------------------------------------------------- 2D case ---
+def potential_case(ni=64, nj=64, seed=0, corr_len=8.0, angle_deg=30.0, anisotropy=10.0, rate=1.0e-13):
+    """Single-phase incompressible potential problem (numerics/PotentialCalculator).
+
+    Returns a dict with the grid, the permeability tensors (6 per cell), the
+    Dirichlet cells/values and the right-hand-side rate terms.
+    """
+    logk = grf((ni, nj), corr_len, 2.0, 1.0, seed)  # log10 kmax [mD]
+    kmax = _cells_ijk_to_linear(10.0 ** logk) * MILLIDARCY
+    kmin = kmax / anisotropy
+    a = math.radians(angle_deg)
+    c, s = math.cos(a), math.sin(a)
+    # K = R diag(kmax, kmin) R^T
+    kxx = c * c * kmax + s * s * kmin
+    kyy = s * s * kmax + c * c * kmin
+    kxy = c * s * (kmax - kmin)
+    n = ni * nj
+    perm = np.zeros((n, 6))
+    perm[:, 0] = kxx
+    perm[:, 1] = kyy
+    perm[:, 2] = kmin  # permz must be present for RockDataParser to build a tensor
+    perm[:, 3] = kxy
+    dirichlet_cells = []
+    dirichlet_values = []
+    for j in range(nj):
+        dirichlet_cells.append(0 + j * ni)
+        dirichlet_values.append(1.0)
+    for j in range(nj):
+        dirichlet_cells.append((ni - 1) + j * ni)
+        dirichlet_values.append(0.0)
+    # The corner cells (0,0) and (ni-1,nj-1) are Dirichlet cells, so the
+    # injector/producer pair sits one column inside: (1,0) and (ni-2,nj-1).
+    rates = {1 + 0 * ni: rate, (ni - 2) + (nj - 1) * ni: -rate}
+    return dict(
+        dim=2, ni=ni, nj=nj, nk=0, dx=1.0, dy=1.0, dz=-1.0, perm=np.ascontiguousarray(perm),
+        porosity=np.full(n, 0.2), dirichlet_cells=np.array(dirichlet_cells, dtype=np.int32),
+        dirichlet_values=np.array(dirichlet_values), rates=rates, seed=seed,
+    )
+
+
+def potential_rhs(case):
+    n = case["ni"] * case["nj"]
+    b = np.zeros(n)
+    for cell, q in case["rates"].items():
+        b[cell] += q
+    for cell, v in zip(case["dirichlet_cells"], case["dirichlet_values"]):
+        b[cell] = v
+    return b
+
+
+# --------------------------------------------------------------- 3D case ---
+def perturbed_nodes(ni, nj, nk, dx, dy, dz, frac, seed):
+    """Corner points of an ni x nj x nk grid (i fastest), each displaced by
+    U(-frac, frac) of the cell size along every axis."""
+    g = rng(seed)
+    npi, npj, npk = ni + 1, nj + 1, nk + 1
+    k, j, i = np.meshgrid(np.arange(npk), np.arange(npj), np.arange(npi), indexing="ij")
+    x = i * dx + g.uniform(-frac, frac, i.shape) * dx
+    y = j * dy + g.uniform(-frac, frac, i.shape) * dy
+    z = k * dz + g.uniform(-frac, frac, i.shape) * abs(dz)
+    pts = np.stack([x.reshape(-1), y.reshape(-1), z.reshape(-1)], axis=1)
+    return np.ascontiguousarray(pts)
+
+
+def two_phase_fluid(keep, p_range=(20 * BAR, 600 * BAR), n_p=64):
+    """Oil/water black-oil fluid: exponential compressibility tables for the
+    molar densities (4e-5 /bar water, 1e-4 /bar oil), constant viscosities
+    (1 cP water, 5 cP oil), no gas component, no mass transfer."""
+    p0 = 200 * BAR
+    ps = np.linspace(p_range[0], p_range[1], n_p)
+    Ts = np.array([250.0, 450.0])
+    Cs = np.array([0.0, 1.0])
+    xiw0, cw = 1000.0 / 0.01801528, 4.0e-5 / BAR
+    xio0, co = 800.0 / 0.2, 1.0e-4 / BAR
+    xiw = np.repeat((xiw0 * np.exp(cw * (ps - p0)))[:, None], 2, axis=1)
+    xio = np.repeat(np.repeat((xio0 * np.exp(co * (ps - p0)))[:, None, None], 2, axis=1), 2, axis=2)
+    f = abi.rsg_blackoil()
+    f.nc = 2
+    f.molecular_weight[0] = 0.01801528
+    f.molecular_weight[1] = 0.2
+    f.group[0] = 0
+    f.group[1] = 1
+    f.water_density = abi.table(keep, [ps, Ts], xiw)
+    f.water_viscosity = abi.constant(1.0 * CENTIPOISE, 2)
+    f.water_enthalpy = abi.constant(0.0, 2)
+    f.bubble_point = abi.constant(0.0, 2)
+    f.dew_point = abi.constant(0.0, 2)
+    f.oil_density = abi.table(keep, [ps, Cs, Ts], xio)
+    f.gas_density = abi.constant(100.0, 3)
+    f.oil_viscosity = abi.constant(5.0 * CENTIPOISE, 3)
+    f.gas_viscosity = abi.constant(1.0e-5, 3)
+    f.oil_enthalpy = abi.constant(0.0, 3)
+    f.gas_enthalpy = abi.constant(0.0, 3)
+    return f
+
+
+def corey(swc=0.2, sor=0.2, n=2.0):
+    c = abi.rsg_corey()
+    c.Sr[0], c.Sr[1], c.Sr[2] = swc, sor, 0.0
+    for ph in range(3):
+        c.n[ph] = n
+        c.ke[ph] = 1.0
+    c.aw = c.aow = c.ag = c.aog = 1.0
+    return c
+
+
+def runspec(method=abi.BICGSTAB, precond=abi.PC_ILU, rtol=1e-8, atol=1e-50, max_linear=5000,
+            max_newton=10, ptol=1e-6, stop_rule=0):
+    s = abi.rsg_runspec()
+    s.max_nonlinear_pressure_iterations = max_newton
+    s.pressure_tolerance = ptol
+    s.linear_solver = method
+    s.preconditioner = precond
+    s.max_linear_iterations = max_linear
+    s.relative_tolerance = rtol
+    s.absolute_tolerance = atol
+    s.divergence_tolerance = 1e5
+    s.truncate_negative_moles = 0
+    s.newton_stop_rule = stop_rule
+    s.gmres_restart = 30
+    return s
+
+
+def two_phase_case(ni=128, nj=128, nk=32, seed=1, perturb=0.1, corr_len=8.0, kz_ratio=0.1, sw0=0.25,
+                   rate_m3_per_day=0.02, dt=8640.0):
+    """3D oil/water case (five-spot: four corner injector columns as Regular
+    sources, a centre producer column as a Fixed source)."""
+    n = ni * nj * nk
+    nodes = perturbed_nodes(ni, nj, nk, 1.0, 1.0, -1.0, perturb, seed)
+    logk = grf((ni, nj, nk), corr_len, 2.0, 1.0, seed + 1000)
+    kx = _cells_ijk_to_linear(10.0 ** logk) * MILLIDARCY
+    perm = np.zeros((n, 6))
+    perm[:, 0] = kx
+    perm[:, 1] = kx
+    perm[:, 2] = kz_ratio * kx
+    poro = rng(seed + 2000).uniform(0.20, 0.30, n)
+    comp = np.zeros(n)
+
+    def column(i, j):
+        return np.array([i + j * ni + k * ni * nj for k in range(nk)], dtype=np.int32)
+
+    injectors = [column(0, 0), column(ni - 1, 0), column(0, nj - 1), column(ni - 1, nj - 1)]
+    producer = column(ni // 2, nj // 2)
+    # initial water/oil mole fractions giving S_w ~ sw0 at 200 bar
+    xiw0, xio0 = 1000.0 / 0.01801528, 800.0 / 0.2
+    nw, no = sw0 * xiw0, (1 - sw0) * xio0
+    cw, co = nw / (nw + no), no / (nw + no)
+    q_water = rate_m3_per_day * xiw0 / 86400.0  # mol/s per injector cell
+    return dict(
+        dim=3, ni=ni, nj=nj, nk=nk, nodes=nodes, perm=np.ascontiguousarray(perm), porosity=poro,
+        compaction=comp, injectors=injectors, producer=producer, fractions=(cw, co), q_water=q_water,
+        temperature=350.0, datum_pressure=200 * BAR, datum_depth=0.0, dt=dt, seed=seed,
+    )
+
+
+def build_sources(keep, case):
+    srcs = (abi.rsg_source * (len(case["injectors"]) + 1))()
+    for a, cells in enumerate(case["injectors"]):
+        arr = keep.i32(cells)
+        srcs[a].type = abi.SOURCE_REGULAR
+        srcs[a].num_elements = len(arr)
+        srcs[a].elements = abi.iptr(arr)
+        srcs[a].q[0] = case["q_water"]
+    arr = keep.i32(case["producer"])
+    last = len(case["injectors"])
+    srcs[last].type = abi.SOURCE_FIXED
+    srcs[last].num_elements = len(arr)
+    srcs[last].elements = abi.iptr(arr)
+    srcs[last].temperature = case["temperature"]
+    srcs[last].fraction[0] = case["fractions"][0]
+    srcs[last].fraction[1] = case["fractions"][1]
+    return srcs
+
+
+def build_initial(case):
+    init = abi.rsg_initial()
+    init.datum_depth = case["datum_depth"]
+    init.datum_pressure = case["datum_pressure"]
+    init.temperature = abi.constant(case["temperature"], 1)
+    init.fraction[0] = abi.constant(case["fractions"][0], 1)
+    init.fraction[1] = abi.constant(case["fractions"][1], 1)
+    for nu in range(2, abi.MAX_COMPONENTS):
+        init.fraction[nu] = abi.constant(0.0, 1)
+    return init
