@@ -160,6 +160,8 @@ def run_resgpu(args, rank, world, local_rank):
 
     # end to end through the public API with page-locked host staging
     nc = sim.nc
+    if args.no_e2e:
+        return finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, None, rank)
     hp = api.PinnedArray(n)
     hN = api.PinnedArray(nc * n)
     hS = api.PinnedArray(3 * n)
@@ -182,13 +184,21 @@ def run_resgpu(args, rank, world, local_rank):
     e2e_units = sum_over_ranks(float(n) * e2e_newton, world)
     h2d = (1 + nc) * n * 8
     d2h = (1 + nc + 3) * n * 8
+    e2e = {"value": e2e_units / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    return finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, e2e, rank)
+
+
+def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, e2e, rank=0):
+    from ressim_gb300 import api
 
     # per-kernel device times from a separate profiled step (not the timed one)
-    ctx.set_profiling(True)
-    ctx.profile_reset()
-    sim.step(dt)
-    prof = ctx.profile()
-    ctx.set_profiling(False)
+    prof = {}
+    if not args.no_kernel_profile:
+        ctx.set_profiling(True)
+        ctx.profile_reset()
+        sim.step(dt)
+        prof = ctx.profile()
+        ctx.set_profiling(False)
     rp, col = mesh.pattern(0)
     lower_b, upper_b = sweep_bytes(rp, col)
     hbm, peak_kind = peaks()
@@ -230,8 +240,10 @@ def run_resgpu(args, rank, world, local_rank):
             "cells": n, "pattern_nnz": len(col), "newton_iterations": newton, "linear_iterations": linear,
             "dt_s": dt, "l2": "matrix and factors (>300 MB) exceed the 129 MB L2", "parallelism": f"replicas x{world}",
         },
-        "e2e": {"value": e2e_units / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": e2e,
         "gpu_launches": launches,
+        "sweep_mode": {-1: "undecided", 0: "one launch per level", 1: "one cluster walks all levels"}.get(
+            api.lib().rsg_sweep_mode()),
         "roofline": roof,
         "spmv": spmv,
         "kernel_shares": shares,
@@ -356,6 +368,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, nargs=3, default=[64, 64, 16])
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
+    ap.add_argument("--no-kernel-profile", action="store_true", help="skip the event-bracketed per-kernel pass")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

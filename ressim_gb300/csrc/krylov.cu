@@ -291,9 +291,10 @@ __global__ void __launch_bounds__(RT) k_spmv_dot(int n, const int* __restrict__ 
     int base = sb[row >> 5] + (row & 31);
     int len = rl[row];
     double d = 0;
+#pragma unroll 8
     for (int k = 0; k < len; ++k) {
       int q = base + 32 * k;
-      d += val[q] * x[col[q]];
+      d += val[q] * __ldg(x + col[q]);
     }
     double yi = (d != 0) ? d : 0.0;
     y[row] = yi;
@@ -506,7 +507,7 @@ struct Solver {
     if (n_ == n && w1.size()) return;
     n = n_;
     for (auto* b : {&w1, &w2, &w3, &w4, &w5, &w6, &w7, &w8, &w9}) b->resize(n);
-    nblk = std::max(1, std::min(blocks_for(n, RT), ctx->num_sms * 4));
+    nblk = std::max(1, std::min(blocks_for(n, RT), 16384));
     part.resize((size_t)4 * nblk);
   }
 

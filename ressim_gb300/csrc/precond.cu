@@ -99,6 +99,114 @@ __global__ void __launch_bounds__(512) k_sweep_cluster(SweepArgs<T> a) {
   }
 }
 
+// ILU sweeps with a three-stage software pipeline per warp: slot metadata
+// (row id, length, slice base) is loaded two levels ahead, the coefficients,
+// column indices, right-hand side and diagonal one level ahead, and only the
+// gathers of already-computed x values (L2 hits written by the previous
+// levels) remain between two cluster barriers.  Loads are predicated rather
+// than branched on, so issuing them never waits for earlier loads.  Rows are
+// summed in CSR order as in the sequential loop.  Each warp owns one slice
+// per level; levels with more slices than warps take the remaining slices
+// through the plain path.
+struct SlotMeta {
+  int row, len, base;
+};
+
+template <typename T, int MAXW>
+struct RowPrefetch {
+  int row, len, base;
+  T b, d;
+  T v[MAXW];
+  int c[MAXW];
+};
+
+template <typename T>
+__device__ __forceinline__ SlotMeta load_meta(const SweepArgs<T>& a, const int* ls, int l, int gwarp, int lane) {
+  SlotMeta m{-1, 0, 0};
+  if (l >= a.nlev) return m;
+  const int s = ls[l] + gwarp;
+  if (s >= ls[l + 1]) return m;
+  const int slot = s * 32 + lane;
+  m.row = a.row[slot];
+  m.len = a.len[slot];
+  m.base = a.slice_base[s] + lane;
+  return m;
+}
+
+template <int KIND, typename T, int MAXW>
+__device__ __forceinline__ void load_coeffs(const SweepArgs<T>& a, const int* ls, const SlotMeta& m, int l, int gwarp,
+                                            int lane, RowPrefetch<T, MAXW>& p) {
+  p.row = m.row;
+  p.len = m.row >= 0 ? m.len : 0;
+  p.base = m.base;
+  const int r = m.row >= 0 ? m.row : 0;
+  p.b = a.b[r];
+  if (KIND == SW_ILU_UPPER) {
+    const int s = (m.row >= 0) ? ls[l] + gwarp : 0;
+    p.d = a.diag[s * 32 + lane];
+  }
+#pragma unroll
+  for (int k = 0; k < MAXW; ++k)
+    if (k < p.len) {
+      p.v[k] = a.val[p.base + 32 * k];
+      p.c[k] = a.col[p.base + 32 * k];
+    }
+}
+
+template <int KIND, typename T, int MAXW>
+__device__ __forceinline__ void finish_row(const SweepArgs<T>& a, const RowPrefetch<T, MAXW>& p) {
+  if (p.row < 0) return;
+  T xv[MAXW];
+#pragma unroll
+  for (int k = 0; k < MAXW; ++k)
+    if (k < p.len) xv[k] = ld_l2(a.x + p.c[k]);
+  T sum = 0;
+#pragma unroll
+  for (int k = 0; k < MAXW; ++k)
+    if (k < p.len) sum += p.v[k] * xv[k];
+  for (int k = MAXW; k < p.len; ++k) {
+    int q = p.base + 32 * k;
+    sum += a.val[q] * ld_l2(a.x + a.col[q]);
+  }
+  if (KIND == SW_ILU_LOWER) st_l2(a.x + p.row, p.b - sum);
+  else st_l2(a.x + p.row, (p.b - sum) / p.d);
+}
+
+constexpr int SWEEP_MAX_LEVELS = 8192;  // level offsets staged in shared memory
+
+template <int KIND, typename T, int MAXW>
+__global__ void __launch_bounds__(256) k_sweep_pipelined(SweepArgs<T> a) {
+  if (a.active && *a.active != 0) return;
+  __shared__ int ls[SWEEP_MAX_LEVELS + 1];
+  for (int q = threadIdx.x; q <= a.nlev; q += blockDim.x) ls[q] = a.level_slices[q];
+  __syncthreads();
+  cg::cluster_group cluster = cg::this_cluster();
+  const int wpc = blockDim.x >> 5;
+  const int gwarp = (int)cluster.block_rank() * wpc + (threadIdx.x >> 5);
+  const int nwarps = (int)cluster.num_blocks() * wpc;
+  const int lane = threadIdx.x & 31;
+  RowPrefetch<T, MAXW> cur, nxt;
+  SlotMeta m1 = load_meta(a, ls, 1, gwarp, lane);
+  {
+    SlotMeta m0 = load_meta(a, ls, 0, gwarp, lane);
+    load_coeffs<KIND, T, MAXW>(a, ls, m0, 0, gwarp, lane, cur);
+  }
+  for (int l = 0; l < a.nlev; ++l) {
+    const SlotMeta m2 = load_meta(a, ls, l + 2, gwarp, lane);
+    load_coeffs<KIND, T, MAXW>(a, ls, m1, l + 1, gwarp, lane, nxt);
+    finish_row<KIND, T, MAXW>(a, cur);
+    const int s1 = ls[l + 1];
+    for (int s = ls[l] + gwarp + nwarps; s < s1; s += nwarps) {
+      const int slot = s * 32 + lane;
+      const int row = a.row[slot];
+      if (row >= 0) sweep_row<KIND, T>(a, slot, row, s);
+    }
+    cluster.sync();
+    cur = nxt;
+    m1 = m2;
+  }
+}
+
 // Fallback: one launch per level.
 template <int KIND, typename T>
 __global__ void k_sweep_level(SweepArgs<T> a, int l) {
@@ -113,6 +221,11 @@ __global__ void k_sweep_level(SweepArgs<T> a, int l) {
 // ILU(0) factorisation, one thread per row, rows of a level in parallel.
 // Row k reads only rows of earlier levels (its lower neighbours), which are
 // final once the barrier of their level has passed.
+// The elimination of row k is a fixed program of the pattern: for every
+// lower entry i (ascending) the pairs (l, j) with data[l] -= LUki * data[j]
+// in the order of the merge scan of ILU.java:113-120.  The host lists those
+// pairs once per pattern (upd_ptr indexed by CSR position, upd_l, upd_j), so
+// the device only streams them.
 struct FactorArgs {
   int nlev;
   const int* level_slices;
@@ -120,26 +233,62 @@ struct FactorArgs {
   const int* rowptr;
   const int* col;
   const int* diag;
+  const int* upd_ptr;
+  const int* upd_l;
+  const int* upd_j;
   double* data;
   int* flag;  // first zero-pivot row + 1
 };
 
-__device__ __forceinline__ void factor_row(const FactorArgs& a, int k) {
-  const int r0 = a.rowptr[k], r1 = a.rowptr[k + 1], dk = a.diag[k];
+constexpr int FACTOR_ROW_MAX = 32;  // rows up to this length keep their values in a local array
+constexpr int FACTOR_BATCH = 16;
+
+__device__ __forceinline__ void factor_row_global(const FactorArgs& a, int k) {
+  const int r0 = a.rowptr[k], dk = a.diag[k];
   for (int i = r0; i < dk; ++i) {
     const int index = a.col[i];
     const double LUii = ld_l2(a.data + a.diag[index]);
     if (LUii == 0) atomicCAS(a.flag, 0, i + 1);
     const double LUki = ld_l2(a.data + i) / LUii;
     st_l2(a.data + i, LUki);
-    const int j1 = a.rowptr[index + 1];
-    int l = r0 + 1;
-    for (int j = a.diag[index] + 1; j < j1; ++j) {
-      const int cj = a.col[j];
-      while (l < r1 && a.col[l] < cj) l++;
-      if (l < r1 && a.col[l] == cj) st_l2(a.data + l, ld_l2(a.data + l) - LUki * ld_l2(a.data + j));
+    for (int u = a.upd_ptr[i]; u < a.upd_ptr[i + 1]; ++u) {
+      const int l = a.upd_l[u];
+      st_l2(a.data + l, ld_l2(a.data + l) - LUki * ld_l2(a.data + a.upd_j[u]));
     }
   }
+}
+
+__device__ __forceinline__ void factor_row(const FactorArgs& a, int k) {
+  const int r0 = a.rowptr[k], r1 = a.rowptr[k + 1], dk = a.diag[k];
+  if (r1 - r0 > FACTOR_ROW_MAX) {
+    factor_row_global(a, k);
+    return;
+  }
+  // the row's own values: only this thread reads or writes them
+  double rowv[FACTOR_ROW_MAX];
+  for (int q = 0; q < r1 - r0; ++q) rowv[q] = ld_l2(a.data + r0 + q);
+  for (int i = r0; i < dk; ++i) {
+    const double LUii = ld_l2(a.data + a.diag[a.col[i]]);
+    if (LUii == 0) atomicCAS(a.flag, 0, i + 1);
+    const double LUki = rowv[i - r0] / LUii;
+    rowv[i - r0] = LUki;
+    const int u0 = a.upd_ptr[i], u1 = a.upd_ptr[i + 1];
+    for (int ub = u0; ub < u1; ub += FACTOR_BATCH) {
+      // values of earlier rows: independent loads issued together
+      double dj[FACTOR_BATCH];
+      int lo[FACTOR_BATCH];
+#pragma unroll
+      for (int q = 0; q < FACTOR_BATCH; ++q)
+        if (ub + q < u1) {
+          dj[q] = ld_l2(a.data + a.upd_j[ub + q]);
+          lo[q] = a.upd_l[ub + q] - r0;
+        }
+#pragma unroll
+      for (int q = 0; q < FACTOR_BATCH; ++q)
+        if (ub + q < u1) rowv[lo[q]] = rowv[lo[q]] - LUki * dj[q];
+    }
+  }
+  for (int q = 0; q < r1 - r0; ++q) st_l2(a.data + r0 + q, rowv[q]);
 }
 
 __global__ void __launch_bounds__(512) k_factor_cluster(FactorArgs a) {
@@ -340,9 +489,8 @@ static void plan_values(Context& ctx, SweepPlan& P, const double* csr_vals, bool
 static int g_cluster_ok = -1;  // probed once per process
 
 template <typename Kernel, typename Args>
-static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Args& args) {
+static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Args& args, int threads = 512) {
   int& cluster_ok = g_cluster_ok;
-  const int threads = 512;
   if (cluster_ok < 0) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ctx.cluster_size);
@@ -381,7 +529,10 @@ static void run_sweep(Context& ctx, const char* name, const SweepPlan& P, const 
                       T* x, T* xx, T omega, const int* active) {
   SweepArgs<T> a{P.nlev, P.level_slices.get(), P.slice_base.get(), P.row.get(), P.len.get(), P.col.get(), val, diag,
                  b, x, xx, omega, active};
-  if (launch_cluster(ctx, name, k_sweep_cluster<KIND, T>, a)) return;
+  if ((KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER) && P.nlev <= SWEEP_MAX_LEVELS) {
+    if (launch_cluster(ctx, name, k_sweep_pipelined<KIND, T, 16>, a, 256)) return;
+  } else if (launch_cluster(ctx, name, k_sweep_cluster<KIND, T>, a))
+    return;
   for (int l = 0; l < P.nlev; ++l) {
     int slices = P.h_level_slices[l + 1] - P.h_level_slices[l];
     RSG_LAUNCH(ctx, name, (k_sweep_level<KIND, T>), blocks_for(slices, 8), 256, 0, a, l);
@@ -395,7 +546,7 @@ struct ILUPrecond : Precond {
   SweepPlan Lp, Up;
   DeviceBuffer<double> LU, y;
   DeviceBuffer<float> yf;
-  DeviceBuffer<int> flag;
+  DeviceBuffer<int> flag, upd_ptr, upd_l, upd_j;
   const int* pattern_id = nullptr;
   explicit ILUPrecond(Context* c) : ctx(c) {}
 
@@ -421,6 +572,43 @@ struct ILUPrecond : Precond {
           }
       }
     }
+    // elimination program (see FactorArgs)
+    {
+      std::vector<int> uptr(M.nnz + 1, 0), ul, uj;
+      ul.reserve((size_t)M.nnz * 4);
+      uj.reserve((size_t)M.nnz * 4);
+      for (int k = 0; k < M.n; ++k) {
+        const int r1 = rp[k + 1];
+        for (int i = rp[k]; i < M.h_diag[k]; ++i) {
+          const int index = cl[i];
+          int l = rp[k] + 1;
+          int cnt = 0;
+          for (int j = M.h_diag[index] + 1; j < rp[index + 1]; ++j) {
+            while (l < r1 && cl[l] < cl[j]) l++;
+            if (l < r1 && cl[l] == cl[j]) {
+              ul.push_back(l);
+              uj.push_back(j);
+              cnt++;
+            }
+          }
+          uptr[i + 1] = cnt;
+        }
+      }
+      for (int q = 0; q < M.nnz; ++q) uptr[q + 1] += uptr[q];
+      if (ul.size() > (size_t)INT32_MAX) throw Error(RSG_UNSUPPORTED, "ILU elimination program too large");
+      if (ul.empty()) {
+        ul.push_back(0);
+        uj.push_back(0);
+      }
+      upd_ptr.resize(M.nnz + 1);
+      upd_l.resize(ul.size());
+      upd_j.resize(uj.size());
+      RSG_CUDA(cudaMemcpyAsync(upd_ptr.get(), uptr.data(), sizeof(int) * uptr.size(), cudaMemcpyHostToDevice,
+                               ctx->stream));
+      RSG_CUDA(cudaMemcpyAsync(upd_l.get(), ul.data(), sizeof(int) * ul.size(), cudaMemcpyHostToDevice, ctx->stream));
+      RSG_CUDA(cudaMemcpyAsync(upd_j.get(), uj.data(), sizeof(int) * uj.size(), cudaMemcpyHostToDevice, ctx->stream));
+      ctx->sync();
+    }
     build_plan(M, Lp, false, 0, false);
     build_plan(M, Up, true, 1, true);
     LU.resize(std::max(M.nnz, 1));
@@ -438,8 +626,8 @@ struct ILUPrecond : Precond {
     // LU.set(A) then factor() (ILU.java:80-125)
     RSG_LAUNCH(*ctx, "ilu_copy", k_copy, blocks_for(M.nnz, 256), 256, 0, (int64_t)M.nnz, M.val.get(), LU.get());
     RSG_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), ctx->stream));
-    FactorArgs fa{Lp.nlev, Lp.level_slices.get(), Lp.row.get(), M.rowptr.get(), M.col.get(), M.diag.get(), LU.get(),
-                  flag.get()};
+    FactorArgs fa{Lp.nlev,      Lp.level_slices.get(), Lp.row.get(), M.rowptr.get(), M.col.get(), M.diag.get(),
+                  upd_ptr.get(), upd_l.get(),           upd_j.get(),  LU.get(),       flag.get()};
     if (!launch_cluster(*ctx, "ilu_factor", k_factor_cluster, fa)) {
       for (int l = 0; l < Lp.nlev; ++l) {
         int slots = (Lp.h_level_slices[l + 1] - Lp.h_level_slices[l]) * 32;
