@@ -152,6 +152,29 @@ rsg_status rsg_precond_trans_apply(rsg_solver* s, const double* b, double* x);
 /* Residual history of the last solve (monitor values in call order). */
 rsg_status rsg_solver_history(rsg_solver* s, int32_t max_len, double* out, int32_t* len);
 
+/* No-allocation CG: conjugate gradients with the diagonal preconditioner on
+ * a CSR matrix and vectors that are already in device memory, for callers
+ * that cannot allocate device memory while they run (a host runtime that
+ * has reserved the GPU memory it may use, or a loop that forbids
+ * allocation).  No counterpart in the reference: it computes what
+ * rsg_solver_solve computes for RSG_CG with RSG_PC_DIAGONAL, with the same
+ * reduction order.
+ *
+ * All workspace (five vectors of n doubles plus reduction partials, about
+ * 40 MiB) is one static device array that every GPU loading the library
+ * holds until the process exits.  n may not exceed RSG_NOALLOC_MAX_ROWS
+ * (RSG_BAD_ARG otherwise).  The entry point calls no cudaMalloc or cudaFree.
+ * Its first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU (different
+ * streams or threads) race and must be serialised by the caller.
+ * stream: a cudaStream_t, or NULL for the default stream.  The call returns
+ * when the solve has finished; d_x holds the result (also on failure). */
+#define RSG_NOALLOC_MAX_ROWS 1048576
+rsg_status rsg_cg_diagonal_noalloc(int32_t device, void* stream, int32_t n, int32_t nnz, const int32_t* d_row_ptr,
+                                   const int32_t* d_col, const double* d_val, const double* d_b, double* d_x,
+                                   double rtol, double atol, double dtol, int32_t max_iter, rsg_solve_info* info);
+
 /* ------------------------------------------------- mesh + MPFA-O -------- */
 /* Structured hexahedral (dim 3) or quadrilateral (dim 2, nk = 0) mesh in
  * RS's StructuredMeshGenerator numbering.  coords: 3 doubles per corner point

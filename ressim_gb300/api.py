@@ -90,6 +90,8 @@ def _declare(L):
         "rsg_precond_apply": (i32, [vp, P(d), P(d)]),
         "rsg_precond_trans_apply": (i32, [vp, P(d), P(d)]),
         "rsg_solver_history": (i32, [vp, i32, P(d), P(i32)]),
+        "rsg_cg_diagonal_noalloc": (i32, [i32, vp, i32, i32, vp, vp, vp, vp, vp, d, d, d, i32,
+                                            P(abi.rsg_solve_info)]),
         "rsg_mesh_create_structured": (i32, [vp, i32, i32, i32, i32, P(d), d, d, d, d, d, d, P(d), PP()]),
         "rsg_mesh_destroy": (i32, [vp]),
         "rsg_mesh_compute_mpfa": (i32, [vp, d]),
@@ -244,6 +246,12 @@ class CompRowMatrix:
         y = np.zeros(self.n)
         self.ctx.check(lib().rsg_csr_trans_mult(self.h, abi.dptr(x), abi.dptr(y)), "transMult")
         return y
+
+    def device_arrays(self):
+        """Device pointers (row_ptr, col, values) of the matrix."""
+        rp, col, val = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        self.ctx.check(lib().rsg_csr_device_arrays(self.h, C.byref(rp), C.byref(col), C.byref(val)), "device_arrays")
+        return rp.value, col.value, val.value
 
     def zero_rows(self, diagonal, rows):
         r = _i32(rows)
