@@ -136,6 +136,11 @@ rsg_status rsg_solver_destroy(rsg_solver* s);
 rsg_status rsg_solver_set_monitor(rsg_solver* s, double rtol, double atol, double dtol, int32_t max_iter);
 /* GMRES.setRestart (default 30) */
 rsg_status rsg_solver_set_restart(rsg_solver* s, int32_t restart);
+/* Mixed precision (RSG_FGMRES_MIXED): FP64 flexible GMRES(restart) whose
+ * preconditioner is `inner_iterations` FP32 BiCGstab steps (stopping early at
+ * inner_rtol) with the FP32 copy of the preconditioner.  Default 10, 1e-3.
+ * No counterpart in the reference (a new capability beside MTJ's solvers). */
+rsg_status rsg_solver_set_inner(rsg_solver* s, int32_t inner_iterations, double inner_rtol);
 /* SSOR omegas (SSOR(F, reverse, omegaF, omegaR)) */
 rsg_status rsg_solver_set_ssor(rsg_solver* s, double omega_f, double omega_r, int32_t reverse);
 /* Preconditioner.setMatrix(A): ILU(0) factorisation / diagonal inversion. */
@@ -270,6 +275,10 @@ typedef struct {
   int32_t newton_stop_rule;  /* 0: RS rule dp[0] < tol (Discretisation.java:324); 1: max |dp/p| < tol */
   double omega, ax, ay;      /* BodyForces (field/Field.java:184-202) */
   int32_t gmres_restart;     /* 30 */
+  /* RSG_FGMRES_MIXED only (no RunSpec counterpart): FP32 inner BiCGstab steps
+   * per outer step and the inner relative tolerance; 0 keeps 10 and 1e-3 */
+  int32_t inner_iterations;
+  double inner_tolerance;
 } rsg_runspec;
 
 typedef struct {

@@ -122,6 +122,8 @@ class rsg_runspec(C.Structure):
         ("ax", C.c_double),
         ("ay", C.c_double),
         ("gmres_restart", C.c_int32),
+        ("inner_iterations", C.c_int32),
+        ("inner_tolerance", C.c_double),
     ]
 
 

@@ -84,6 +84,7 @@ def _declare(L):
         "rsg_solver_set_monitor": (i32, [vp, d, d, d, i32]),
         "rsg_solver_set_restart": (i32, [vp, i32]),
         "rsg_solver_set_ssor": (i32, [vp, d, d, i32]),
+        "rsg_solver_set_inner": (i32, [vp, i32, d]),
         "rsg_solver_setup": (i32, [vp, vp]),
         "rsg_solver_solve": (i32, [vp, vp, P(d), P(d), P(abi.rsg_solve_info)]),
         "rsg_solver_solve_device": (i32, [vp, vp, vp, vp, P(abi.rsg_solve_info)]),
@@ -289,6 +290,10 @@ class IterativeSolver:
     def set_monitor(self, rtol, atol, dtol, max_iter):
         self.ctx.check(lib().rsg_solver_set_monitor(self.h, rtol, atol, dtol, max_iter), "set_monitor")
 
+    def set_inner(self, iterations, rtol):
+        """Inner FP32 BiCGstab steps per outer step of the mixed-precision solver."""
+        self.ctx.check(lib().rsg_solver_set_inner(self.h, iterations, rtol), "set_inner")
+
     def set_ssor(self, omega_f, omega_r, reverse=True):
         self.ctx.check(lib().rsg_solver_set_ssor(self.h, omega_f, omega_r, int(reverse)), "set_ssor")
 
@@ -336,6 +341,12 @@ class BiCGstab(IterativeSolver):
 
 class GMRES(IterativeSolver):
     method = abi.GMRES
+
+
+class MixedFGMRES(IterativeSolver):
+    """FP64 flexible GMRES with an FP32 BiCGstab + FP32 preconditioner inside."""
+
+    method = abi.FGMRES_MIXED
 
 
 class Mesh:

@@ -35,6 +35,7 @@ enum Epi {
   EPI_CG_RHO,      // rho = r.z, beta
   EPI_CG_ALPHA,    // alpha = rho / (p.q)
   EPI_CG_NEXT,     // rho_1 = rho; iter++; monitor(|r|)
+  EPI_BICG_S_IN,   // inner (mixed precision) s check against the initial residual of the inner solve
   EPI_GM_NORMR,    // normr = |r| (no monitor)
   EPI_GM_OUTER,    // iter++ (unless first); monitor(normr); inner setup + monitor(|s0|)
   EPI_GM_H,        // H(k,i) = w.v_k
@@ -109,6 +110,11 @@ __device__ void run_epilogue(int epi, KState* s, const double* t, double* hist, 
       else if (m < 0) s->status = m;
       break;
     }
+    case EPI_BICG_S_IN:
+      // unlike BiCGstab.java's check, the initial residual is not replaced
+      // by |s| on the first iteration, so an exact preconditioner converges
+      if (sqrt(t[0]) < jmax(s->rtol * s->initR, s->atol)) s->status = KS_CONVERGED_S;
+      break;
     case EPI_BICG_OMEGA: s->omega = t[0] / t[1]; break;
     case EPI_BICG_NEXT:
       s->rho_2 = s->rho_1;
@@ -473,6 +479,121 @@ __global__ void k_copy_vec(int n, const double* __restrict__ a, double* __restri
   if (i < n) b[i] = a[i];
 }
 
+// ---- FP32 inner BiCGstab for the mixed-precision solver.  Vectors and the
+// preconditioner are FP32; dot products accumulate in FP64 and the scalar
+// recurrences (KState) stay FP64.
+__global__ void k_inner_reset(KState* s, double rtol, double atol, int maxIter) {
+  KState z = {};
+  z.rho_1 = z.rho_2 = z.alpha = z.beta = z.omega = 1;
+  z.rtol = rtol;
+  z.atol = atol;
+  z.dtol = 1e300;
+  z.maxIter = maxIter;
+  z.first = 1;
+  z.hist_cap = 0;
+  *s = z;
+}
+
+// r = rt = (float) v (x0 = 0), x = 0; reduces r.r twice (rtilde.r = r.r)
+__global__ void __launch_bounds__(RT) k_f32_init(int n, const double* __restrict__ v, float* __restrict__ r,
+                                                 float* __restrict__ rt, float* __restrict__ x, RedArgs ra) {
+  double acc[2] = {0, 0};
+  for (int i = blockIdx.x * RT + threadIdx.x; i < n; i += gridDim.x * RT) {
+    float ri = (float)v[i];
+    r[i] = ri;
+    rt[i] = ri;
+    x[i] = 0.f;
+    acc[0] += (double)ri * ri;
+    acc[1] += (double)ri * ri;
+  }
+  reduce_finish<2>(acc, ra.part, ra.ticket, EPI_BICG_TOP, ra.s, ra.hist, ra.g, 0);
+}
+
+__global__ void k_f32_bicg_p(int n, const float* __restrict__ r, const float* __restrict__ v, float* __restrict__ p,
+                             const KState* s) {
+  if (stopped(s)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (s->first) {
+    p[i] = r[i];
+    return;
+  }
+  const float mo = (float)(-s->omega), beta = (float)s->beta;
+  float temp = mo * v[i] + p[i];
+  p[i] = r[i] + beta * temp;
+}
+
+template <int K>
+__global__ void __launch_bounds__(RT) k_f32_spmv_dot(int n, const int* __restrict__ sb, const int* __restrict__ rl,
+                                                     const int* __restrict__ col, const float* __restrict__ val,
+                                                     const float* __restrict__ x, float* __restrict__ y,
+                                                     const float* __restrict__ w, RedArgs ra, int epi) {
+  if (stopped(ra.s)) return;
+  double v[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) v[q] = 0;
+  for (int row = blockIdx.x * RT + threadIdx.x; row < n; row += gridDim.x * RT) {
+    int base = sb[row >> 5] + (row & 31);
+    int len = rl[row];
+    float d = 0;
+#pragma unroll 8
+    for (int k = 0; k < len; ++k) {
+      int q = base + 32 * k;
+      d = fmaf(val[q], __ldg(x + col[q]), d);
+    }
+    y[row] = d;
+    if (K == 1) v[0] += (double)w[row] * d;
+    if (K == 2) {
+      v[0] += (double)d * w[row];
+      v[1] += (double)d * d;
+    }
+  }
+  reduce_finish<K>(v, ra.part, ra.ticket, epi, ra.s, ra.hist, ra.g, 0);
+}
+
+__global__ void __launch_bounds__(RT) k_f32_bicg_s(int n, const float* __restrict__ r, const float* __restrict__ v,
+                                                   float* __restrict__ sv, RedArgs ra) {
+  if (stopped(ra.s)) return;
+  const float ma = (float)(-ra.s->alpha);
+  double acc[1] = {0};
+  for (int i = blockIdx.x * RT + threadIdx.x; i < n; i += gridDim.x * RT) {
+    float si = r[i] + ma * v[i];
+    sv[i] = si;
+    acc[0] += (double)si * si;
+  }
+  reduce_finish<1>(acc, ra.part, ra.ticket, EPI_BICG_S_IN, ra.s, ra.hist, ra.g, 0);
+}
+
+__global__ void k_f32_bicg_xfinal(int n, const float* __restrict__ phat, float* __restrict__ x, KState* s) {
+  if (*(volatile int*)&s->status != KS_CONVERGED_S) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] += (float)s->alpha * phat[i];
+}
+
+__global__ void __launch_bounds__(RT) k_f32_bicg_update(int n, const float* __restrict__ phat,
+                                                        const float* __restrict__ shat, const float* __restrict__ sv,
+                                                        const float* __restrict__ t, const float* __restrict__ rtilde,
+                                                        float* __restrict__ x, float* __restrict__ r, RedArgs ra) {
+  if (stopped(ra.s)) return;
+  const float alpha = (float)ra.s->alpha, omega = (float)ra.s->omega;
+  double acc[2] = {0, 0};
+  for (int i = blockIdx.x * RT + threadIdx.x; i < n; i += gridDim.x * RT) {
+    x[i] = x[i] + alpha * phat[i] + omega * shat[i];
+    float ri = sv[i] - omega * t[i];
+    r[i] = ri;
+    acc[0] += (double)ri * ri;
+    acc[1] += (double)rtilde[i] * ri;
+  }
+  reduce_finish<2>(acc, ra.part, ra.ticket, EPI_BICG_NEXT, ra.s, ra.hist, ra.g, 0);
+}
+
+__global__ void k_f32_to_f64(int n, const float* __restrict__ a, double* __restrict__ b, const KState* sin,
+                             KState* sout) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+  if (i == 0) sout->inner += sin->iter;
+}
+
 }  // namespace
 
 // ----------------------------------------------------------------------
@@ -487,6 +608,13 @@ struct Solver {
   DeviceBuffer<double> part, hist, gmH, gmS, gmC, gmSn;
   DeviceBuffer<unsigned> ticket;
   DeviceBuffer<KState> state;
+  // mixed precision: FP32 inner BiCGstab workspace, inner state, Z basis
+  int inner_iters = 10;
+  double inner_rtol = 1e-3;
+  DeviceBuffer<float> f1, f2, f3, f4, f5, f6, f7, f8, fx;
+  DeviceBuffer<double> Zb, part_in, hist_in;
+  DeviceBuffer<unsigned> ticket_in;
+  DeviceBuffer<KState> state_in;
   KState* hstate = nullptr;  // pinned mirror
   int nblk = 0;
   Csr* setup_for = nullptr;
@@ -546,6 +674,7 @@ struct Solver {
       case RSG_CG: run_cg(A, b, x); break;
       case RSG_BICGSTAB: run_bicgstab(A, b, x); break;
       case RSG_GMRES: run_gmres(A, b, x); break;
+      case RSG_FGMRES_MIXED: run_fgmres_mixed(A, b, x); break;
       default: throw Error(RSG_UNSUPPORTED, "unknown iterative method");
     }
     read_state();
@@ -553,7 +682,7 @@ struct Solver {
       info->iterations = hstate->iter;
       info->residual = hstate->residual;
       info->initial_residual = hstate->initR;
-      info->inner_iterations = 0;
+      info->inner_iterations = hstate->inner;
       info->refinements = 0;
       info->reason = hstate->status < 0 ? -hstate->status : RSG_OK;
     }
@@ -615,6 +744,87 @@ struct Solver {
     }
   }
 
+  // Flexible GMRES(m) in FP64 (right preconditioned, modified Gram-Schmidt,
+  // Givens rotations as in GMRES.java) whose preconditioner is a short FP32
+  // BiCGstab with the FP32 ILU(0) factors and an FP32 SpMV.  The outer
+  // monitor sees the true FP64 residual ||b - A x|| at each restart and the
+  // rotated residual estimate inside a cycle, with DefaultIterationMonitor
+  // semantics.
+  void run_fgmres_mixed(Csr& A, const double* b, double* x) {
+    const int m = restart;
+    const size_t ld = (size_t)n;
+    if (V.size() < (size_t)(m + 1) * ld) V.resize((size_t)(m + 1) * ld);
+    if (Zb.size() < (size_t)m * ld) Zb.resize((size_t)m * ld);
+    for (auto* f : {&f1, &f2, &f3, &f4, &f5, &f6, &f7, &f8, &fx})
+      if (f->size() != (size_t)n) f->resize(n);
+    gmH.resize((size_t)(m + 1) * m);
+    gmS.resize(m + 1);
+    gmC.resize(m + 1);
+    gmSn.resize(m + 1);
+    part_in.resize((size_t)4 * nblk);
+    hist_in.resize(1);
+    ticket_in.resize(1);
+    state_in.resize(1);
+    RSG_CUDA(cudaMemsetAsync(ticket_in.get(), 0, sizeof(unsigned), ctx->stream));
+    RSG_CUDA(cudaMemsetAsync(gmH.get(), 0, sizeof(double) * (m + 1) * m, ctx->stream));
+    A.refresh_sell_f32();
+    double *w = w1.get(), *r = w3.get();
+    auto vcol = [&](int j) { return V.get() + (size_t)j * ld; };
+    auto zcol = [&](int j) { return Zb.get() + (size_t)j * ld; };
+    const int eb = blocks_for(n, 256);
+    GmresDev gd{gmH.get(), gmS.get(), gmC.get(), gmSn.get()};
+    RedArgs ri{part_in.get(), ticket_in.get(), state_in.get(), hist_in.get(), gd};
+    KState* sin = state_in.get();
+    const int* act_in = &sin->status;
+    float *ir = f1.get(), *irt = f2.get(), *ip = f3.get(), *iv = f4.get(), *iph = f5.get(), *is = f6.get(),
+          *ish = f7.get(), *it = f8.get(), *ix = fx.get();
+    // r = b - A x; monitor(|r|)
+    RSG_LAUNCH(*ctx, "fgm_resid", k_resid, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(), A.sell_col.get(),
+               A.sell_val.get(), x, b, r, (double*)nullptr, red(), (int)EPI_NONE);
+    RSG_LAUNCH(*ctx, "fgm_norm", k_dot, nblk, RT, 0, n, r, r, red(), (int)EPI_GM_OUTER, 0);
+    for (;;) {
+      read_state();
+      if (hstate->status != 0) break;
+      RSG_LAUNCH(*ctx, "gm_vset", k_gm_vset, eb, 256, 0, n, r, vcol(0), state.get());
+      while (!hstate->gm_exit && hstate->status == 0) {
+        const int i = hstate->gm_i;
+        // z_i = M(v_i): FP32 BiCGstab + ILU(0) from zero
+        RSG_LAUNCH(*ctx, "inner_reset", k_inner_reset, 1, 1, 0, sin, inner_rtol, 0.0, inner_iters);
+        RSG_LAUNCH(*ctx, "inner_init", k_f32_init, nblk, RT, 0, n, vcol(i), ir, irt, ix, ri);
+        for (int q = 0; q < inner_iters; ++q) {
+          RSG_LAUNCH(*ctx, "inner_p", k_f32_bicg_p, eb, 256, 0, n, ir, iv, ip, sin);
+          pc->apply_f32(ip, iph, act_in);
+          RSG_LAUNCH(*ctx, "inner_spmv_dot", k_f32_spmv_dot<1>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
+                     A.sell_col.get(), A.sell_valf.get(), iph, iv, irt, ri, (int)EPI_BICG_ALPHA);
+          RSG_LAUNCH(*ctx, "inner_s", k_f32_bicg_s, nblk, RT, 0, n, ir, iv, is, ri);
+          RSG_LAUNCH(*ctx, "inner_xfinal", k_f32_bicg_xfinal, eb, 256, 0, n, iph, ix, sin);
+          RSG_LAUNCH(*ctx, "status_fix", k_status_fix, 1, 1, 0, sin);
+          pc->apply_f32(is, ish, act_in);
+          RSG_LAUNCH(*ctx, "inner_spmv_dot", k_f32_spmv_dot<2>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
+                     A.sell_col.get(), A.sell_valf.get(), ish, it, is, ri, (int)EPI_BICG_OMEGA);
+          RSG_LAUNCH(*ctx, "inner_update", k_f32_bicg_update, nblk, RT, 0, n, iph, ish, is, it, irt, ix, ir, ri);
+        }
+        RSG_LAUNCH(*ctx, "to_f64", k_f32_to_f64, eb, 256, 0, n, ix, zcol(i), (const KState*)sin, state.get());
+        // w = A z_i, then the Arnoldi step of GMRES.java:146-162 on w
+        launch_spmv(*ctx, A, zcol(i), w, nullptr);
+        for (int k2 = 0; k2 <= i; ++k2)
+          RSG_LAUNCH(*ctx, "gm_mgs", k_gm_mgs, nblk, RT, 0, n, w, k2 > 0 ? vcol(k2 - 1) : (const double*)nullptr,
+                     vcol(k2), red(), k2, (int)EPI_GM_H);
+        RSG_LAUNCH(*ctx, "gm_mgs", k_gm_mgs, nblk, RT, 0, n, w, vcol(i), (const double*)nullptr, red(), i + 1,
+                   (int)EPI_GM_NORMW);
+        RSG_LAUNCH(*ctx, "gm_vset", k_gm_vset, eb, 256, 0, n, w, vcol(i + 1), state.get());
+        read_state();
+      }
+      if (hstate->status != 0) break;
+      RSG_LAUNCH(*ctx, "gm_trisolve", k_gm_trisolve, 1, 1, 0, state.get(), gd);
+      RSG_LAUNCH(*ctx, "gm_xupdate", k_gm_xupdate, eb, 256, 0, n, x, Zb.get(), (int64_t)ld, state.get(), gd);
+      RSG_LAUNCH(*ctx, "fgm_resid", k_resid, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(), A.sell_col.get(),
+                 A.sell_val.get(), x, b, r, (double*)nullptr, red(), (int)EPI_NONE);
+      RSG_LAUNCH(*ctx, "iter_inc", k_iter_inc, 1, 1, 0, state.get());
+      RSG_LAUNCH(*ctx, "fgm_norm", k_dot, nblk, RT, 0, n, r, r, red(), (int)EPI_GM_OUTER, 0);
+    }
+  }
+
   void run_gmres(Csr& A, const double* b, double* x) {
     const int m = restart;
     const size_t ld = (size_t)n;
@@ -667,8 +877,10 @@ void SolverDeleter::operator()(Solver* s) const { delete s; }
 
 SolverPtr make_solver(Context* ctx, int method, int precond, double rtol, double atol, double dtol, int maxit,
                       int restart) {
-  if (method != RSG_CG && method != RSG_BICGSTAB && method != RSG_GMRES)
+  if (method != RSG_CG && method != RSG_BICGSTAB && method != RSG_GMRES && method != RSG_FGMRES_MIXED)
     throw Error(RSG_UNSUPPORTED, "linear solver not available");
+  if (method == RSG_FGMRES_MIXED && precond != RSG_PC_ILU && precond != RSG_PC_DIAGONAL && precond != RSG_PC_NONE)
+    throw Error(RSG_UNSUPPORTED, "the mixed-precision solver takes ILU, diagonal or no preconditioning");
   SolverPtr s(new Solver(ctx, method, precond));
   s->rtol = rtol;
   s->atol = atol;
@@ -684,6 +896,11 @@ void solver_setup(Solver& s, Csr& A) {
 }
 
 void solver_solve(Solver& s, Csr& A, const double* b, double* x, rsg_solve_info* info) { s.solve(A, b, x, info); }
+
+void solver_set_inner(Solver& s, int iterations, double rtol) {
+  s.inner_iters = iterations;
+  s.inner_rtol = rtol;
+}
 
 }  // namespace rsg
 
@@ -701,7 +918,8 @@ rsg_status rsg_solver_create(rsg_ctx* ctx, int32_t method, int32_t precond, rsg_
   if (method < RSG_CG || method > RSG_FGMRES_MIXED) return RSG_BAD_ARG;
   rsg_solver* h = new rsg_solver();
   rsg_status st = guarded(&ctx->c, [&] {
-    if (method == RSG_FGMRES_MIXED) throw rsg::Error(RSG_UNSUPPORTED, "use rsg_solver_create_mixed");
+    if (method == RSG_FGMRES_MIXED && precond != RSG_PC_ILU && precond != RSG_PC_DIAGONAL && precond != RSG_PC_NONE)
+      throw rsg::Error(RSG_UNSUPPORTED, "the mixed-precision solver takes ILU, diagonal or no preconditioning");
     h->s.reset(new rsg::Solver(&ctx->c, method, precond));
   });
   if (st != RSG_OK) {
@@ -731,6 +949,13 @@ rsg_status rsg_solver_set_monitor(rsg_solver* s, double rtol, double atol, doubl
 rsg_status rsg_solver_set_restart(rsg_solver* s, int32_t restart) {
   if (!s || restart <= 0) return RSG_BAD_ARG;
   s->s->restart = restart;
+  return RSG_OK;
+}
+
+rsg_status rsg_solver_set_inner(rsg_solver* s, int32_t inner_iterations, double inner_rtol) {
+  if (!s || inner_iterations <= 0) return RSG_BAD_ARG;
+  s->s->inner_iters = inner_iterations;
+  s->s->inner_rtol = inner_rtol;
   return RSG_OK;
 }
 

@@ -58,6 +58,7 @@ struct KState {
   int gm_i;       // GMRES inner index
   int gm_exit;    // GMRES inner loop finished
   int restart;
+  int inner;      // mixed precision: inner iterations summed over outer steps
 };
 
 enum { KS_RUNNING = 0, KS_CONVERGED = 1, KS_CONVERGED_S = 2 };
@@ -86,6 +87,7 @@ SolverPtr make_solver(Context* ctx, int method, int precond, double rtol, double
                       int restart);
 void solver_setup(Solver& s, Csr& A);
 void solver_solve(Solver& s, Csr& A, const double* b, double* x, rsg_solve_info* info);
+void solver_set_inner(Solver& s, int iterations, double rtol);
 
 // Launches of BLAS-1 style kernels shared by the drivers.
 void launch_spmv(Context& ctx, Csr& A, const double* x, double* y, const int* active);

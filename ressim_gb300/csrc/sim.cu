@@ -1255,6 +1255,7 @@ rsg_status rsg_sim_create(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_blackoil* flui
     S.solver = make_solver(&c, spec->linear_solver, spec->preconditioner, spec->relative_tolerance,
                                    spec->absolute_tolerance, spec->divergence_tolerance, spec->max_linear_iterations,
                                    spec->gmres_restart > 0 ? spec->gmres_restart : 30);
+    if (spec->inner_iterations > 0) solver_set_inner(*S.solver, spec->inner_iterations, spec->inner_tolerance);
     c.sync();
   });
   if (st != RSG_OK) {

@@ -156,7 +156,7 @@ def corey(swc=0.2, sor=0.2, n=2.0):
 
 
 def runspec(method=abi.BICGSTAB, precond=abi.PC_ILU, rtol=1e-8, atol=1e-50, max_linear=5000,
-            max_newton=10, ptol=1e-6, stop_rule=0):
+            max_newton=10, ptol=1e-6, stop_rule=0, inner_iterations=0, inner_tolerance=0.0):
     s = abi.rsg_runspec()
     s.max_nonlinear_pressure_iterations = max_newton
     s.pressure_tolerance = ptol
@@ -169,6 +169,8 @@ def runspec(method=abi.BICGSTAB, precond=abi.PC_ILU, rtol=1e-8, atol=1e-50, max_
     s.truncate_negative_moles = 0
     s.newton_stop_rule = stop_rule
     s.gmres_restart = 30
+    s.inner_iterations = inner_iterations
+    s.inner_tolerance = inner_tolerance
     return s
 
 

@@ -230,7 +230,7 @@ def test_potential_case_matches_oracle(ctx):
     assert np.linalg.norm(r) <= 1.1e-10 * np.linalg.norm(b - A.mult(b))
 
 
-def _two_phase(ctx, ni, nj, nk, seed=1, spec_kw=None):
+def _two_phase(ctx, ni, nj, nk, seed=1, spec_kw=None, oracle_spec_kw=None):
     case = W.two_phase_case(ni=ni, nj=nj, nk=nk, seed=seed)
     keep = abi.Keep()
     fluid = W.two_phase_fluid(keep)
@@ -240,7 +240,8 @@ def _two_phase(ctx, ni, nj, nk, seed=1, spec_kw=None):
     spec = W.runspec(**(spec_kw or {}))
     gm, om = _mpfa_pair(ctx, 3, ni, nj, nk, case["perm"], case["nodes"])
     gs = api.Discretisation(ctx, gm, fluid, co, case["porosity"], case["compaction"], srcs, init, spec)
-    os_ = O.Simulator(om, fluid, co, case["porosity"], case["compaction"], srcs, init, spec)
+    ospec = spec if oracle_spec_kw is None else W.runspec(**oracle_spec_kw)
+    os_ = O.Simulator(om, fluid, co, case["porosity"], case["compaction"], srcs, init, ospec)
     return case, gm, om, gs, os_, keep
 
 
