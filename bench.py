@@ -285,7 +285,8 @@ def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, ne
         },
         "e2e": e2e,
         "gpu_launches": launches,
-        "sweep_mode": {-1: "undecided", 0: "one launch per level", 1: "one cluster walks all levels"}.get(
+        "sweep_mode": {-1: "undecided", 0: "one launch per level", 1: "one cluster walks all levels",
+                       2: "one cluster, values pushed through distributed shared memory"}.get(
             api.lib().rsg_sweep_mode()),
         "roofline": roof,
         "spmv": spmv,

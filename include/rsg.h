@@ -80,7 +80,9 @@ rsg_status rsg_context_destroy(rsg_ctx* ctx);
 const char* rsg_context_last_error(rsg_ctx* ctx);
 /* How the level-scheduled triangular sweeps run in this process:
  * -1 not decided yet, 0 one launch per level, 1 one thread-block cluster
- * walking all levels with hardware cluster barriers. */
+ * walking all levels with hardware cluster barriers, 2 ILU sweeps on one
+ * cluster exchanging values through distributed shared memory (st.async +
+ * mbarrier transaction counts, no cluster barrier per level). */
 int32_t rsg_sweep_mode(void);
 /* Number of kernels this context has launched so far. */
 int64_t rsg_context_kernel_launches(rsg_ctx* ctx);

@@ -86,10 +86,14 @@ struct Context {
   // pinned host staging for small scalar reads
   void* pinned = nullptr;
   cudaEvent_t timers[64] = {};
+  // set by kernels whose bounded waits ran out (1 + site); read after solves
+  DeviceBuffer<int> dev_err;
 
   cudaEvent_t get_event();
   void flush_profile();  // requires a synchronized stream
   void sync();
+  // throws RSG_TIMEOUT (and clears the flag) when a kernel's bounded wait ran out
+  void check_device_error();
 };
 
 // Launch helper: counts launches and (optionally) brackets them with events.

@@ -35,6 +35,18 @@ void Context::sync() {
   if (profiling) flush_profile();
 }
 
+void Context::check_device_error() {
+  int* h = static_cast<int*>(pinned) + 512;  // upper half of the staging page
+  RSG_CUDA(cudaMemcpyAsync(h, dev_err.get(), sizeof(int), cudaMemcpyDeviceToHost, stream));
+  sync();
+  if (*h != 0) {
+    const int at = *h;
+    RSG_CUDA(cudaMemsetAsync(dev_err.get(), 0, sizeof(int), stream));
+    sync();
+    throw Error(RSG_TIMEOUT, "a level walk's wait ran out at level " + std::to_string(at - 1));
+  }
+}
+
 }  // namespace rsg
 
 using rsg::guarded;
@@ -81,6 +93,8 @@ rsg_status rsg_context_create(int32_t device, rsg_ctx** out) {
     h->c.num_sms = prop.multiProcessorCount;
     RSG_CUDA(cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking));
     RSG_CUDA(cudaMallocHost(&h->c.pinned, 4096));
+    h->c.dev_err.resize(1);
+    RSG_CUDA(cudaMemsetAsync(h->c.dev_err.get(), 0, sizeof(int), h->c.stream));
   });
   if (st != RSG_OK) {
     delete h;

@@ -634,7 +634,12 @@ struct Solver {
   void ensure(int n_) {
     if (n_ == n && w1.size()) return;
     n = n_;
-    for (auto* b : {&w1, &w2, &w3, &w4, &w5, &w6, &w7, &w8, &w9}) b->resize(n);
+    // zero like MTJ's new DenseVector(n): SSOR starts its sweeps from the
+    // previous contents of its output vector
+    for (auto* b : {&w1, &w2, &w3, &w4, &w5, &w6, &w7, &w8, &w9}) {
+      b->resize(n);
+      RSG_CUDA(cudaMemsetAsync(b->get(), 0, sizeof(double) * n, ctx->stream));
+    }
     nblk = std::max(1, std::min(blocks_for(n, RT), 16384));
     part.resize((size_t)4 * nblk);
   }
@@ -678,6 +683,7 @@ struct Solver {
       default: throw Error(RSG_UNSUPPORTED, "unknown iterative method");
     }
     read_state();
+    ctx->check_device_error();
     if (info) {
       info->iterations = hstate->iter;
       info->residual = hstate->residual;
@@ -1010,6 +1016,7 @@ static rsg_status precond_host(rsg_solver* s, const double* b, double* x, bool t
     else s->s->pc->apply(db.get(), dx.get(), nullptr);
     RSG_CUDA(cudaMemcpyAsync(x, dx.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
+    ctx->check_device_error();
   });
 }
 

@@ -22,7 +22,16 @@ struct SweepPlan {
   DeviceBuffer<double> diag;  // diagonal per slot row (upper sweeps)
   DeviceBuffer<float> diagf;
   int max_rows_per_level = 0;
+  // Push-ring schedule for one cluster of RING_CTAS x RING_WARPS warps: every
+  // level fits the cluster's warps (one slice per warp) and every entry
+  // refers to a row of the last ring_R - 1 levels.  ring_R == 0: unavailable.
+  int ring_R = 0, ring_slot = 0;
+  DeviceBuffer<int> ridx;         // per entry slot: ring index of the column's value
+  DeviceBuffer<int> ring_expect;  // per level and CTA rank: rows the other CTAs push
 };
+
+constexpr int RING_CTAS = 8;
+constexpr int RING_WARPS = 8;
 
 struct Csr {
   Context* ctx = nullptr;

@@ -12,6 +12,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <string>
 
 #include "linalg.cuh"
 
@@ -204,6 +206,207 @@ __global__ void __launch_bounds__(256) k_sweep_pipelined(SweepArgs<T> a) {
     cluster.sync();
     cur = nxt;
     m1 = m2;
+  }
+}
+
+// ILU sweeps with the computed values exchanged through distributed shared
+// memory instead of L2.  Every CTA of the cluster keeps a replica of the
+// values of the last R levels (a ring of R level slots in its shared
+// memory).  The lane that computes a row writes the value into its own
+// replica and pushes it into the other CTAs' replicas with st.async, whose
+// completion is counted in bytes on the receiving CTA's mbarrier of that
+// level slot.  Besides its rows, each CTA pushes one 8-byte token per level
+// to every other CTA once it has finished the previous level, so a level's
+// phase completes only when every CTA is done with the level before it: no
+// CTA runs more than one level ahead of another.  A CTA starts level l once
+// its mbarrier of level l-1 has seen every byte owed to it (armed with
+// expect_tx from a host-built table) and a CTA barrier has published its
+// own rows; all operand gathers are then local shared-memory loads and there
+// is no cluster-wide barrier per level.
+//
+// Slot reuse: a CTA pushing level l into slot l mod R has seen the token of
+// every CTA for level l-1, so each of them has finished level l-2 and is at
+// most computing level l-1, whose operands lie in levels >= l-1-(R-2) when
+// R >= lookback + 2; slot l mod R held level l-R, which nobody reads any
+// more, and its mbarrier phase for level l-R has completed.
+struct RingArgs {
+  int R;                // ring depth in levels (>= lookback + 2)
+  int slot;             // values per level slot (slices x 32)
+  const int* ridx;      // per entry slot: ring index of the column's value
+  const int* expect;    // per level and CTA rank: rows pushed by the other CTAs
+  int* err;             // set to 1 + level when a wait runs out
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned cluster_addr(unsigned a, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned a, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arm(unsigned a, unsigned tx) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(tx) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(unsigned a, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: false when the phase did not complete within the limit
+__device__ __forceinline__ bool mbar_wait(unsigned a, unsigned parity) {
+  for (int i = 0; i < (1 << 22); ++i)
+    if (mbar_test(a, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void push_b64(unsigned remote, unsigned long long v, unsigned rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(remote), "l"(v),
+               "r"(rbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void push_value(unsigned remote, double v, unsigned rbar) {
+  push_b64(remote, (unsigned long long)__double_as_longlong(v), rbar);
+}
+
+__device__ __forceinline__ void push_value(unsigned remote, float v, unsigned rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(remote),
+               "r"(__float_as_uint(v)), "r"(rbar)
+               : "memory");
+}
+
+template <int KIND, typename T, int MAXW>
+__device__ __forceinline__ void load_ring_coeffs(const SweepArgs<T>& a, const RingArgs& g, const int* ls,
+                                                 const SlotMeta& m, int l, int gwarp, int lane,
+                                                 RowPrefetch<T, MAXW>& p) {
+  p.row = m.row;
+  p.len = m.row >= 0 ? m.len : 0;
+  p.base = m.base;
+  const int r = m.row >= 0 ? m.row : 0;
+  p.b = a.b[r];
+  if (KIND == SW_ILU_UPPER) {
+    const int s = (m.row >= 0) ? ls[l] + gwarp : 0;
+    p.d = a.diag[s * 32 + lane];
+  }
+#pragma unroll
+  for (int k = 0; k < MAXW; ++k)
+    if (k < p.len) {
+      p.v[k] = a.val[p.base + 32 * k];
+      p.c[k] = g.ridx[p.base + 32 * k];
+    }
+}
+
+constexpr int RING_TOKEN_BYTES = 8;
+
+// Dynamic shared memory of k_sweep_ring: ring, mbarriers, tokens, level offsets.
+template <typename T>
+__host__ __device__ inline size_t ring_smem_bytes(int R, int slot, int nlev) {
+  return sizeof(T) * (size_t)R * slot + 8 * (size_t)R + RING_TOKEN_BYTES * (size_t)RING_CTAS +
+         4 * (size_t)(nlev + 1);
+}
+
+template <int KIND, typename T, int MAXW>
+__global__ void __launch_bounds__(RING_WARPS * 32) k_sweep_ring(SweepArgs<T> a, RingArgs g) {
+  if (a.active && *a.active != 0) return;  // uniform over the cluster
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* ring = reinterpret_cast<T*>(smem);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + sizeof(T) * (size_t)g.R * g.slot);
+  unsigned long long* tok = bar + g.R;
+  int* ls = reinterpret_cast<int*>(tok + RING_CTAS);
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned rank = cluster.block_rank();
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)rank * RING_WARPS + (threadIdx.x >> 5);
+  const unsigned ring0 = smem_addr(ring), bar0 = smem_addr(bar), tok0 = smem_addr(tok);
+  if (threadIdx.x < g.R) mbar_init(bar0 + 8 * threadIdx.x, 1);
+  for (int q = threadIdx.x; q <= a.nlev; q += blockDim.x) ls[q] = a.level_slices[q];
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  cluster.sync();  // every replica's barriers exist before the first push
+  unsigned rring[RING_CTAS], rbar[RING_CTAS];
+#pragma unroll
+  for (int c = 0; c < RING_CTAS; ++c) {
+    rring[c] = cluster_addr(ring0, c);
+    rbar[c] = cluster_addr(bar0, c);
+  }
+  RowPrefetch<T, MAXW> cur, nxt;
+  SlotMeta m1 = load_meta(a, ls, 1, gwarp, lane);
+  {
+    SlotMeta m0 = load_meta(a, ls, 0, gwarp, lane);
+    load_ring_coeffs<KIND, T, MAXW>(a, g, ls, m0, 0, gwarp, lane, cur);
+  }
+  const unsigned token_tx = RING_TOKEN_BYTES * (RING_CTAS - 1);
+  int exp_cur = (threadIdx.x == 0 && a.nlev > 0) ? g.expect[rank] : 0;
+  int slot_l = 0, par_l = 0, slot_p = 0, par_p = 0;  // level l and level l-1
+  bool ok = true;
+  for (int l = 0; l < a.nlev; ++l) {
+    if (threadIdx.x == 0) mbar_arm(bar0 + 8 * slot_l, (unsigned)(exp_cur * sizeof(T)) + token_tx);
+    const int exp_nxt = (threadIdx.x == 0 && l + 1 < a.nlev) ? g.expect[(l + 1) * RING_CTAS + rank] : 0;
+    const SlotMeta m2 = load_meta(a, ls, l + 2, gwarp, lane);
+    load_ring_coeffs<KIND, T, MAXW>(a, g, ls, m1, l + 1, gwarp, lane, nxt);
+    const int late = (l > 0) ? !mbar_wait(bar0 + 8 * slot_p, par_p) : 0;
+    if (__syncthreads_or(late)) {
+      if (threadIdx.x == 0) atomicCAS(g.err, 0, 1 + l);
+      ok = false;
+      break;
+    }
+    if (threadIdx.x == 0) {
+      // this CTA has finished level l-1
+#pragma unroll
+      for (int c = 0; c < RING_CTAS; ++c)
+        if (c != (int)rank)
+          push_b64(cluster_addr(tok0, c) + RING_TOKEN_BYTES * rank, (unsigned long long)l, rbar[c] + 8 * slot_l);
+    }
+    if (cur.row >= 0) {
+      T sum = 0;
+#pragma unroll
+      for (int k = 0; k < MAXW; ++k)
+        if (k < cur.len) sum += cur.v[k] * ring[cur.c[k]];
+      for (int k = MAXW; k < cur.len; ++k) {
+        const int q = cur.base + 32 * k;
+        sum += a.val[q] * ring[g.ridx[q]];
+      }
+      const T v = (KIND == SW_ILU_LOWER) ? cur.b - sum : (cur.b - sum) / cur.d;
+      const int own = slot_l * g.slot + gwarp * 32 + lane;
+      ring[own] = v;
+      const unsigned off = (unsigned)(own * sizeof(T)), boff = (unsigned)(8 * slot_l);
+#pragma unroll
+      for (int c = 0; c < RING_CTAS; ++c)
+        if (c != (int)rank) push_value(rring[c] + off, v, rbar[c] + boff);
+      a.x[cur.row] = v;
+    }
+    cur = nxt;
+    m1 = m2;
+    exp_cur = exp_nxt;
+    slot_p = slot_l;
+    par_p = par_l;
+    if (++slot_l == g.R) {
+      slot_l = 0;
+      par_l ^= 1;
+    }
+  }
+  if (ok && a.nlev > 0) {
+    // everything owed to this CTA lands before any CTA may exit
+    if (!mbar_wait(bar0 + 8 * slot_p, par_p)) {
+      atomicCAS(g.err, 0, 1 + a.nlev);
+      ok = false;
+    }
+  }
+  cluster.sync();
+  if (*(volatile int*)g.err != 0) {
+    // a wait ran out somewhere: give pushes still in flight time to land
+    for (int i = 0; i < 64; ++i) __nanosleep(1000);
   }
 }
 
@@ -437,6 +640,44 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
         src[base[s] + 32 * k + lane] = q;
       }
     }
+  // push-ring schedule (lower or upper ILU parts only)
+  std::vector<int> ridx, expect;
+  P.ring_R = 0;
+  if (entries != 2) {
+    int max_sl = 0, look = 0;
+    for (int l = 0; l < nlev; ++l) max_sl = std::max(max_sl, level_slices[l + 1] - level_slices[l]);
+    std::vector<int> ring_pos(n);  // slice offset within the level * 32 + lane
+    for (int l = 0; l < nlev; ++l)
+      for (int t = 0; t < cnt[l + 1] - cnt[l]; ++t) ring_pos[order[cnt[l] + t]] = t;
+    for (int i = 0; i < n; ++i) {
+      int b0, b1, c0, c1;
+      row_entries(i, b0, b1, c0, c1);
+      for (int q = b0; q < b1; ++q) look = std::max(look, lev[i] - lev[cl[q]]);
+    }
+    const int R = look + 2;
+    if (max_sl <= RING_CTAS * RING_WARPS && R <= 32) {
+      P.ring_R = R;
+      P.ring_slot = max_sl * 32;
+      ridx.assign(col.size(), 0);
+      for (int s = 0; s < ns; ++s)
+        for (int lane = 0; lane < 32; ++lane) {
+          int r = row[(size_t)s * 32 + lane];
+          if (r < 0) continue;
+          for (int k = 0; k < len[(size_t)s * 32 + lane]; ++k) {
+            int c = col[base[s] + 32 * k + lane];
+            ridx[base[s] + 32 * k + lane] = (lev[c] % R) * P.ring_slot + ring_pos[c];
+          }
+        }
+      expect.assign((size_t)nlev * RING_CTAS, 0);
+      for (int l = 0; l < nlev; ++l) {
+        int rows = cnt[l + 1] - cnt[l];
+        for (int c = 0; c < RING_CTAS; ++c) {
+          int own = std::min(std::max(rows - c * RING_WARPS * 32, 0), RING_WARPS * 32);
+          expect[(size_t)l * RING_CTAS + c] = rows - own;
+        }
+      }
+    }
+  }
   Context& ctx = *A.ctx;
   P.nlev = nlev;
   P.nslices = ns;
@@ -458,6 +699,12 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
   up(P.len, len);
   up(P.col, col);
   up(P.src, src);
+  if (P.ring_R) {
+    P.ridx.resize(ridx.size());
+    P.ring_expect.resize(expect.size());
+    up(P.ridx, ridx);
+    up(P.ring_expect, expect);
+  }
   if (with_diag) {
     P.diag_src.resize(dsrc.size());
     P.diag.resize(dsrc.size());
@@ -524,11 +771,72 @@ static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Ar
   return true;
 }
 
+// Push-ring launch: one cluster of RING_CTAS CTAs with the ring, its
+// mbarriers and the level offsets in dynamic shared memory.  Returns false
+// when the ring does not fit or the cluster cannot be scheduled.
+static int g_ring_mode = -1;  // -1: not probed; 0 off; 1 on (RSG_SWEEP=pipelined switches it off)
+static bool g_ring_used = false;
+
+template <int KIND, typename T>
+static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, const SweepArgs<T>& a) {
+  if (g_ring_mode < 0) {
+    const char* e = getenv("RSG_SWEEP");
+    g_ring_mode = (e && std::string(e) == "pipelined") ? 0 : 1;
+  }
+  if (!g_ring_mode || !P.ring_R || ctx.cluster_size != RING_CTAS) return false;
+  const size_t smem = ring_smem_bytes<T>(P.ring_R, P.ring_slot, P.nlev);
+  if (smem > 200 * 1024) return false;
+  auto kern = k_sweep_ring<KIND, T, 16>;
+  static int attr_set[2][2] = {{0, 0}, {0, 0}};
+  int& done = attr_set[KIND == SW_ILU_UPPER][sizeof(T) == 8];
+  if (!done) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(RING_CTAS);
+    cfg.blockDim = dim3(RING_WARPS * 32);
+    cfg.dynamicSmemBytes = 200 * 1024;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = RING_CTAS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, (const void*)kern, &cfg);
+    cudaGetLastError();
+    done = (e == cudaSuccess && nclusters >= 1) ? 1 : -1;
+  }
+  if (done < 0) return false;
+  RingArgs g{P.ring_R, P.ring_slot, P.ridx.get(), P.ring_expect.get(), ctx.dev_err.get()};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(RING_CTAS);
+  cfg.blockDim = dim3(RING_WARPS * 32);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = RING_CTAS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  LaunchScope scope(ctx, name);
+  RSG_CUDA(cudaLaunchKernelEx(&cfg, kern, a, g));
+  g_ring_used = true;
+  return true;
+}
+
 template <int KIND, typename T>
 static void run_sweep(Context& ctx, const char* name, const SweepPlan& P, const T* val, const T* diag, const T* b,
                       T* x, T* xx, T omega, const int* active) {
   SweepArgs<T> a{P.nlev, P.level_slices.get(), P.slice_base.get(), P.row.get(), P.len.get(), P.col.get(), val, diag,
                  b, x, xx, omega, active};
+  if constexpr (KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER)
+    if (launch_ring<KIND, T>(ctx, name, P, a)) return;
   if ((KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER) && P.nlev <= SWEEP_MAX_LEVELS) {
     if (launch_cluster(ctx, name, k_sweep_pipelined<KIND, T, 16>, a, 256)) return;
   } else if (launch_cluster(ctx, name, k_sweep_cluster<KIND, T>, a))
@@ -820,4 +1128,4 @@ void release_trans_plan(const Precond* p) {
 
 }  // namespace rsg
 
-extern "C" int32_t rsg_sweep_mode(void) { return rsg::g_cluster_ok; }
+extern "C" int32_t rsg_sweep_mode(void) { return rsg::g_ring_used ? 2 : rsg::g_cluster_ok; }
