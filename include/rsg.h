@@ -158,6 +158,15 @@ rsg_status rsg_precond_apply(rsg_solver* s, const double* b, double* x);
 rsg_status rsg_precond_trans_apply(rsg_solver* s, const double* b, double* x);
 /* Residual history of the last solve (monitor values in call order). */
 rsg_status rsg_solver_history(rsg_solver* s, int32_t max_len, double* out, int32_t* len);
+/* AMG hierarchy built by rsg_solver_setup (sparse/AMG.java:224-286), for
+ * inspection: the number of levels, and per level k its operator (CSR), the
+ * aggregate of each node (pt, -1 if none) and the smoothed interpolation in
+ * CompColMatrix form (colptr, rowind, data).  sizes = {n, nnz, coarse size,
+ * nnz of the interpolation}; the coarse size is 0 on the last level.  Any
+ * array may be NULL.  No counterpart in the reference (its fields are private). */
+rsg_status rsg_solver_amg_levels(rsg_solver* s, int32_t* levels);
+rsg_status rsg_solver_amg_level(rsg_solver* s, int32_t k, int32_t* sizes, int32_t* rowptr, int32_t* col,
+                                double* val, int32_t* pt, int32_t* colptr, int32_t* rowind, double* idata);
 
 /* No-allocation CG: conjugate gradients with the diagonal preconditioner on
  * a CSR matrix and vectors that are already in device memory, for callers

@@ -38,6 +38,7 @@ std::unique_ptr<Preconditioner> make_pc(int precond, double omegaF, double omega
       s->reverse = reverse != 0;
       return std::unique_ptr<Preconditioner>(s);
     }
+    case P_AMG: return std::unique_ptr<Preconditioner>(new AMG());
   }
   throw Failure(ST_UNSUPPORTED, "preconditioner not available in the oracle");
 }
@@ -329,6 +330,61 @@ int orc_sim_jacobian(void* h, double* vals, double* rhs) {
   if (vals && !s->lastJ.empty()) std::memcpy(vals, s->lastJ.data(), sizeof(double) * s->lastJ.size());
   if (rhs && !s->lastRhs.empty()) std::memcpy(rhs, s->lastRhs.data(), sizeof(double) * s->lastRhs.size());
   return 0;
+}
+
+// AMG hierarchy access for the parity tests.
+void* orc_amg_create(int n, int nnz, const int* rowptr, const int* col, const double* val, int* status, char* err,
+                     int errlen) {
+  try {
+    auto* a = new AMG();
+    a->setMatrix(make_csr(n, nnz, rowptr, col, val));
+    *status = 0;
+    return a;
+  } catch (Failure& f) {
+    *status = f.status;
+    put_err(err, errlen, f.what());
+    return nullptr;
+  }
+}
+
+void orc_amg_destroy(void* h) { delete (AMG*)h; }
+
+int orc_amg_levels(void* h) { return (int)((AMG*)h)->L.size(); }
+
+// sizes[0..3] = n, nnz, c (coarse size, 0 on the last level), nnz of I
+void orc_amg_level_sizes(void* h, int k, int* sizes) {
+  const AMGLevel& l = ((AMG*)h)->L[k];
+  sizes[0] = l.A.n;
+  sizes[1] = l.A.nnz();
+  sizes[2] = l.c;
+  sizes[3] = (int)l.rowind.size();
+}
+
+void orc_amg_level_get(void* h, int k, int* rowptr, int* col, double* val, int* pt, int* colptr, int* rowind,
+                       double* Idata) {
+  const AMGLevel& l = ((AMG*)h)->L[k];
+  std::memcpy(rowptr, l.A.rowptr.data(), sizeof(int) * (l.A.n + 1));
+  std::memcpy(col, l.A.col.data(), sizeof(int) * l.A.nnz());
+  std::memcpy(val, l.A.data.data(), sizeof(double) * l.A.nnz());
+  if (pt && !l.pt.empty()) std::memcpy(pt, l.pt.data(), sizeof(int) * l.pt.size());
+  if (colptr && !l.colptr.empty()) std::memcpy(colptr, l.colptr.data(), sizeof(int) * l.colptr.size());
+  if (rowind && !l.rowind.empty()) std::memcpy(rowind, l.rowind.data(), sizeof(int) * l.rowind.size());
+  if (Idata && !l.Idata.empty()) std::memcpy(Idata, l.Idata.data(), sizeof(double) * l.Idata.size());
+}
+
+int orc_amg_apply(void* h, const double* b, double* x, int trans, char* err, int errlen) {
+  AMG* a = (AMG*)h;
+  const int n = a->L[0].A.n;
+  try {
+    Vec vb(b, b + n), vx(x, x + n);
+    if (trans) a->transApply(vb, vx);
+    else a->apply(vb, vx);
+    std::memcpy(x, vx.data(), sizeof(double) * n);
+    return 0;
+  } catch (Failure& f) {
+    put_err(err, errlen, f.what());
+    return f.status;
+  }
 }
 
 int orc_sim_residual_volume(void* h, double* R, double* dRdp) {

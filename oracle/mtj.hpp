@@ -136,6 +136,36 @@ struct SSOR : Preconditioner {
   void setMatrix(const CompRowMatrix& A) override;
 };
 
+// Smoothed-aggregation AMG V-cycle (sparse/AMG.java) with the default
+// parameters of AMG() (:204-206): SSOR(1, 1.85) pre- and SSOR(1.85, 1)
+// post-smoothing, one of each, V-cycle, coarsest size 40, omega 2/3.
+struct AMGLevel {
+  CompRowMatrix A;              // Galerkin operator of this level
+  std::vector<int> pt;          // tentative prolongation: aggregate of each node (-1: none)
+  int c = 0;                    // coarse size
+  std::vector<int> colptr, rowind;  // smoothed interpolation I (n x c), CompColMatrix
+  Vec Idata;
+  SSOR pre, post;
+  Vec u, f, r;
+};
+
+struct AMG : Preconditioner {
+  double omegaPreF = 1, omegaPreR = 1.85, omegaPostF = 1.85, omegaPostR = 1;
+  int nu1 = 1, nu2 = 1, gamma = 1, min = 40;
+  double omega = 2. / 3;
+  std::vector<AMGLevel> L;  // L.size() == m; the last level keeps only A, u, f
+  Vec lu;                   // LU factors of the coarsest operator (column major)
+  std::vector<int> piv;
+  int nc = 0;               // coarsest size
+  bool singular = false;
+  bool transpose = false;
+  void apply(const Vec& b, Vec& x) override;       // AMG.java:208-214
+  void transApply(const Vec& b, Vec& x) override;  // :216-222
+  void setMatrix(const CompRowMatrix& A) override; // :224-286
+  void cycle(int k);                               // :288-313
+  void directSolve();                              // :315-323
+};
+
 enum Method : int32_t { M_CG = 0, M_BICGSTAB = 1, M_GMRES = 2 };
 enum Precond : int32_t { P_NONE = 0, P_DIAGONAL = 1, P_ILU = 2, P_SSOR = 3, P_AMG = 4 };
 
@@ -146,6 +176,11 @@ enum Precond : int32_t { P_NONE = 0, P_DIAGONAL = 1, P_ILU = 2, P_SSOR = 3, P_AM
 void cg_solve(const CompRowMatrix& A, const Vec& b, Vec& x, Preconditioner& M, IterationMonitor& it);
 void bicgstab_solve(const CompRowMatrix& A, const Vec& b, Vec& x, Preconditioner& M, IterationMonitor& it);
 void gmres_solve(const CompRowMatrix& A, const Vec& b, Vec& x, Preconditioner& M, IterationMonitor& it, int restart);
+
+// netlib dgetf2 (unblocked LU with partial pivoting, as dgetrf runs it for
+// n below its block size) and dgetrs ('N' or 'T') on a column-major matrix.
+int dgetf2(int n, double* A, int lda, int* ipiv);
+void dgetrs(bool trans, int n, const double* A, int lda, const int* ipiv, double* b);
 
 // Dense LU with partial pivoting as netlib LAPACK dgesv (dgetf2 + dgetrs),
 // the routine MTJ's DenseMatrix.solve -> LUsolve reaches

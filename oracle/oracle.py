@@ -61,6 +61,16 @@ def _declare(L):
     L.orc_sim_state.argtypes = [vp, P(d), P(d), P(d)]
     L.orc_sim_jacobian.argtypes = [vp, P(d), P(d)]
     L.orc_sim_residual_volume.argtypes = [vp, P(d), P(d)]
+    L.orc_amg_create.restype = vp
+    L.orc_amg_create.argtypes = [i, i, P(C.c_int32), P(C.c_int32), P(d), P(i), C.c_char_p, i]
+    L.orc_amg_destroy.argtypes = [vp]
+    L.orc_amg_levels.argtypes = [vp]
+    L.orc_amg_levels.restype = i
+    L.orc_amg_level_sizes.argtypes = [vp, i, P(C.c_int32)]
+    L.orc_amg_level_get.argtypes = [vp, i, P(C.c_int32), P(C.c_int32), P(d), P(C.c_int32), P(C.c_int32),
+                                    P(C.c_int32), P(d)]
+    L.orc_amg_apply.argtypes = [vp, P(d), P(d), i, C.c_char_p, i]
+    L.orc_amg_apply.restype = i
 
 
 class OracleError(RuntimeError):
@@ -294,3 +304,51 @@ class Simulator:
         d = np.zeros(self.n)
         lib().orc_sim_residual_volume(self.h, abi.dptr(R), abi.dptr(d))
         return R, d
+
+
+class AMG:
+    """MTJ AMG() on the CPU: hierarchy (per level: A, aggregates pt,
+    interpolation I in CompColMatrix form) and the V-cycle apply."""
+
+    def __init__(self, rowptr, col, val):
+        rowptr, col, val = _i32(rowptr), _i32(col), _f64(val)
+        st = C.c_int(0)
+        err = C.create_string_buffer(512)
+        self.h = lib().orc_amg_create(len(rowptr) - 1, len(col), abi.iptr(rowptr), abi.iptr(col), abi.dptr(val),
+                                      C.byref(st), err, 512)
+        if not self.h:
+            raise OracleError(st.value, err.value.decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_amg_destroy(self.h)
+            self.h = None
+
+    def levels(self):
+        return lib().orc_amg_levels(self.h)
+
+    def level(self, k):
+        sz = np.zeros(4, np.int32)
+        lib().orc_amg_level_sizes(self.h, k, abi.iptr(sz))
+        n, nnz, c, pn = (int(v) for v in sz)
+        rp = np.zeros(n + 1, np.int32)
+        col = np.zeros(max(nnz, 1), np.int32)
+        val = np.zeros(max(nnz, 1))
+        pt = np.zeros(max(n, 1), np.int32) if c else None
+        cp = np.zeros(c + 1, np.int32) if c else None
+        ri = np.zeros(max(pn, 1), np.int32) if c else None
+        iv = np.zeros(max(pn, 1)) if c else None
+        lib().orc_amg_level_get(self.h, k, abi.iptr(rp), abi.iptr(col), abi.dptr(val), abi.iptr(pt), abi.iptr(cp),
+                                abi.iptr(ri), abi.dptr(iv))
+        out = {"n": n, "rowptr": rp, "col": col[:nnz], "val": val[:nnz], "c": c}
+        if c:
+            out.update(pt=pt[:n], colptr=cp, rowind=ri[:pn], Idata=iv[:pn])
+        return out
+
+    def apply(self, b, x0, trans=False):
+        x = _f64(x0).copy()
+        err = C.create_string_buffer(512)
+        st = lib().orc_amg_apply(self.h, abi.dptr(_f64(b)), abi.dptr(x), int(trans), err, 512)
+        if st != 0:
+            raise OracleError(st, err.value.decode())
+        return x

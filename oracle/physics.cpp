@@ -479,6 +479,7 @@ Simulator::Simulator(const Mesh& m, const rsg_blackoil& fluid, const rsg_corey& 
     case RSG_PC_DIAGONAL: M.reset(new DiagonalPreconditioner()); break;
     case RSG_PC_ILU: M.reset(new ILU()); break;
     case RSG_PC_SSOR: M.reset(new SSOR()); break;
+    case RSG_PC_AMG: M.reset(new AMG()); break;
     default: throw Failure(ST_UNSUPPORTED, "preconditioner not available in the oracle");
   }
   p_prev.assign(n, 0);

@@ -91,6 +91,8 @@ def _declare(L):
         "rsg_precond_apply": (i32, [vp, P(d), P(d)]),
         "rsg_precond_trans_apply": (i32, [vp, P(d), P(d)]),
         "rsg_solver_history": (i32, [vp, i32, P(d), P(i32)]),
+        "rsg_solver_amg_levels": (i32, [vp, P(i32)]),
+        "rsg_solver_amg_level": (i32, [vp, i32, P(i32), P(i32), P(i32), P(d), P(i32), P(i32), P(i32), P(d)]),
         "rsg_cg_diagonal_noalloc": (i32, [i32, vp, i32, i32, vp, vp, vp, vp, vp, d, d, d, i32,
                                             P(abi.rsg_solve_info)]),
         "rsg_mesh_create_structured": (i32, [vp, i32, i32, i32, i32, P(d), d, d, d, d, d, d, P(d), PP()]),
@@ -322,6 +324,32 @@ class IterativeSolver:
         f = lib().rsg_precond_trans_apply if trans else lib().rsg_precond_apply
         self.ctx.check(f(self.h, abi.dptr(b), abi.dptr(x)), "apply")
         return x
+
+    def amg_levels(self):
+        n = C.c_int32(0)
+        self.ctx.check(lib().rsg_solver_amg_levels(self.h, C.byref(n)), "amg_levels")
+        return n.value
+
+    def amg_level(self, k):
+        """Level k of the AMG hierarchy: operator (CSR), aggregates and the
+        interpolation operator by columns."""
+        sz = np.zeros(4, np.int32)
+        self.ctx.check(lib().rsg_solver_amg_level(self.h, k, abi.iptr(sz), *([None] * 7)), "amg_level")
+        n, nnz, c, pn = (int(v) for v in sz)
+        rp = np.zeros(n + 1, np.int32)
+        col = np.zeros(max(nnz, 1), np.int32)
+        val = np.zeros(max(nnz, 1))
+        pt = np.zeros(max(n, 1), np.int32)
+        cp = np.zeros(c + 1, np.int32)
+        ri = np.zeros(max(pn, 1), np.int32)
+        iv = np.zeros(max(pn, 1))
+        self.ctx.check(lib().rsg_solver_amg_level(self.h, k, abi.iptr(sz), abi.iptr(rp), abi.iptr(col), abi.dptr(val),
+                                                  abi.iptr(pt), abi.iptr(cp), abi.iptr(ri), abi.dptr(iv)),
+                       "amg_level")
+        out = {"n": n, "rowptr": rp, "col": col[:nnz], "val": val[:nnz], "c": c}
+        if c:
+            out.update(pt=pt[:n], colptr=cp, rowind=ri[:pn], Idata=iv[:pn])
+        return out
 
     def history(self):
         n = C.c_int32(0)

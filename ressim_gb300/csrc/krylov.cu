@@ -1023,6 +1023,24 @@ static rsg_status precond_host(rsg_solver* s, const double* b, double* x, bool t
 rsg_status rsg_precond_apply(rsg_solver* s, const double* b, double* x) { return precond_host(s, b, x, false); }
 rsg_status rsg_precond_trans_apply(rsg_solver* s, const double* b, double* x) { return precond_host(s, b, x, true); }
 
+rsg_status rsg_solver_amg_levels(rsg_solver* s, int32_t* levels) {
+  if (!s || !levels) return RSG_BAD_ARG;
+  return guarded(s->s->ctx, [&] { *levels = rsg::amg_levels(s->s->pc.get()); });
+}
+
+rsg_status rsg_solver_amg_level(rsg_solver* s, int32_t k, int32_t* sizes, int32_t* rowptr, int32_t* col,
+                                double* val, int32_t* pt, int32_t* colptr, int32_t* rowind, double* idata) {
+  if (!s) return RSG_BAD_ARG;
+  return guarded(s->s->ctx, [&] {
+    int sz[4];
+    rsg::amg_level_sizes(s->s->pc.get(), k, sz);
+    if (sizes)
+      for (int q = 0; q < 4; ++q) sizes[q] = sz[q];
+    if (rowptr || col || val || pt || colptr || rowind || idata)
+      rsg::amg_level_get(s->s->pc.get(), k, rowptr, col, val, pt, colptr, rowind, idata);
+  });
+}
+
 rsg_status rsg_solver_history(rsg_solver* s, int32_t max_len, double* out, int32_t* len) {
   if (!s) return RSG_BAD_ARG;
   return guarded(s->s->ctx, [&] {

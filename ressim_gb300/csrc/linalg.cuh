@@ -22,16 +22,15 @@ struct SweepPlan {
   DeviceBuffer<double> diag;  // diagonal per slot row (upper sweeps)
   DeviceBuffer<float> diagf;
   int max_rows_per_level = 0;
-  // Push-ring schedule for one cluster of RING_CTAS x RING_WARPS warps: every
-  // level fits the cluster's warps (one slice per warp) and every entry
-  // refers to a row of the last ring_R - 1 levels.  ring_R == 0: unavailable.
+  // Push-ring schedule for one cluster whose warps take one slice each
+  // (RING_SLICES warps in all): every level fits and every entry refers to a
+  // row of the last ring_R - 2 levels.  ring_R == 0: unavailable.
   int ring_R = 0, ring_slot = 0;
-  DeviceBuffer<int> ridx;         // per entry slot: ring index of the column's value
-  DeviceBuffer<int> ring_expect;  // per level and CTA rank: rows the other CTAs push
+  DeviceBuffer<int> ridx;            // per entry slot: ring index of the column's value
+  DeviceBuffer<int> ring_expect[2];  // clusters of 8 / 16 CTAs: per level and rank, rows the others push
 };
 
-constexpr int RING_CTAS = 8;
-constexpr int RING_WARPS = 8;
+constexpr int RING_SLICES = 64;
 
 struct Csr {
   Context* ctx = nullptr;
@@ -85,6 +84,11 @@ struct Precond {
 };
 
 std::unique_ptr<Precond> make_precond(Context* ctx, int kind);
+std::unique_ptr<Precond> make_amg(Context* ctx);  // amg.cu
+int amg_levels(Precond* p);
+void amg_level_sizes(Precond* p, int k, int* sizes);
+void amg_level_get(Precond* p, int k, int* rowptr, int* col, double* val, int* pt, int* colptr, int* rowind,
+                   double* Idata);
 
 // Krylov solver handle (defined in krylov.cu)
 struct Solver;

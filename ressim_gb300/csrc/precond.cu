@@ -309,22 +309,24 @@ __device__ __forceinline__ void load_ring_coeffs(const SweepArgs<T>& a, const Ri
 }
 
 constexpr int RING_TOKEN_BYTES = 8;
+constexpr int RING_MAX_CTAS = 16;
 
 // Dynamic shared memory of k_sweep_ring: ring, mbarriers, tokens, level offsets.
 template <typename T>
 __host__ __device__ inline size_t ring_smem_bytes(int R, int slot, int nlev) {
-  return sizeof(T) * (size_t)R * slot + 8 * (size_t)R + RING_TOKEN_BYTES * (size_t)RING_CTAS +
+  return sizeof(T) * (size_t)R * slot + 8 * (size_t)R + RING_TOKEN_BYTES * (size_t)RING_MAX_CTAS +
          4 * (size_t)(nlev + 1);
 }
 
-template <int KIND, typename T, int MAXW>
-__global__ void __launch_bounds__(RING_WARPS * 32) k_sweep_ring(SweepArgs<T> a, RingArgs g) {
+template <int KIND, typename T, int MAXW, int RING_CTAS>
+__global__ void __launch_bounds__(RING_SLICES / RING_CTAS * 32) k_sweep_ring(SweepArgs<T> a, RingArgs g) {
+  constexpr int RING_WARPS = RING_SLICES / RING_CTAS;
   if (a.active && *a.active != 0) return;  // uniform over the cluster
   extern __shared__ __align__(16) unsigned char smem[];
   T* ring = reinterpret_cast<T*>(smem);
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + sizeof(T) * (size_t)g.R * g.slot);
   unsigned long long* tok = bar + g.R;
-  int* ls = reinterpret_cast<int*>(tok + RING_CTAS);
+  int* ls = reinterpret_cast<int*>(tok + RING_MAX_CTAS);
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
   const int lane = threadIdx.x & 31;
@@ -641,7 +643,7 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
       }
     }
   // push-ring schedule (lower or upper ILU parts only)
-  std::vector<int> ridx, expect;
+  std::vector<int> ridx, expect[2];
   P.ring_R = 0;
   if (entries != 2) {
     int max_sl = 0, look = 0;
@@ -655,7 +657,7 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
       for (int q = b0; q < b1; ++q) look = std::max(look, lev[i] - lev[cl[q]]);
     }
     const int R = look + 2;
-    if (max_sl <= RING_CTAS * RING_WARPS && R <= 32) {
+    if (max_sl <= RING_SLICES && R <= 32) {
       P.ring_R = R;
       P.ring_slot = max_sl * 32;
       ridx.assign(col.size(), 0);
@@ -668,12 +670,16 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
             ridx[base[s] + 32 * k + lane] = (lev[c] % R) * P.ring_slot + ring_pos[c];
           }
         }
-      expect.assign((size_t)nlev * RING_CTAS, 0);
-      for (int l = 0; l < nlev; ++l) {
-        int rows = cnt[l + 1] - cnt[l];
-        for (int c = 0; c < RING_CTAS; ++c) {
-          int own = std::min(std::max(rows - c * RING_WARPS * 32, 0), RING_WARPS * 32);
-          expect[(size_t)l * RING_CTAS + c] = rows - own;
+      for (int e = 0; e < 2; ++e) {
+        const int C = 8 << e, W = RING_SLICES / C;
+        auto& ex = expect[e];
+        ex.assign((size_t)nlev * C, 0);
+        for (int l = 0; l < nlev; ++l) {
+          int rows = cnt[l + 1] - cnt[l];
+          for (int c = 0; c < C; ++c) {
+            int own = std::min(std::max(rows - c * W * 32, 0), W * 32);
+            ex[(size_t)l * C + c] = rows - own;
+          }
         }
       }
     }
@@ -701,9 +707,11 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
   up(P.src, src);
   if (P.ring_R) {
     P.ridx.resize(ridx.size());
-    P.ring_expect.resize(expect.size());
     up(P.ridx, ridx);
-    up(P.ring_expect, expect);
+    for (int e = 0; e < 2; ++e) {
+      P.ring_expect[e].resize(expect[e].size());
+      up(P.ring_expect[e], expect[e]);
+    }
   }
   if (with_diag) {
     P.diag_src.resize(dsrc.size());
@@ -771,55 +779,61 @@ static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Ar
   return true;
 }
 
-// Push-ring launch: one cluster of RING_CTAS CTAs with the ring, its
-// mbarriers and the level offsets in dynamic shared memory.  Returns false
-// when the ring does not fit or the cluster cannot be scheduled.
-static int g_ring_mode = -1;  // -1: not probed; 0 off; 1 on (RSG_SWEEP=pipelined switches it off)
+// Push-ring launch: one cluster with the ring, its mbarriers and the level
+// offsets in dynamic shared memory.  FP64 walks use a cluster of 16 CTAs
+// (4 warps each) when the device schedules one, since their time per level
+// is bound by the SMs' FP64 rate; FP32 walks use 8 CTAs of 8 warps.
+// RSG_SWEEP=pipelined switches the ring off, RSG_RING_CTAS=8|16 forces the
+// cluster size.  Returns false when the ring does not fit or no cluster can
+// be scheduled.
+static int g_ring_mode = -1;  // -1: not read; 0 off; 1 on
+static int g_ring_ctas = 0;   // forced cluster size, 0: automatic
 static bool g_ring_used = false;
 
-template <int KIND, typename T>
-static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, const SweepArgs<T>& a) {
-  if (g_ring_mode < 0) {
-    const char* e = getenv("RSG_SWEEP");
-    g_ring_mode = (e && std::string(e) == "pipelined") ? 0 : 1;
-  }
-  if (!g_ring_mode || !P.ring_R || ctx.cluster_size != RING_CTAS) return false;
-  const size_t smem = ring_smem_bytes<T>(P.ring_R, P.ring_slot, P.nlev);
-  if (smem > 200 * 1024) return false;
-  auto kern = k_sweep_ring<KIND, T, 16>;
-  static int attr_set[2][2] = {{0, 0}, {0, 0}};
-  int& done = attr_set[KIND == SW_ILU_UPPER][sizeof(T) == 8];
-  if (!done) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(RING_CTAS);
-    cfg.blockDim = dim3(RING_WARPS * 32);
-    cfg.dynamicSmemBytes = 200 * 1024;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = RING_CTAS;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, (const void*)kern, &cfg);
+template <typename Kernel>
+static bool ring_schedulable(Kernel kern, int ctas, size_t smem) {
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
-    done = (e == cudaSuccess && nclusters >= 1) ? 1 : -1;
+    return false;
   }
-  if (done < 0) return false;
-  RingArgs g{P.ring_R, P.ring_slot, P.ridx.get(), P.ring_expect.get(), ctx.dev_err.get()};
+  if (ctas > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(RING_CTAS);
-  cfg.blockDim = dim3(RING_WARPS * 32);
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(RING_SLICES / ctas * 32);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ctas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, (const void*)kern, &cfg);
+  cudaGetLastError();
+  return e == cudaSuccess && nclusters >= 1;
+}
+
+constexpr size_t RING_SMEM_MAX = 200 * 1024;
+
+template <int KIND, typename T, int CTAS>
+static bool launch_ring_n(Context& ctx, const char* name, const SweepPlan& P, const SweepArgs<T>& a, size_t smem) {
+  auto kern = k_sweep_ring<KIND, T, 16, CTAS>;
+  static int ok = 0;  // per instantiation: 0 not probed, 1 schedulable, -1 not
+  if (!ok) ok = ring_schedulable(kern, CTAS, RING_SMEM_MAX) ? 1 : -1;
+  if (ok < 0) return false;
+  RingArgs g{P.ring_R, P.ring_slot, P.ridx.get(), P.ring_expect[CTAS == 16].get(), ctx.dev_err.get()};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CTAS);
+  cfg.blockDim = dim3(RING_SLICES / CTAS * 32);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = ctx.stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = RING_CTAS;
+  attr[0].val.clusterDim.x = CTAS;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
@@ -828,6 +842,22 @@ static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, cons
   RSG_CUDA(cudaLaunchKernelEx(&cfg, kern, a, g));
   g_ring_used = true;
   return true;
+}
+
+template <int KIND, typename T>
+static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, const SweepArgs<T>& a) {
+  if (g_ring_mode < 0) {
+    const char* e = getenv("RSG_SWEEP");
+    g_ring_mode = (e && std::string(e) == "pipelined") ? 0 : 1;
+    const char* c = getenv("RSG_RING_CTAS");
+    g_ring_ctas = c ? atoi(c) : 0;
+  }
+  if (!g_ring_mode || !P.ring_R) return false;
+  const size_t smem = ring_smem_bytes<T>(P.ring_R, P.ring_slot, P.nlev);
+  if (smem > RING_SMEM_MAX) return false;
+  const bool want16 = g_ring_ctas ? g_ring_ctas == 16 : sizeof(T) == 8;
+  if (want16 && launch_ring_n<KIND, T, 16>(ctx, name, P, a, smem)) return true;
+  return launch_ring_n<KIND, T, 8>(ctx, name, P, a, smem);
 }
 
 template <int KIND, typename T>
@@ -1108,6 +1138,7 @@ std::unique_ptr<Precond> make_precond(Context* ctx, int kind) {
     case RSG_PC_DIAGONAL: return std::unique_ptr<Precond>(new DiagPrecond(ctx));
     case RSG_PC_ILU: return std::unique_ptr<Precond>(new ILUPrecond(ctx));
     case RSG_PC_SSOR: return std::unique_ptr<Precond>(new SSORPrecond(ctx));
+    case RSG_PC_AMG: return make_amg(ctx);
   }
   throw Error(RSG_UNSUPPORTED, "preconditioner not implemented");
 }
