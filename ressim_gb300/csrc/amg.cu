@@ -662,6 +662,10 @@ struct AMGPrecond : Precond {
     Context& c = *ctx;
     Csr& A = *lv.A;
     const int n = A.n, nnz = A.nnz;
+    // Aggregator.findDiagonalIndices (AMG.java:446-461)
+    for (int i = 0; i < n; ++i)
+      if (A.h_diag[i] < 0)
+        throw Error(RSG_MISSING_DIAGONAL, "Matrix is missing a diagonal entry on row " + std::to_string(i + 1));
     const int eb = blocks_for(n, 256);
     DeviceBuffer<unsigned char> S(std::max(nnz, 1)), R0(n), free2(n);
     DeviceBuffer<int> a1(n), a2(n), a3(n);
