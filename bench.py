@@ -109,6 +109,12 @@ def build_case(args):
     return case, keep, fluid, co, srcs, init, spec
 
 
+# DRAM bytes (read + write) per launch of the ILU(0) level walks, from one ncu
+# capture of this workload (profiles/ilu_sweep_ring_two_phase_128x128x32.md);
+# keyed by grid size and kernel family.
+NCU_TRAFFIC = {(128, 128, 32): {"ilu_lower": 91_904_000, "ilu_upper": 95_707_136}}
+
+
 def sweep_bytes(rp, col):
     """Algorithmic bytes of one ILU(0) triangular sweep: each strictly
     lower (or upper) coefficient (8 B) and its column index (4 B), the
@@ -254,8 +260,9 @@ def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, ne
         tot_ms, cnt = sweeps[k]
         per_launch = tot_ms / cnt / 1e3
         achieved = fam_bytes[k] / per_launch / 1e9
+        traffic = NCU_TRAFFIC.get((args.ni, args.nj, args.nk), {}).get(k)
         roof = {"bound": "hbm", "kernel": k, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 5), "traffic": None, "peak_source": peak_kind,
+                "frac": round(achieved / hbm, 5), "traffic": traffic, "peak_source": peak_kind,
                 "bytes_per_launch": fam_bytes[k], "avg_launch_us": round(per_launch * 1e6, 2)}
     spmv_ms = prof.get("spmv_dot", (0, 1))
     spmv_bytes = 12 * len(col) + 4 * (n + 1) + 16 * n + 8 * n

@@ -283,7 +283,11 @@ __global__ void __launch_bounds__(RT) k_resid(int n, const int* __restrict__ sb,
   reduce_finish<2>(v, ra.part, ra.ticket, epi, ra.s, ra.hist, ra.g, 0);
 }
 
-// y = A x (mult semantics) and dots y.w (and y.z, y.y)
+// y = A x (mult semantics) and dots y.w (and y.z, y.y).  Each product is
+// fused into its running sum (one rounding per term): on this part the FP64
+// pipe, not HBM, bounds an unfused SpMV (a multiply and an add per entry).
+// The Krylov iterates therefore differ from MTJ's in the last bits, within
+// the solver parity bound; rsg_csr_mult keeps MTJ's unfused arithmetic.
 template <int K>
 __global__ void __launch_bounds__(RT) k_spmv_dot(int n, const int* __restrict__ sb, const int* __restrict__ rl,
                                                  const int* __restrict__ col, const double* __restrict__ val,
@@ -300,14 +304,14 @@ __global__ void __launch_bounds__(RT) k_spmv_dot(int n, const int* __restrict__ 
 #pragma unroll 8
     for (int k = 0; k < len; ++k) {
       int q = base + 32 * k;
-      d += val[q] * __ldg(x + col[q]);
+      d = __fma_rn(val[q], __ldg(x + col[q]), d);
     }
     double yi = (d != 0) ? d : 0.0;
     y[row] = yi;
-    if (K == 1) v[0] += w[row] * yi;  // rtilde.dot(v) / p.dot(q) order: w_i * y_i
+    if (K == 1) v[0] = __fma_rn(w[row], yi, v[0]);  // rtilde.dot(v) / p.dot(q)
     if (K == 2) {
-      v[0] += yi * w[row];  // t.dot(s)
-      v[1] += yi * yi;      // t.dot(t)
+      v[0] = __fma_rn(yi, w[row], v[0]);  // t.dot(s)
+      v[1] = __fma_rn(yi, yi, v[1]);      // t.dot(t)
     }
   }
   reduce_finish<K>(v, ra.part, ra.ticket, epi, ra.s, ra.hist, ra.g, 0);
