@@ -322,6 +322,42 @@ rsg_status rsg_sim_get_jacobian(rsg_sim* s, double* values, double* rhs);
 /* Per-cell secondaries after the last update: R, dRdp (n each). */
 rsg_status rsg_sim_get_residual_volume(rsg_sim* s, double* R, double* dRdp);
 
+/* Time-step control: the RunSpec keys of numerics/RunSpec.java:146-204 (the
+ * defaults are those of RunSpec). */
+typedef struct {
+  double lambda;                        /* Lambda, 0.5 */
+  double target_residual_volume;        /* TargetResidualVolume, 1e-2 */
+  int32_t target_nonlinear_iterations;  /* TargetNonLinearPressureIterations, 5 */
+  double target_throughput;             /* TargetThroughputRatio, 0.5 */
+  double dt_min, dt_max;                /* TimeStepMinimum, TimeStepMaximum [s] */
+} rsg_dt_control;
+
+typedef struct {
+  double residual_volume, pressure_iterations, throughput; /* the three dt factors */
+  int32_t limit; /* 0 none, 1 maximum timestep, 2 residual volume, 3 pressure iterations, 4 throughput */
+} rsg_dt_factors;
+
+typedef struct {
+  int32_t steps, retries;           /* accepted steps, retracted attempts */
+  int32_t newton_iterations, linear_iterations;
+  double time;                      /* field time reached [s] */
+  int32_t status;                   /* status of the last attempt */
+} rsg_step_to_info;
+
+/* Field.getTime: advanced by every rsg_sim_step, restored by rsg_sim_retract. */
+rsg_status rsg_sim_get_time(rsg_sim* s, double* t);
+/* Discretisation.calculateDt(dt) (numerics/Discretisation.java:928-1002): the
+ * next time step after a successful step of size dt. */
+rsg_status rsg_sim_calculate_dt(rsg_sim* s, double dt, const rsg_dt_control* c, double* dt_new, rsg_dt_factors* f);
+/* Discretisation.throughputFactor (:986-998) */
+rsg_status rsg_sim_throughput_factor(rsg_sim* s, const rsg_dt_control* c, double* factor);
+/* TimeStepper.stepTo(endTime) (numerics/TimeStepper.java:58-102): steps to
+ * end_time; a step that fails with a SolverFailure status (1, 2, 3, 7, 8, 13)
+ * is retracted and retried with dt * min(1/2, throughputFactor) while
+ * dt > dt_min.  *dt is the time step carried between calls (TimeStepper.dt,
+ * dt_min initially). */
+rsg_status rsg_sim_step_to(rsg_sim* s, double end_time, const rsg_dt_control* c, double* dt, rsg_step_to_info* info);
+
 #ifdef __cplusplus
 }
 #endif

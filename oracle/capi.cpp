@@ -307,6 +307,26 @@ int orc_sim_step(void* h, double dt, rsg_step_info* info, char* err, int errlen)
   return 0;
 }
 
+double orc_sim_time(void* h) { return ((Simulator*)h)->time; }
+
+int orc_sim_calculate_dt(void* h, double dt, const rsg_dt_control* c, double* dt_new, rsg_dt_factors* f) {
+  *dt_new = ((Simulator*)h)->calculateDt(dt, *c, f);
+  return 0;
+}
+
+double orc_sim_throughput_factor(void* h, const rsg_dt_control* c) { return ((Simulator*)h)->throughputFactor(*c); }
+
+int orc_sim_step_to(void* h, double end_time, const rsg_dt_control* c, double* dt, rsg_step_to_info* info, char* err,
+                    int errlen) {
+  try {
+    return ((Simulator*)h)->stepTo(end_time, *c, *dt, info);
+  } catch (Failure& f) {
+    put_err(err, errlen, f.what());
+    if (info) info->status = f.status;
+    return f.status;
+  }
+}
+
 int orc_sim_retract(void* h) {
   ((Simulator*)h)->retract();
   return 0;

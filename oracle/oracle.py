@@ -61,6 +61,12 @@ def _declare(L):
     L.orc_sim_state.argtypes = [vp, P(d), P(d), P(d)]
     L.orc_sim_jacobian.argtypes = [vp, P(d), P(d)]
     L.orc_sim_residual_volume.argtypes = [vp, P(d), P(d)]
+    L.orc_sim_time.restype = d
+    L.orc_sim_time.argtypes = [vp]
+    L.orc_sim_calculate_dt.argtypes = [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_dt_factors)]
+    L.orc_sim_throughput_factor.restype = d
+    L.orc_sim_throughput_factor.argtypes = [vp, P(abi.rsg_dt_control)]
+    L.orc_sim_step_to.argtypes = [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_step_to_info), C.c_char_p, i]
     L.orc_amg_create.restype = vp
     L.orc_amg_create.argtypes = [i, i, P(C.c_int32), P(C.c_int32), P(d), P(i), C.c_char_p, i]
     L.orc_amg_destroy.argtypes = [vp]
@@ -282,6 +288,26 @@ class Simulator:
         if st != 0 and raise_on_fail:
             raise OracleError(st, err.value.decode())
         return info
+
+    def time(self):
+        return lib().orc_sim_time(self.h)
+
+    def calculate_dt(self, dt, ctl):
+        out = C.c_double(0)
+        f = abi.rsg_dt_factors()
+        lib().orc_sim_calculate_dt(self.h, dt, C.byref(ctl), C.byref(out), C.byref(f))
+        return out.value, f
+
+    def throughput_factor(self, ctl):
+        return lib().orc_sim_throughput_factor(self.h, C.byref(ctl))
+
+    def step_to(self, end_time, ctl, dt):
+        """TimeStepper.stepTo; returns (status, dt carried to the next call, info)."""
+        d = C.c_double(dt)
+        info = abi.rsg_step_to_info()
+        err = C.create_string_buffer(512)
+        st = lib().orc_sim_step_to(self.h, end_time, C.byref(ctl), C.byref(d), C.byref(info), err, 512)
+        return st, d.value, info
 
     def retract(self):
         lib().orc_sim_retract(self.h)

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <memory>
 #include <set>
 
@@ -830,7 +831,9 @@ void Simulator::molarMass(double dt) {
 int Simulator::step(double dt, rsg_step_info* info) {
   // Discretisation.solve (:208-225) with PressureNewtonRaphson.solve (:280-332)
   storeCurrentState();
-  int pressureIterations = 0;
+  time += dt;  // field.changeTime(dt)
+  lastDt = dt;
+  pressureIterations = 0;
   double dpMax = 0, dpMax_prev = 0, diff = 0;
   int linIts = 0;
   const bool refRule = spec.newton_stop_rule == 0;
@@ -866,7 +869,8 @@ int Simulator::step(double dt, rsg_step_info* info) {
 }
 
 void Simulator::retract() {
-  // Discretisation.retractField -> Field.retract (field/Field.java:535-545)
+  // Discretisation.retractField(dt) -> Field.retract(t - dt, ...) (field/Field.java:535-545)
+  time -= lastDt;
   const int n = mesh->numElements();
   for (int i = 0; i < n; ++i) {
     cv[i].p = p_prev[i];
@@ -874,6 +878,112 @@ void Simulator::retract() {
     for (int nu = 0; nu < nc; ++nu) cv[i].N[nu] = N_prev[(size_t)nu * n + i];
   }
   calculateSecondaries();
+}
+
+// Math.max with Java's NaN rule
+static double jmax(double a, double b) {
+  if (a != a) return a;
+  if (b != b) return b;
+  return a >= b ? a : b;
+}
+
+double Simulator::dtFactor(double value, double target, const rsg_dt_control& c) const {
+  // Discretisation.dtFactor (:1000-1002)
+  return (1 + c.lambda) * target / (value + c.lambda * target);
+}
+
+double Simulator::residualVolumeFactor(const rsg_dt_control& c) const {
+  // :966-978
+  double maxR = 0;
+  for (int i = 0; i < mesh->numElements(); ++i) {
+    double R = cv[i].R;
+    double Vp = mesh->evolume[i] * cv[i].phi;
+    maxR = jmax(maxR, std::fabs(R) / Vp);
+  }
+  return dtFactor(maxR, c.target_residual_volume, c);
+}
+
+double Simulator::throughputFactor(const rsg_dt_control& c) const {
+  // :986-998; N[i] is the state stored at the start of the step
+  const int n = mesh->numElements();
+  double dNm = 0;
+  for (int i = 0; i < n; ++i) {
+    double Ni = 0;
+    for (int nu = 0; nu < nc; ++nu) Ni += N_prev[(size_t)nu * n + i];
+    double dNi = 0;
+    for (int nu = 0; nu < nc; ++nu) dNi += std::fabs(dN[(size_t)nu * n + i]);
+    dNm = jmax(dNm, dNi / Ni);
+  }
+  return dtFactor(dNm, c.target_throughput, c);
+}
+
+double Simulator::calculateDt(double dt, const rsg_dt_control& c, rsg_dt_factors* f) const {
+  // :928-964
+  double R = residualVolumeFactor(c);
+  double NR = dtFactor(pressureIterations, c.target_nonlinear_iterations, c);
+  double T = throughputFactor(c);
+  double dt_R = dt * R, dt_NR = dt * NR, dt_T = dt * T;
+  double dtNew = std::numeric_limits<double>::max();
+  dtNew = std::min(dtNew, dt_R);
+  dtNew = std::min(dtNew, dt_NR);
+  dtNew = std::min(dtNew, dt_T);
+  dtNew = std::min(dtNew, c.dt_max);
+  int limit = 0;
+  if (c.dt_max == dtNew) limit = 1;
+  else if (dt_R == dtNew) limit = 2;
+  else if (dt_NR == dtNew) limit = 3;
+  else if (dt_T == dtNew) limit = 4;
+  dtNew = std::max(dtNew, c.dt_min);
+  if (f) {
+    f->residual_volume = R;
+    f->pressure_iterations = NR;
+    f->throughput = T;
+    f->limit = limit;
+  }
+  return dtNew;
+}
+
+static bool solver_failure(int st) {
+  return st == ST_NOT_CONVERGED_ITERATIONS || st == ST_NOT_CONVERGED_DIVERGENCE || st == ST_NOT_CONVERGED_BREAKDOWN ||
+         st == ST_NONPOSITIVE_PRESSURE || st == ST_NEGATIVE_MOLES || st == ST_NEWTON_NOT_CONVERGED;
+}
+
+int Simulator::stepTo(double endTime, const rsg_dt_control& c, double& dt, rsg_step_to_info* info) {
+  // TimeStepper.stepTo (:58-102) with adjustDtForReporting (:117-128)
+  rsg_step_to_info loc{};
+  rsg_step_to_info& in = info ? *info : loc;
+  in = rsg_step_to_info{};
+  while (time < endTime) {
+    if (dt + time > endTime) dt = endTime - time;
+    while (true) {
+      rsg_step_info si{};
+      int st = 0;
+      try {
+        step(dt, &si);
+      } catch (Failure& f) {
+        st = f.status;
+        if (!solver_failure(st)) throw;
+      }
+      in.status = st;
+      if (st == 0) {
+        in.steps++;
+        in.newton_iterations += si.newton_iterations;
+        in.linear_iterations += si.linear_iterations;
+        break;
+      }
+      if (!(dt > c.dt_min)) {
+        in.time = time;
+        return st;  // timestep cannot be further reduced
+      }
+      retract();
+      in.retries++;
+      double factor = std::min(1. / 2., throughputFactor(c));
+      dt = std::min(std::max(dt * factor, c.dt_min), c.dt_max);
+    }
+    dt = calculateDt(dt, c, nullptr);
+  }
+  in.time = time;
+  return 0;
 }
 
 }  // namespace orc

@@ -112,6 +112,8 @@ struct Simulator {
   Vec lastJ, lastRhs;
   int lastLinearIterations = 0;
   double massBalance = 0;
+  double time = 0, lastDt = 0;  // Field.t, the last attempted step
+  int pressureIterations = 0;   // PressureNewtonRaphson.pressureIterations
 
   Simulator(const Mesh& mesh, const rsg_blackoil& fluid, const rsg_corey& rf, const double* poro, const double* comp,
             int nsources, const rsg_source* src, const rsg_initial& init, const rsg_runspec& spec);
@@ -132,6 +134,13 @@ struct Simulator {
   double updatePressure();
   void molarMass(double dt);
   void retract();
+  // Discretisation.calculateDt and its factors (:928-1002)
+  double dtFactor(double value, double target, const rsg_dt_control& c) const;
+  double residualVolumeFactor(const rsg_dt_control& c) const;
+  double throughputFactor(const rsg_dt_control& c) const;
+  double calculateDt(double dt, const rsg_dt_control& c, rsg_dt_factors* f) const;
+  // TimeStepper.stepTo (numerics/TimeStepper.java:58-102)
+  int stepTo(double endTime, const rsg_dt_control& c, double& dt, rsg_step_to_info* info);
 };
 
 }  // namespace orc

@@ -127,6 +127,50 @@ class rsg_runspec(C.Structure):
     ]
 
 
+class rsg_dt_control(C.Structure):
+    _fields_ = [
+        ("lambda_", C.c_double),
+        ("target_residual_volume", C.c_double),
+        ("target_nonlinear_iterations", C.c_int32),
+        ("target_throughput", C.c_double),
+        ("dt_min", C.c_double),
+        ("dt_max", C.c_double),
+    ]
+
+
+def dt_control(dt_min, dt_max, lam=0.5, target_residual_volume=1e-2, target_nonlinear_iterations=5,
+               target_throughput=0.5):
+    """RunSpec's time-step keys with RunSpec's defaults."""
+    c = rsg_dt_control()
+    c.lambda_ = lam
+    c.target_residual_volume = target_residual_volume
+    c.target_nonlinear_iterations = target_nonlinear_iterations
+    c.target_throughput = target_throughput
+    c.dt_min = dt_min
+    c.dt_max = dt_max
+    return c
+
+
+class rsg_dt_factors(C.Structure):
+    _fields_ = [
+        ("residual_volume", C.c_double),
+        ("pressure_iterations", C.c_double),
+        ("throughput", C.c_double),
+        ("limit", C.c_int32),
+    ]
+
+
+class rsg_step_to_info(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int32),
+        ("retries", C.c_int32),
+        ("newton_iterations", C.c_int32),
+        ("linear_iterations", C.c_int32),
+        ("time", C.c_double),
+        ("status", C.c_int32),
+    ]
+
+
 class rsg_step_info(C.Structure):
     _fields_ = [
         ("newton_iterations", C.c_int32),

@@ -113,6 +113,10 @@ def _declare(L):
         "rsg_sim_set_state": (i32, [vp, P(d), P(d)]),
         "rsg_sim_get_jacobian": (i32, [vp, P(d), P(d)]),
         "rsg_sim_get_residual_volume": (i32, [vp, P(d), P(d)]),
+        "rsg_sim_get_time": (i32, [vp, P(d)]),
+        "rsg_sim_calculate_dt": (i32, [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_dt_factors)]),
+        "rsg_sim_throughput_factor": (i32, [vp, P(abi.rsg_dt_control), P(d)]),
+        "rsg_sim_step_to": (i32, [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_step_to_info)]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)
@@ -484,6 +488,34 @@ class Discretisation:
 
     def retract(self):
         self.ctx.check(lib().rsg_sim_retract(self.h), "retract")
+
+    def time(self):
+        """Field.getTime [s]."""
+        t = C.c_double(0)
+        self.ctx.check(lib().rsg_sim_get_time(self.h, C.byref(t)), "time")
+        return t.value
+
+    def calculate_dt(self, dt, ctl):
+        """Discretisation.calculateDt: (next dt, rsg_dt_factors)."""
+        out = C.c_double(0)
+        f = abi.rsg_dt_factors()
+        self.ctx.check(lib().rsg_sim_calculate_dt(self.h, dt, C.byref(ctl), C.byref(out), C.byref(f)), "calculateDt")
+        return out.value, f
+
+    def throughput_factor(self, ctl):
+        out = C.c_double(0)
+        self.ctx.check(lib().rsg_sim_throughput_factor(self.h, C.byref(ctl), C.byref(out)), "throughputFactor")
+        return out.value
+
+    def step_to(self, end_time, ctl, dt):
+        """TimeStepper.stepTo: (status, dt carried to the next call, rsg_step_to_info).
+        A status other than 0 is a failure the time step could not be reduced past."""
+        d = C.c_double(dt)
+        info = abi.rsg_step_to_info()
+        st = lib().rsg_sim_step_to(self.h, end_time, C.byref(ctl), C.byref(d), C.byref(info))
+        if st not in (0, 1, 2, 3, 7, 8, 13):
+            self.ctx.check(st, "stepTo")
+        return st, d.value, info
 
     def state(self):
         p = np.zeros(self.n)

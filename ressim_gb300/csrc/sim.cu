@@ -12,6 +12,8 @@
 // ascending connection order, so the assembled Jacobian, residual and mass
 // changes equal the sequential Java loops without atomics.
 #include <algorithm>
+#include <cstring>
+#include <limits>
 #include <cmath>
 
 #include "mesh.cuh"
@@ -867,6 +869,30 @@ static double fmax_out(const rsg_function& f) {
   return *std::max_element(f.data, f.data + total);
 }
 
+// Per-cell terms of Discretisation.residualVolumeFactor and throughputFactor
+// (numerics/Discretisation.java:966-998), reduced by maximum: |R| / (V phi)
+// with the porosity of calculateRockProperties, and sum_nu |dN_nu| / N_prev
+// with dN zero in locked cells.  Both are non-negative (or NaN, which wins as
+// Math.max lets it), so their IEEE bit patterns order like their values.
+__global__ void k_dt_terms(SimDev d, const int* __restrict__ locked, const double* __restrict__ N_prev,
+                           const double* __restrict__ dN, unsigned long long* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const int n = d.n;
+  const double c = d.cr[i];
+  const double dpp = d.p[i] - d.p0[i];
+  const double phi = d.phi0[i] * (1 + c * dpp + c * c * dpp * dpp / 2);
+  const double Vp = d.vol[i] * phi;
+  const double r = fabs(d.R[i]) / Vp;
+  double Ni = 0, dNi = 0;
+  for (int nu = 0; nu < d.nc; ++nu) Ni += N_prev[(int64_t)nu * n + i];
+  if (!locked[i])
+    for (int nu = 0; nu < d.nc; ++nu) dNi += fabs(dN[(int64_t)nu * n + i]);
+  const double t = dNi / Ni;
+  atomicMax(out, (unsigned long long)__double_as_longlong(r));
+  atomicMax(out + 1, (unsigned long long)__double_as_longlong(t));
+}
+
 struct Sim {
   Context* ctx;
   Mesh* mesh;
@@ -888,6 +914,9 @@ struct Sim {
   DeviceBuffer<double> dp0;
   rsg_csr A;
   SolverPtr solver;
+  double time = 0, last_dt = 0;  // Field.t and the last attempted step
+  int last_newton = 0;           // PressureNewtonRaphson.pressureIterations
+  DeviceBuffer<unsigned long long> dt_terms;
   std::vector<double> h_src_total;  // dt-independent sum of regular source rates per component
   bool keep_jacobian = false;
 
@@ -961,6 +990,8 @@ struct Sim {
   void step(double dt, rsg_step_info* info) {
     if (!(dt > 0)) throw Error(RSG_BAD_ARG, "time step must be positive");
     store_state();
+    time += dt;  // field.changeTime(dt)
+    last_dt = dt;
     int its = 0, lin = 0;
     double dpMax = 0, dp0h = 0;
     const bool ref_rule = spec.newton_stop_rule == 0;
@@ -1011,6 +1042,7 @@ struct Sim {
     ctx->sync();
     if (bad != INT32_MAX) throw Error(RSG_NEGATIVE_MOLES, "Negative number of moles in element " + std::to_string(bad));
     secondaries();
+    last_newton = its;
     if (info) {
       info->newton_iterations = its;
       info->linear_iterations = lin;
@@ -1045,7 +1077,102 @@ struct Sim {
     return worst;
   }
 
+  // residual-volume and throughput terms (max over cells)
+  void dt_terms_max(double* rmax, double* tmax) {
+    dt_terms.resize(2);
+    RSG_CUDA(cudaMemsetAsync(dt_terms.get(), 0, 2 * sizeof(unsigned long long), ctx->stream));
+    RSG_LAUNCH(*ctx, "dt_terms", k_dt_terms, blocks_for(n, 256), 256, 0, dev(), locked.get(), N_prev.get(),
+               dNbuf.get(), dt_terms.get());
+    unsigned long long h[2];
+    RSG_CUDA(cudaMemcpyAsync(h, dt_terms.get(), sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    std::memcpy(rmax, &h[0], sizeof(double));
+    std::memcpy(tmax, &h[1], sizeof(double));
+  }
+
+  static double dt_factor(double value, double target, const rsg_dt_control& c) {
+    // Discretisation.dtFactor (:1000-1002)
+    return (1 + c.lambda) * target / (value + c.lambda * target);
+  }
+
+  double throughput_factor(const rsg_dt_control& c) {
+    double r, t;
+    dt_terms_max(&r, &t);
+    return dt_factor(t, c.target_throughput, c);
+  }
+
+  double calculate_dt(double dt, const rsg_dt_control& c, rsg_dt_factors* f) {
+    // Discretisation.calculateDt (:928-964)
+    double rmax, tmax;
+    dt_terms_max(&rmax, &tmax);
+    const double R = dt_factor(rmax, c.target_residual_volume, c);
+    const double NR = dt_factor(last_newton, c.target_nonlinear_iterations, c);
+    const double T = dt_factor(tmax, c.target_throughput, c);
+    const double dt_R = dt * R, dt_NR = dt * NR, dt_T = dt * T;
+    double dtNew = std::numeric_limits<double>::max();
+    dtNew = std::min(dtNew, dt_R);
+    dtNew = std::min(dtNew, dt_NR);
+    dtNew = std::min(dtNew, dt_T);
+    dtNew = std::min(dtNew, c.dt_max);
+    int limit = 0;
+    if (c.dt_max == dtNew) limit = 1;
+    else if (dt_R == dtNew) limit = 2;
+    else if (dt_NR == dtNew) limit = 3;
+    else if (dt_T == dtNew) limit = 4;
+    dtNew = std::max(dtNew, c.dt_min);
+    if (f) {
+      f->residual_volume = R;
+      f->pressure_iterations = NR;
+      f->throughput = T;
+      f->limit = limit;
+    }
+    return dtNew;
+  }
+
+  static bool solver_failure(int st) {
+    return st == RSG_NOT_CONVERGED_ITERATIONS || st == RSG_NOT_CONVERGED_DIVERGENCE ||
+           st == RSG_NOT_CONVERGED_BREAKDOWN || st == RSG_NONPOSITIVE_PRESSURE || st == RSG_NEGATIVE_MOLES ||
+           st == RSG_NEWTON_NOT_CONVERGED;
+  }
+
+  int step_to(double end_time, const rsg_dt_control& c, double& dt, rsg_step_to_info& in) {
+    // TimeStepper.stepTo (numerics/TimeStepper.java:58-102)
+    in = rsg_step_to_info{};
+    while (time < end_time) {
+      if (dt + time > end_time) dt = end_time - time;  // adjustDtForReporting
+      for (;;) {
+        rsg_step_info si{};
+        int st = RSG_OK;
+        try {
+          step(dt, &si);
+        } catch (const Error& e) {
+          st = e.status;
+          if (!solver_failure(st)) throw;
+        }
+        in.status = st;
+        if (st == RSG_OK) {
+          in.steps++;
+          in.newton_iterations += si.newton_iterations;
+          in.linear_iterations += si.linear_iterations;
+          break;
+        }
+        if (!(dt > c.dt_min)) {
+          in.time = time;
+          return st;  // the time step cannot be reduced further
+        }
+        retract();
+        in.retries++;
+        const double factor = std::min(1. / 2., throughput_factor(c));
+        dt = std::min(std::max(dt * factor, c.dt_min), c.dt_max);
+      }
+      dt = calculate_dt(dt, c, nullptr);
+    }
+    in.time = time;
+    return RSG_OK;
+  }
+
   void retract() {
+    time -= last_dt;  // Field.retract(t - dt, ...)
     copy(p_prev, p, n);
     copy(T_prev, T, n);
     copy(N_prev, N, (int64_t)nc * n);
@@ -1278,6 +1405,35 @@ rsg_status rsg_sim_step(rsg_sim* s, double dt, rsg_step_info* info) {
   rsg_status st = guarded(s->s->ctx, [&] { s->s->step(dt, info); });
   if (info && st != RSG_OK) info->status = st;
   return st;
+}
+
+rsg_status rsg_sim_get_time(rsg_sim* s, double* t) {
+  if (!s || !t) return RSG_BAD_ARG;
+  *t = s->s->time;
+  return RSG_OK;
+}
+
+rsg_status rsg_sim_calculate_dt(rsg_sim* s, double dt, const rsg_dt_control* c, double* dt_new, rsg_dt_factors* f) {
+  if (!s || !c || !dt_new) return RSG_BAD_ARG;
+  return guarded(s->s->ctx, [&] { *dt_new = s->s->calculate_dt(dt, *c, f); });
+}
+
+rsg_status rsg_sim_throughput_factor(rsg_sim* s, const rsg_dt_control* c, double* factor) {
+  if (!s || !c || !factor) return RSG_BAD_ARG;
+  return guarded(s->s->ctx, [&] { *factor = s->s->throughput_factor(*c); });
+}
+
+rsg_status rsg_sim_step_to(rsg_sim* s, double end_time, const rsg_dt_control* c, double* dt, rsg_step_to_info* info) {
+  if (!s || !c || !dt) return RSG_BAD_ARG;
+  rsg_step_to_info loc{};
+  rsg_step_to_info& in = info ? *info : loc;
+  int st = RSG_OK;
+  rsg_status g = guarded(s->s->ctx, [&] { st = s->s->step_to(end_time, *c, *dt, in); });
+  if (g != RSG_OK) {
+    in.status = g;
+    return g;
+  }
+  return (rsg_status)st;
 }
 
 rsg_status rsg_sim_retract(rsg_sim* s) {

@@ -287,3 +287,30 @@ def test_two_phase_retract_restores_state(ctx):
     gs.retract()
     p1, N1, S1 = gs.state()
     assert np.array_equal(p0, p1) and np.array_equal(N0, N1) and np.array_equal(S0, S1)
+
+
+def test_step_to_adaptive_dt_matches_oracle(ctx):
+    """TimeStepper.stepTo with Discretisation.calculateDt: the same accepted
+    steps, retries and final time as the oracle, state within 1e-10."""
+    case, gm, om, gs, os_, keep = _two_phase(ctx, 12, 12, 4, spec_kw=dict(rtol=1e-12))
+    ctl = abi.dt_control(1.0, 100 * 86400.0)
+    gdt = odt = 20 * 86400.0  # a first step this large fails once and is retracted and retried
+    retries = 0
+    for end in (40 * 86400.0, 60 * 86400.0):
+        gst, gdt, gi = gs.step_to(end, ctl, gdt)
+        ost, odt, oi = os_.step_to(end, ctl, odt)
+        assert gst == ost == 0
+        assert (gi.steps, gi.retries, gi.newton_iterations) == (oi.steps, oi.retries, oi.newton_iterations)
+        retries += gi.retries
+        assert gs.time() == os_.time() == end
+        assert abs(gdt - odt) <= 1e-9 * odt
+        gp, gN, gS = gs.state()
+        op, oN, oS = os_.state()
+        assert np.max(np.abs(gp - op) / np.abs(op)) <= 1e-10
+        assert np.max(np.abs(gS - oS)) <= 1e-10
+    assert retries >= 1
+    g_new, gf = gs.calculate_dt(gdt, ctl)
+    o_new, of = os_.calculate_dt(odt, ctl)
+    assert gf.limit == of.limit
+    assert abs(g_new - o_new) <= 1e-9 * o_new
+    assert abs(gs.throughput_factor(ctl) - os_.throughput_factor(ctl)) <= 1e-9 * abs(os_.throughput_factor(ctl))
