@@ -344,6 +344,14 @@ typedef struct {
   int32_t status;                   /* status of the last attempt */
 } rsg_step_to_info;
 
+/* Ensembles: rsg_sim_step on every member, concurrently.  Each member must
+ * own its context (its own stream); members are driven from up to
+ * max_concurrent host threads (0: one per member), so their kernels overlap
+ * on the GPU.  Returns the first failing member's status (statuses[i] and
+ * infos[i] hold each member's).  Results equal stepping each member alone.
+ * No counterpart in the reference (RS runs one field per process). */
+rsg_status rsg_ensemble_step(int32_t count, rsg_sim* const* sims, const double* dt, int32_t max_concurrent,
+                             rsg_step_info* infos, int32_t* statuses);
 /* Field.getTime: advanced by every rsg_sim_step, restored by rsg_sim_retract. */
 rsg_status rsg_sim_get_time(rsg_sim* s, double* t);
 /* Discretisation.calculateDt(dt) (numerics/Discretisation.java:928-1002): the

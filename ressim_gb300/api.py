@@ -114,6 +114,7 @@ def _declare(L):
         "rsg_sim_get_jacobian": (i32, [vp, P(d), P(d)]),
         "rsg_sim_get_residual_volume": (i32, [vp, P(d), P(d)]),
         "rsg_sim_get_time": (i32, [vp, P(d)]),
+        "rsg_ensemble_step": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
         "rsg_sim_calculate_dt": (i32, [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_dt_factors)]),
         "rsg_sim_throughput_factor": (i32, [vp, P(abi.rsg_dt_control), P(d)]),
         "rsg_sim_step_to": (i32, [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_step_to_info)]),
@@ -561,3 +562,17 @@ class PinnedArray:
         if getattr(self, "p", None):
             lib().rsg_host_free(self.p)
             self.p = None
+
+
+def ensemble_step(sims, dts, max_concurrent=0):
+    """Steps every Discretisation of `sims` (each on its own Context)
+    concurrently; returns (per-member rsg_step_info list, statuses)."""
+    n = len(sims)
+    hs = (C.c_void_p * n)(*[s.h for s in sims])
+    d = np.ascontiguousarray(np.broadcast_to(np.asarray(dts, np.float64), (n,)))
+    infos = (abi.rsg_step_info * n)()
+    sts = np.zeros(n, np.int32)
+    st = lib().rsg_ensemble_step(n, hs, abi.dptr(d), max_concurrent, infos, abi.iptr(sts))
+    if st not in (0, 1, 2, 3, 7, 8, 13):
+        raise RSGError(st, "ensemble_step")
+    return list(infos), sts

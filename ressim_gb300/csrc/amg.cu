@@ -23,6 +23,7 @@
 // overlapping aggregates in ascending node order (MTJ's order is that of a
 // java.util.HashSet).
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <string>
 
@@ -683,11 +684,8 @@ struct AMGPrecond : Precond {
       gbits.resize((n + 31) / 32);
       smem = stage;
     }
-    static bool attr = false;
-    if (!attr) {
-      RSG_CUDA(cudaFuncSetAttribute(k_agg_greedy, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-      attr = true;
-    }
+    static std::once_flag attr;
+    std::call_once(attr, [] { cudaFuncSetAttribute(k_agg_greedy, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
     RSG_CUDA(cudaMemsetAsync(counter.get(), 0, sizeof(int), c.stream));
     PhaseArgs p1{n, A.rowptr.get(), A.col.get(), S.get(), R0.get(), nullptr, a1.get(), counter.get(), gbits.get(),
                  flag.get(), 0};

@@ -12,6 +12,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <cstdlib>
 #include <string>
 
@@ -741,11 +743,16 @@ static void plan_values(Context& ctx, SweepPlan& P, const double* csr_vals, bool
 
 // Cluster launch of a level walk; falls back to one launch per level when
 // clusters of the requested size cannot be scheduled.
-static int g_cluster_ok = -1;  // probed once per process
+// Probes run once per process; contexts driven from several host threads
+// (ensembles) take the lock for them.
+static std::mutex g_probe_mu;
+static std::atomic<int> g_cluster_ok{-1};  // probed once per process
 
 template <typename Kernel, typename Args>
 static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Args& args, int threads = 512) {
-  int& cluster_ok = g_cluster_ok;
+  std::atomic<int>& cluster_ok = g_cluster_ok;
+  std::unique_lock<std::mutex> lk(g_probe_mu, std::defer_lock);
+  if (cluster_ok < 0) lk.lock();
   if (cluster_ok < 0) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ctx.cluster_size);
@@ -762,6 +769,7 @@ static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Ar
     cluster_ok = (e == cudaSuccess && nclusters >= 1) ? 1 : 0;
     cudaGetLastError();
   }
+  if (lk.owns_lock()) lk.unlock();
   if (!cluster_ok) return false;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(ctx.cluster_size);
@@ -786,9 +794,9 @@ static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Ar
 // RSG_SWEEP=pipelined switches the ring off, RSG_RING_CTAS=8|16 forces the
 // cluster size.  Returns false when the ring does not fit or no cluster can
 // be scheduled.
-static int g_ring_mode = -1;  // -1: not read; 0 off; 1 on
-static int g_ring_ctas = 0;   // forced cluster size, 0: automatic
-static bool g_ring_used = false;
+static std::atomic<int> g_ring_mode{-1};  // -1: not read; 0 off; 1 on
+static int g_ring_ctas = 0;               // forced cluster size, 0: automatic
+static std::atomic<bool> g_ring_used{false};
 
 template <typename Kernel>
 static bool ring_schedulable(Kernel kern, int ctas, size_t smem) {
@@ -822,8 +830,11 @@ constexpr size_t RING_SMEM_MAX = 200 * 1024;
 template <int KIND, typename T, int CTAS>
 static bool launch_ring_n(Context& ctx, const char* name, const SweepPlan& P, const SweepArgs<T>& a, size_t smem) {
   auto kern = k_sweep_ring<KIND, T, 16, CTAS>;
-  static int ok = 0;  // per instantiation: 0 not probed, 1 schedulable, -1 not
-  if (!ok) ok = ring_schedulable(kern, CTAS, RING_SMEM_MAX) ? 1 : -1;
+  static std::atomic<int> ok{0};  // per instantiation: 0 not probed, 1 schedulable, -1 not
+  if (!ok) {
+    std::lock_guard<std::mutex> lk(g_probe_mu);
+    if (!ok) ok = ring_schedulable(kern, CTAS, RING_SMEM_MAX) ? 1 : -1;
+  }
   if (ok < 0) return false;
   RingArgs g{P.ring_R, P.ring_slot, P.ridx.get(), P.ring_expect[CTAS == 16].get(), ctx.dev_err.get()};
   cudaLaunchConfig_t cfg = {};
@@ -847,10 +858,13 @@ static bool launch_ring_n(Context& ctx, const char* name, const SweepPlan& P, co
 template <int KIND, typename T>
 static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, const SweepArgs<T>& a) {
   if (g_ring_mode < 0) {
-    const char* e = getenv("RSG_SWEEP");
-    g_ring_mode = (e && std::string(e) == "pipelined") ? 0 : 1;
-    const char* c = getenv("RSG_RING_CTAS");
-    g_ring_ctas = c ? atoi(c) : 0;
+    std::lock_guard<std::mutex> lk(g_probe_mu);
+    if (g_ring_mode < 0) {
+      const char* c = getenv("RSG_RING_CTAS");
+      g_ring_ctas = c ? atoi(c) : 0;
+      const char* e = getenv("RSG_SWEEP");
+      g_ring_mode = (e && std::string(e) == "pipelined") ? 0 : 1;
+    }
   }
   if (!g_ring_mode || !P.ring_R) return false;
   const size_t smem = ring_smem_bytes<T>(P.ring_R, P.ring_slot, P.nlev);
@@ -1159,4 +1173,4 @@ void release_trans_plan(const Precond* p) {
 
 }  // namespace rsg
 
-extern "C" int32_t rsg_sweep_mode(void) { return rsg::g_ring_used ? 2 : rsg::g_cluster_ok; }
+extern "C" int32_t rsg_sweep_mode(void) { return rsg::g_ring_used.load() ? 2 : rsg::g_cluster_ok.load(); }

@@ -12,6 +12,9 @@
 // ascending connection order, so the assembled Jacobian, residual and mass
 // changes equal the sequential Java loops without atomics.
 #include <algorithm>
+#include <atomic>
+#include <set>
+#include <thread>
 #include <cstring>
 #include <limits>
 #include <cmath>
@@ -1405,6 +1408,41 @@ rsg_status rsg_sim_step(rsg_sim* s, double dt, rsg_step_info* info) {
   rsg_status st = guarded(s->s->ctx, [&] { s->s->step(dt, info); });
   if (info && st != RSG_OK) info->status = st;
   return st;
+}
+
+rsg_status rsg_ensemble_step(int32_t count, rsg_sim* const* sims, const double* dt, int32_t max_concurrent,
+                             rsg_step_info* infos, int32_t* statuses) {
+  if (count < 0 || (count > 0 && (!sims || !dt))) return RSG_BAD_ARG;
+  std::set<rsg::Context*> ctxs;
+  for (int i = 0; i < count; ++i) {
+    if (!sims[i]) return RSG_BAD_ARG;
+    if (!ctxs.insert(sims[i]->s->ctx).second) return RSG_BAD_ARG;  // members must not share a context
+  }
+  const int workers = std::max(1, max_concurrent > 0 ? std::min<int>(max_concurrent, count) : count);
+  std::atomic<int> next{0};
+  std::vector<rsg_status> st(count, RSG_OK);
+  auto work = [&]() {
+    for (;;) {
+      const int i = next++;
+      if (i >= count) return;
+      rsg::Sim& m = *sims[i]->s;
+      rsg_step_info inf{};
+      st[i] = guarded(m.ctx, [&] {
+        RSG_CUDA(cudaSetDevice(m.ctx->device));
+        m.step(dt[i], &inf);
+      });
+      inf.status = st[i];
+      if (infos) infos[i] = inf;
+      if (statuses) statuses[i] = st[i];
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int w = 1; w < workers && w < count; ++w) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  for (int i = 0; i < count; ++i)
+    if (st[i] != RSG_OK) return st[i];
+  return RSG_OK;
 }
 
 rsg_status rsg_sim_get_time(rsg_sim* s, double* t) {

@@ -235,3 +235,27 @@ def build_initial(case):
     for nu in range(2, abi.MAX_COMPONENTS):
         init.fraction[nu] = abi.constant(0.0, 1)
     return init
+
+
+def build_two_phase_sim(ctx, ni, nj, nk, seed=1, **spec_kw):
+    """A Discretisation of the two-phase case on ctx (mesh, MPFA-O,
+    initialisation); returns (sim, case).  The arrays the library reads
+    through raw pointers stay referenced by the returned objects."""
+    from . import api
+
+    case = two_phase_case(ni=ni, nj=nj, nk=nk, seed=seed)
+    keep = abi.Keep()
+    fluid = two_phase_fluid(keep)
+    srcs = build_sources(keep, case)
+    mesh = api.Mesh(ctx, 3, ni, nj, nk, case["perm"], coords=case["nodes"])
+    mesh.compute_mpfa()
+    sim = api.Discretisation(ctx, mesh, fluid, corey(), case["porosity"], case["compaction"], srcs,
+                             build_initial(case), runspec(**spec_kw))
+    sim._member_keep = (keep, srcs, mesh)
+    return sim, case
+
+
+def ensemble_sizes(count, seed=7, lo=(32, 32, 8), hi=(96, 96, 24)):
+    """Grid sizes of an ensemble, each axis uniform in [lo, hi] from a seeded draw."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    return [tuple(int(g.integers(lo[a], hi[a] + 1)) for a in range(3)) for _ in range(count)]
