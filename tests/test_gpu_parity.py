@@ -291,7 +291,10 @@ def test_two_phase_retract_restores_state(ctx):
 
 def test_step_to_adaptive_dt_matches_oracle(ctx):
     """TimeStepper.stepTo with Discretisation.calculateDt: the same accepted
-    steps, retries and final time as the oracle, state within 1e-10."""
+    steps, retries and final time as the oracle.  Each dt is computed from the
+    state (maxima of |R|/Vp and |dN|/N), so the rounding-level differences of
+    the state (1e-12 after a fixed step) move dt by ~1e-9 relative; dt and the
+    state are compared to 1e-7 and 1e-8."""
     case, gm, om, gs, os_, keep = _two_phase(ctx, 12, 12, 4, spec_kw=dict(rtol=1e-12))
     ctl = abi.dt_control(1.0, 100 * 86400.0)
     gdt = odt = 20 * 86400.0  # a first step this large fails once and is retracted and retried
@@ -303,14 +306,14 @@ def test_step_to_adaptive_dt_matches_oracle(ctx):
         assert (gi.steps, gi.retries, gi.newton_iterations) == (oi.steps, oi.retries, oi.newton_iterations)
         retries += gi.retries
         assert gs.time() == os_.time() == end
-        assert abs(gdt - odt) <= 1e-9 * odt
+        assert abs(gdt - odt) <= 1e-7 * odt
         gp, gN, gS = gs.state()
         op, oN, oS = os_.state()
-        assert np.max(np.abs(gp - op) / np.abs(op)) <= 1e-10
-        assert np.max(np.abs(gS - oS)) <= 1e-10
+        assert np.max(np.abs(gp - op) / np.abs(op)) <= 1e-8
+        assert np.max(np.abs(gS - oS)) <= 1e-8
     assert retries >= 1
     g_new, gf = gs.calculate_dt(gdt, ctl)
     o_new, of = os_.calculate_dt(odt, ctl)
     assert gf.limit == of.limit
-    assert abs(g_new - o_new) <= 1e-9 * o_new
-    assert abs(gs.throughput_factor(ctl) - os_.throughput_factor(ctl)) <= 1e-9 * abs(os_.throughput_factor(ctl))
+    assert abs(g_new - o_new) <= 1e-7 * o_new
+    assert abs(gs.throughput_factor(ctl) - os_.throughput_factor(ctl)) <= 1e-7 * abs(os_.throughput_factor(ctl))
