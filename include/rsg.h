@@ -344,6 +344,39 @@ typedef struct {
   int32_t status;                   /* status of the last attempt */
 } rsg_step_to_info;
 
+/* ------------------------------------------- cubic equation of state --- */
+/* fluid/CubicEquationOfState.java: Peng-Robinson (or Soave-Redlich-Kwong)
+ * hydrocarbon phases with an isothermal flash, plus the water phase of
+ * WaterEquationOfState.  Component 0 is water; 1..nc-1 are hydrocarbons.
+ * Units are SI (K, Pa, kg/mol, m3/mol). */
+enum { RSG_EOS_PR = 0, RSG_EOS_SRK = 1 };
+typedef struct {
+  int32_t nc;                                   /* components including water */
+  int32_t eos;                                  /* RSG_EOS_PR (EOS key "PR") */
+  double Tc[RSG_MAX_COMPONENTS], pc[RSG_MAX_COMPONENTS], omega[RSG_MAX_COMPONENTS];
+  double Mw[RSG_MAX_COMPONENTS], Vc[RSG_MAX_COMPONENTS];
+  double shift[RSG_MAX_COMPONENTS];             /* volume shift s (ComponentData/<name>/s) */
+  double bic[RSG_MAX_COMPONENTS * RSG_MAX_COMPONENTS]; /* binary interaction dij, row major, symmetric */
+  double flash_criteria;                        /* FlashSwitchingCriteria: SS above, NR below (1e4) */
+  double flash_tolerance;                       /* FlashTolerance on max |f_oil - f_gas| [Pa] (1e-1) */
+  int32_t flash_max_iterations;                 /* no counterpart (the Java loop is unbounded) */
+  double lbc[5];                                /* Viscosity a1..a5 (0.1023, 0.023364, 0.058533, -0.040758, 0.0093324) */
+  rsg_function water_density, water_viscosity;  /* f(p, T) */
+} rsg_cubic_fluid;
+
+/* Per-phase record of EquationOfStateData, as doubles per cell:
+ * field f of phase a (0 water, 1 oil, 2 gas) of cell i lives at
+ * phases[(a * RSG_CUBIC_FIELDS(nc) + f) * n + i]; fields: present (0/1), V,
+ * xi, dVdp, dVdT, mu, N[nc], dVdN[nc]. */
+#define RSG_CUBIC_FIELDS(nc) (6 + 2 * (nc))
+/* CubicEquationOfState.calculatePhaseState for n cells (p, T: n; N: nc x n,
+ * component major).  phases is in/out: the oil and gas compositions it holds
+ * start the flash where both phases were present, as the Java object's
+ * persisted phase data do.  iterations (n, may be NULL) receives the flash
+ * iterations per cell.  Host arrays, one thread per cell on the GPU. */
+rsg_status rsg_cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
+                                 const double* T, const double* N, double* phases, int32_t* iterations);
+
 /* Ensembles: rsg_sim_step on every member, concurrently.  Each member must
  * own its context (its own stream); members are driven from up to
  * max_concurrent host threads (0: one per member), so their kernels overlap

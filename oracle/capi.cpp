@@ -307,6 +307,54 @@ int orc_sim_step(void* h, double dt, rsg_step_info* info, char* err, int errlen)
   return 0;
 }
 
+void orc_cubic_roots(double a0, double a1, double a2, double* z) { cubic_roots_kat(a0, a1, a2, z); }
+
+// phases: [3][6 + 2 nc][n] as rsg_cubic_phase_state
+int orc_cubic_phase_state(const rsg_cubic_fluid* fl, int n, const double* p, const double* T, const double* N,
+                          double* phases, int* iterations, char* err, int errlen) {
+  const int nc = fl->nc, nf = 6 + 2 * nc;
+  try {
+    Function wden(fl->water_density), wvis(fl->water_viscosity);
+    for (int i = 0; i < n; ++i) {
+      EOSData ph[3];
+      double Ni[RSG_MAX_COMPONENTS] = {0};
+      for (int nu = 0; nu < nc; ++nu) Ni[nu] = N[(size_t)nu * n + i];
+      for (int a = 0; a < 3; ++a) {
+        auto at = [&](int f) -> double& { return phases[((size_t)a * nf + f) * n + i]; };
+        ph[a].present = at(0) != 0;
+        ph[a].V = at(1);
+        ph[a].xi = at(2);
+        ph[a].dVdp = at(3);
+        ph[a].dVdT = at(4);
+        ph[a].mu = at(5);
+        for (int nu = 0; nu < nc; ++nu) {
+          ph[a].N[nu] = at(6 + nu);
+          ph[a].dVdN[nu] = at(6 + nc + nu);
+        }
+      }
+      int it = cubic_phase_state(*fl, wden, wvis, p[i], T[i], Ni, ph);
+      if (iterations) iterations[i] = it;
+      for (int a = 0; a < 3; ++a) {
+        auto at = [&](int f) -> double& { return phases[((size_t)a * nf + f) * n + i]; };
+        at(0) = ph[a].present ? 1 : 0;
+        at(1) = ph[a].V;
+        at(2) = ph[a].xi;
+        at(3) = ph[a].dVdp;
+        at(4) = ph[a].dVdT;
+        at(5) = ph[a].mu;
+        for (int nu = 0; nu < nc; ++nu) {
+          at(6 + nu) = ph[a].N[nu];
+          at(6 + nc + nu) = ph[a].dVdN[nu];
+        }
+      }
+    }
+  } catch (Failure& f) {
+    put_err(err, errlen, f.what());
+    return f.status;
+  }
+  return 0;
+}
+
 double orc_sim_time(void* h) { return ((Simulator*)h)->time; }
 
 int orc_sim_calculate_dt(void* h, double dt, const rsg_dt_control* c, double* dt_new, rsg_dt_factors* f) {

@@ -67,6 +67,8 @@ def _declare(L):
     L.orc_sim_throughput_factor.restype = d
     L.orc_sim_throughput_factor.argtypes = [vp, P(abi.rsg_dt_control)]
     L.orc_sim_step_to.argtypes = [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_step_to_info), C.c_char_p, i]
+    L.orc_cubic_roots.argtypes = [d, d, d, P(d)]
+    L.orc_cubic_phase_state.argtypes = [P(abi.rsg_cubic_fluid), i, P(d), P(d), P(d), P(d), P(i), C.c_char_p, i]
     L.orc_amg_create.restype = vp
     L.orc_amg_create.argtypes = [i, i, P(C.c_int32), P(C.c_int32), P(d), P(i), C.c_char_p, i]
     L.orc_amg_destroy.argtypes = [vp]
@@ -378,3 +380,26 @@ class AMG:
         if st != 0:
             raise OracleError(st, err.value.decode())
         return x
+
+
+def cubic_roots(a0, a1, a2):
+    """CubicEquation(a0, a1, a2): (smallest, middle, largest) root."""
+    z = np.zeros(3)
+    lib().orc_cubic_roots(a0, a1, a2, abi.dptr(z))
+    return tuple(z)
+
+
+def cubic_phase_state(fluid, p, T, N, phases=None):
+    """CubicEquationOfState.calculatePhaseState per cell; returns (phases,
+    flash iterations) in the rsg_cubic_phase_state layout."""
+    p, T, N = _f64(p), _f64(T), _f64(N)
+    n = len(p)
+    nf = abi.cubic_fields(fluid.nc)
+    ph = np.zeros((3, nf, n)) if phases is None else _f64(phases).copy()
+    its = np.zeros(n, np.int32)
+    err = C.create_string_buffer(512)
+    st = lib().orc_cubic_phase_state(C.byref(fluid), n, abi.dptr(p), abi.dptr(T), abi.dptr(N), abi.dptr(ph),
+                                     its.ctypes.data_as(C.POINTER(C.c_int)), err, 512)
+    if st != 0:
+        raise OracleError(st, err.value.decode())
+    return ph, its

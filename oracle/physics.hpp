@@ -143,4 +143,10 @@ struct Simulator {
   int stepTo(double endTime, const rsg_dt_control& c, double& dt, rsg_step_to_info* info);
 };
 
+// Cubic equation of state (cubic.cpp): CubicEquationOfState.calculatePhaseState
+// for one cell; ph = {water, oil, gas} in/out; returns the flash iterations.
+int cubic_phase_state(const rsg_cubic_fluid& fl, const Function& wden, const Function& wvis, double p, double T,
+                      const double* N, EOSData* ph);
+void cubic_roots_kat(double a0, double a1, double a2, double* z);  // CubicEquation roots, ascending
+
 }  // namespace orc

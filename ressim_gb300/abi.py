@@ -127,6 +127,34 @@ class rsg_runspec(C.Structure):
     ]
 
 
+EOS_PR, EOS_SRK = 0, 1
+
+
+class rsg_cubic_fluid(C.Structure):
+    _fields_ = [
+        ("nc", C.c_int32),
+        ("eos", C.c_int32),
+        ("Tc", C.c_double * MAX_COMPONENTS),
+        ("pc", C.c_double * MAX_COMPONENTS),
+        ("omega", C.c_double * MAX_COMPONENTS),
+        ("Mw", C.c_double * MAX_COMPONENTS),
+        ("Vc", C.c_double * MAX_COMPONENTS),
+        ("shift", C.c_double * MAX_COMPONENTS),
+        ("bic", C.c_double * (MAX_COMPONENTS * MAX_COMPONENTS)),
+        ("flash_criteria", C.c_double),
+        ("flash_tolerance", C.c_double),
+        ("flash_max_iterations", C.c_int32),
+        ("lbc", C.c_double * 5),
+        ("water_density", rsg_function),
+        ("water_viscosity", rsg_function),
+    ]
+
+
+def cubic_fields(nc):
+    """Doubles per phase and cell in the rsg_cubic_phase_state layout."""
+    return 6 + 2 * nc
+
+
 class rsg_dt_control(C.Structure):
     _fields_ = [
         ("lambda_", C.c_double),

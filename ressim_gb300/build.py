@@ -1,9 +1,9 @@
 """Builds libresgpu.so (the CUDA library behind include/rsg.h) in-tree.
 
 Each translation unit is compiled for sm_103a in parallel, then linked.
-Fused multiply-add contraction is disabled (--fmad=false) so that every
-product and sum in the property, MPFA and assembly kernels rounds as the
-Java reference evaluates it.
+Fused multiply-add contraction is disabled (--fmad=false for device code,
+-ffp-contract=off for host code) so that every product and sum in the
+property, MPFA and assembly code rounds as the Java reference evaluates it.
 """
 import concurrent.futures as cf
 import os
@@ -17,7 +17,7 @@ LIB = os.path.join(LIB_DIR, "libresgpu.so")
 SOURCES = ["context.cu", "csr.cu", "precond.cu", "amg.cu", "krylov.cu", "mesh.cu", "sim.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 
 def nvcc():

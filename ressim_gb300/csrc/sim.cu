@@ -818,6 +818,8 @@ __global__ void k_sum_blocks(int64_t n, const double* __restrict__ a, double* pa
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
+#include "cubic.cuh"
+
 }  // namespace
 
 // ----------------------------------------------------------------------
@@ -1533,3 +1535,91 @@ rsg_status rsg_sim_get_residual_volume(rsg_sim* s, double* R, double* dRdp) {
 }
 
 }  // extern "C"
+
+rsg_status rsg_cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
+                                 const double* T, const double* N, double* phases, int32_t* iterations) {
+  if (!ctx || !fluid || n < 0 || (n > 0 && (!p || !T || !N || !phases))) return RSG_BAD_ARG;
+  rsg::Context& c = ctx->c;
+  return guarded(&c, [&] {
+    const rsg_cubic_fluid& f = *fluid;
+    if (f.nc < 2 || f.nc > RSG_MAX_COMPONENTS)
+      throw rsg::Error(RSG_BAD_ARG, "a cubic fluid has 2..RSG_MAX_COMPONENTS components");
+    if (f.eos != RSG_EOS_PR && f.eos != RSG_EOS_SRK) throw rsg::Error(RSG_BAD_ARG, "unknown cubic equation of state");
+    if (f.flash_tolerance <= 0) throw rsg::Error(RSG_BAD_ARG, "FlashTolerance must be positive");
+    if (n >= (1 << 24)) throw rsg::Error(RSG_UNSUPPORTED, "at most 2^24 - 1 cells per call");
+    if (n == 0) return;
+    // EOS constants, ComponentParameters() and HydrocarbonViscosity(), on the
+    // host in the Java operand order
+    rsg::DCubic d{};
+    d.nc = f.nc;
+    d.eos = f.eos;
+    d.maxit = f.flash_max_iterations > 0 ? f.flash_max_iterations : 1000;
+    d.criteria = f.flash_criteria;
+    d.tol = f.flash_tolerance;
+    if (f.eos == RSG_EOS_PR) {
+      d.d1 = -(1 + std::sqrt(2.));
+      d.d2 = -(1 - std::sqrt(2.));
+      d.OmegaA = 0.457235529;
+      d.OmegaB = 0.077796074;
+    } else {
+      d.d1 = -1;
+      d.d2 = 0;
+      d.OmegaA = 0.42748;
+      d.OmegaB = 0.08664;
+    }
+    for (int i = 0; i < f.nc; ++i) {
+      d.Tc[i] = f.Tc[i];
+      d.pc[i] = f.pc[i];
+      d.omega[i] = f.omega[i];
+      d.Mw[i] = f.Mw[i];
+      d.Vc[i] = f.Vc[i];
+      d.s[i] = f.shift[i];
+      for (int j = 0; j < f.nc; ++j) d.dij[i][j] = f.bic[i * RSG_MAX_COMPONENTS + j];
+    }
+    for (int i = 1; i < f.nc; ++i) {
+      const double w = f.omega[i];
+      if (f.eos == RSG_EOS_PR)
+        d.mi[i] = w > 0.49 ? 0.379642 + 1.48503 * w - 0.164423 * w * w + 0.016666 * w * w * w
+                           : 0.37464 + 1.53226 * w - 0.26992 * w * w;
+      else
+        d.mi[i] = 0.48508 + 1.55171 * w - 0.15613 * w * w;
+      d.bi[i] = d.OmegaB * rsg::CUBIC_R * f.Tc[i] / f.pc[i];
+      d.sqrtM[i] = std::sqrt(f.Mw[i]);
+      d.zeta_inv[i] = d.sqrtM[i] * std::pow(f.pc[i], 2. / 3) / std::pow(f.Tc[i], 1. / 6);
+    }
+    for (int k = 0; k < 5; ++k) d.lbc[k] = f.lbc[k];
+    rsg::HostFunc wden, wvis;
+    rsg::upload_func(c, f.water_density, wden);
+    rsg::upload_func(c, f.water_viscosity, wvis);
+    d.wden = wden.d;
+    d.wvis = wvis.d;
+    const int nf = 6 + 2 * f.nc;
+    rsg::DeviceBuffer<double> dp(n), dT(n), dN((size_t)f.nc * n), dph((size_t)3 * nf * n);
+    rsg::DeviceBuffer<int> dit(n), derr(1);
+    auto up = [&](double* dst, const double* src, size_t cnt) {
+      RSG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * cnt, cudaMemcpyHostToDevice, c.stream));
+    };
+    up(dp.get(), p, n);
+    up(dT.get(), T, n);
+    up(dN.get(), N, (size_t)f.nc * n);
+    up(dph.get(), phases, (size_t)3 * nf * n);
+    const int big = INT32_MAX;
+    RSG_CUDA(cudaMemcpyAsync(derr.get(), &big, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    RSG_LAUNCH(c, "cubic_phase_state", rsg::k_cubic_phase_state, rsg::blocks_for(n, 128), 128, 0, d, n, dp.get(),
+               dT.get(), dN.get(), dph.get(), dit.get(), derr.get());
+    RSG_CUDA(cudaMemcpyAsync(phases, dph.get(), sizeof(double) * 3 * nf * n, cudaMemcpyDeviceToHost, c.stream));
+    if (iterations)
+      RSG_CUDA(cudaMemcpyAsync(iterations, dit.get(), sizeof(int) * n, cudaMemcpyDeviceToHost, c.stream));
+    int herr = 0;
+    RSG_CUDA(cudaMemcpyAsync(&herr, derr.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    if (herr != INT32_MAX) {
+      const int code = herr >> 24, cell = herr & ((1 << 24) - 1);
+      static const char* what[] = {"", "Z <= 0", "MatrixSingularException", "Rachford-Rice did not converge",
+                                   "flash did not converge", "negative water density derivative"};
+      const rsg_status st = code == rsg::CUBIC_SINGULAR ? RSG_SINGULAR : RSG_PHYSICS;
+      throw rsg::Error(st, std::string(what[code < 6 ? code : 0]) + " in cell " + std::to_string(cell));
+    }
+  });
+}
+

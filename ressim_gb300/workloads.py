@@ -259,3 +259,60 @@ def ensemble_sizes(count, seed=7, lo=(32, 32, 8), hi=(96, 96, 24)):
     """Grid sizes of an ensemble, each axis uniform in [lo, hi] from a seeded draw."""
     g = np.random.Generator(np.random.PCG64(seed))
     return [tuple(int(g.integers(lo[a], hi[a] + 1)) for a in range(3)) for _ in range(count)]
+
+
+def compositional_fluid(keep, seed=3, nhc=3):
+    """Peng-Robinson fluid of the compositional configuration: water plus
+    `nhc` hydrocarbon pseudo-components (the last standing in for CO2) with
+    Tc ~ U(190, 620) K, pc ~ U(20, 50) bar, omega ~ U(0.01, 0.5) and
+    symmetric binary interaction coefficients ~ U(0, 0.15), all seeded.
+    Molecular weights and critical volumes follow Tc (heavier components are
+    more critical); the water phase uses the same density table as the
+    two-phase case and a 0.5 cP viscosity."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    nc = nhc + 1
+    f = abi.rsg_cubic_fluid()
+    f.nc = nc
+    f.eos = abi.EOS_PR
+    Tc = np.sort(g.uniform(190.0, 620.0, nhc))
+    pc = g.uniform(20.0, 50.0, nhc) * BAR
+    om = g.uniform(0.01, 0.5, nhc)
+    for k in range(nhc):
+        i = k + 1
+        f.Tc[i] = Tc[k]
+        f.pc[i] = pc[k]
+        f.omega[i] = om[k]
+        f.Mw[i] = 0.016 + 0.25 * (Tc[k] - 190.0) / 430.0
+        f.Vc[i] = 1.0e-4 + 5.0e-4 * (Tc[k] - 190.0) / 430.0
+        f.shift[i] = 0.0
+    f.Mw[0] = 0.01801528
+    for i in range(1, nc):
+        for j in range(i + 1, nc):
+            d = g.uniform(0.0, 0.15)
+            f.bic[i * abi.MAX_COMPONENTS + j] = f.bic[j * abi.MAX_COMPONENTS + i] = d
+    f.flash_criteria = 1e4
+    f.flash_tolerance = 1e-1
+    f.flash_max_iterations = 1000
+    for k, v in enumerate((0.1023, 0.023364, 0.058533, -0.040758, 0.0093324)):
+        f.lbc[k] = v
+    ps = np.linspace(20 * BAR, 600 * BAR, 64)
+    Ts = np.array([250.0, 450.0])
+    xiw = np.repeat((1000.0 / 0.01801528 * np.exp(4.0e-5 / BAR * (ps - 200 * BAR)))[:, None], 2, axis=1)
+    f.water_density = abi.table(keep, [ps, Ts], xiw)
+    f.water_viscosity = abi.constant(0.5 * CENTIPOISE, 2)
+    return f
+
+
+def compositional_cells(n, nc, seed=5, p_range=(60 * BAR, 400 * BAR), T_range=(300.0, 400.0)):
+    """Seeded per-cell pressure, temperature and moles (component major) for
+    flash tests: water plus hydrocarbon moles of varying composition, some
+    cells without water and some with one hydrocarbon absent."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    p = g.uniform(*p_range, n)
+    T = g.uniform(*T_range, n)
+    N = g.uniform(0.0, 1000.0, (nc, n))
+    N[0, g.random(n) < 0.3] = 0.0
+    for i in range(n):
+        if g.random() < 0.15:
+            N[1 + g.integers(nc - 1), i] = 0.0
+    return p, T, N

@@ -317,3 +317,30 @@ def test_step_to_adaptive_dt_matches_oracle(ctx):
     assert gf.limit == of.limit
     assert abs(g_new - o_new) <= 1e-7 * o_new
     assert abs(gs.throughput_factor(ctl) - os_.throughput_factor(ctl)) <= 1e-7 * abs(os_.throughput_factor(ctl))
+
+
+def test_cubic_phase_state_matches_oracle(ctx):
+    """Peng-Robinson flash and phase properties per cell against the oracle.
+    CUDA's and the C library's exp/log/pow may differ in the last bit, so
+    values are compared to 1e-9 relative where the flash took the same number
+    of iterations (nearly every cell)."""
+    keep = abi.Keep()
+    f = W.compositional_fluid(keep)
+    nc = f.nc
+    p, T, N = W.compositional_cells(3000, nc)
+    gph, gits = api.cubic_phase_state(ctx, f, p, T, N)
+    oph, oits = O.cubic_phase_state(f, p, T, N)
+    assert np.array_equal(gph[:, 0], oph[:, 0])  # presence of each phase
+    same = gits == oits
+    assert same.mean() >= 0.99
+    scale = np.maximum(np.abs(oph), 1e-300)
+    rel = np.abs(gph - oph) / scale
+    rel[np.abs(oph) < 1e-200] = np.abs(gph - oph)[np.abs(oph) < 1e-200]
+    assert np.max(rel[:, :, same]) <= 1e-9
+    # warm start from the persisted phases
+    gph2, gits2 = api.cubic_phase_state(ctx, f, p, T, N, gph)
+    oph2, oits2 = O.cubic_phase_state(f, p, T, N, oph)
+    same2 = same & (gits2 == oits2)
+    rel2 = np.abs(gph2 - oph2) / np.maximum(np.abs(oph2), 1e-300)
+    rel2[np.abs(oph2) < 1e-200] = 0
+    assert np.max(rel2[:, :, same2]) <= 1e-8
