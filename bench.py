@@ -196,6 +196,8 @@ def run_resgpu(args, rank, world, local_rank):
         res["mixed"] = mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, sim, n, dt, res["ms_per_step"], world)
     if args.ensemble > 0 and rank == 0:
         res["ensemble"] = ensemble_leg(args)
+    if args.flash_cells > 0 and rank == 0:
+        res["flash"] = flash_leg(args)
     return res
 
 
@@ -349,6 +351,43 @@ def ensemble_leg(args):
             "speedup_vs_serial": (units / t_conc) / (units_s / t_ser)}
 
 
+def flash_leg(args):
+    """Per-cell Peng-Robinson phase state with isothermal flash
+    (CubicEquationOfState.calculatePhaseState) on the compositional
+    configuration's size, 256x256x16 = 1,048,576 cells: water plus three
+    seeded hydrocarbon pseudo-components, seeded p in 60-400 bar, T in
+    300-400 K.  Timed through the C ABI with host arrays (copies included):
+    a cold call (Wilson K-values) and a warm call from the returned phases.
+    The oracle (single thread) times the same cold call."""
+    from oracle import oracle as O
+    from ressim_gb300 import api
+
+    keep = abi.Keep()
+    f = W.compositional_fluid(keep)
+    n = args.flash_cells
+    p, T, N = W.compositional_cells(n, f.nc)
+    ctx = api.Context(0)
+    try:
+        api.cubic_phase_state(ctx, f, p[:1024], T[:1024], N[:, :1024])  # load and first-launch costs
+        t0 = time.perf_counter()
+        ph, its = api.cubic_phase_state(ctx, f, p, T, N)
+        t_cold = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ph2, its2 = api.cubic_phase_state(ctx, f, p, T, N, ph)
+        t_warm = time.perf_counter() - t0
+    finally:
+        ctx.close()
+    out = {"cells": n, "unit": "cells/s", "cold_value": n / t_cold, "warm_value": n / t_warm,
+           "mean_flash_iterations_cold": float(its.mean()), "mean_flash_iterations_warm": float(its2.mean()),
+           "two_phase_cells": int(((ph[1, 0] > 0) & (ph[2, 0] > 0)).sum())}
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        O.cubic_phase_state(f, p, T, N)
+        out["cpu_oracle_cold_value"] = n / (time.perf_counter() - t0)
+        out["cpu_cores"] = 1
+    return out
+
+
 def oracle_full(args):
     """The oracle (single-threaded C++ restatement of RS + MTJ) on the full
     workload, set to take one Newton iteration per time step (pressure
@@ -472,6 +511,8 @@ def main():
                     help="steps timed with the mixed-precision pressure solver (0: skip)")
     ap.add_argument("--ensemble", type=int, default=16, help="ensemble members stepped concurrently (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=1)
+    ap.add_argument("--flash-cells", type=int, default=1048576,
+                    help="cells of the Peng-Robinson flash leg (0: skip)")
     ap.add_argument("--inner", type=float, nargs=2, default=[10, 1e-3],
                     help="mixed solver: FP32 inner iterations and inner relative tolerance")
     args = ap.parse_args()
