@@ -376,6 +376,12 @@ typedef struct {
  * iterations per cell.  Host arrays, one thread per cell on the GPU. */
 rsg_status rsg_cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
                                  const double* T, const double* N, double* phases, int32_t* iterations);
+/* The same, with a status per cell (cell_status: n, 0 = OK, else the
+ * rsg_status of that cell's failure); every cell is evaluated and the call
+ * returns RSG_OK unless the arguments or the GPU fail. */
+rsg_status rsg_cubic_phase_state_cells(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
+                                       const double* T, const double* N, double* phases, int32_t* iterations,
+                                       int32_t* cell_status);
 
 /* Ensembles: rsg_sim_step on every member, concurrently.  Each member must
  * own its context (its own stream); members are driven from up to

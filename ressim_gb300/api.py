@@ -116,6 +116,8 @@ def _declare(L):
         "rsg_sim_get_time": (i32, [vp, P(d)]),
         "rsg_ensemble_step": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
         "rsg_cubic_phase_state": (i32, [vp, P(abi.rsg_cubic_fluid), i32, P(d), P(d), P(d), P(d), P(i32)]),
+        "rsg_cubic_phase_state_cells": (i32, [vp, P(abi.rsg_cubic_fluid), i32, P(d), P(d), P(d), P(d), P(i32),
+                                              P(i32)]),
         "rsg_sim_calculate_dt": (i32, [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_dt_factors)]),
         "rsg_sim_throughput_factor": (i32, [vp, P(abi.rsg_dt_control), P(d)]),
         "rsg_sim_step_to": (i32, [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_step_to_info)]),
@@ -579,15 +581,21 @@ def ensemble_step(sims, dts, max_concurrent=0):
     return list(infos), sts
 
 
-def cubic_phase_state(ctx, fluid, p, T, N, phases=None):
+def cubic_phase_state(ctx, fluid, p, T, N, phases=None, per_cell=False):
     """CubicEquationOfState.calculatePhaseState for every cell on the GPU.
     N is (nc, n); phases (3, 6 + 2 nc, n) is in/out (zeros: no previous
-    phases).  Returns (phases, flash iterations per cell)."""
+    phases).  Returns (phases, flash iterations per cell); with per_cell,
+    also the status of each cell instead of raising on the first failure."""
     p, T, N = _f64(p), _f64(T), _f64(N)
     n = len(p)
     nf = abi.cubic_fields(fluid.nc)
     ph = np.zeros((3, nf, n)) if phases is None else _f64(phases).copy()
     its = np.zeros(n, np.int32)
+    if per_cell:
+        sts = np.zeros(n, np.int32)
+        ctx.check(lib().rsg_cubic_phase_state_cells(ctx.h, C.byref(fluid), n, abi.dptr(p), abi.dptr(T), abi.dptr(N),
+                                                    abi.dptr(ph), abi.iptr(its), abi.iptr(sts)), "cubic_phase_state")
+        return ph, its, sts
     ctx.check(lib().rsg_cubic_phase_state(ctx.h, C.byref(fluid), n, abi.dptr(p), abi.dptr(T), abi.dptr(N),
                                           abi.dptr(ph), abi.iptr(its)), "cubic_phase_state")
     return ph, its

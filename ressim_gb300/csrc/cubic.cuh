@@ -607,7 +607,8 @@ __device__ int cubic_phase_state(const DCubic& c, double p, double T, const doub
 __global__ void __launch_bounds__(128) k_cubic_phase_state(DCubic c, int n, const double* __restrict__ p,
                                                            const double* __restrict__ T,
                                                            const double* __restrict__ N, double* __restrict__ phases,
-                                                           int* __restrict__ iters, int* __restrict__ err) {
+                                                           int* __restrict__ iters, int* __restrict__ err,
+                                                           int* __restrict__ cell_status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int nc = c.nc, nf = 6 + 2 * nc;
@@ -632,6 +633,7 @@ __global__ void __launch_bounds__(128) k_cubic_phase_state(DCubic c, int n, cons
   const int e = cubic_phase_state(c, p[i], T[i], Ni, ph, &it);
   iters[i] = it;
   if (e) atomicMin(err, e * (1 << 24) + i);
+  if (cell_status) cell_status[i] = e == CUBIC_OK ? RSG_OK : (e == CUBIC_SINGULAR ? RSG_SINGULAR : RSG_PHYSICS);
   for (int a = 0; a < 3; ++a) {
     double* base = phases + (int64_t)a * nf * n + i;
     base[0] = ph[a].present ? 1 : 0;

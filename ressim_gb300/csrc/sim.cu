@@ -1536,8 +1536,9 @@ rsg_status rsg_sim_get_residual_volume(rsg_sim* s, double* R, double* dRdp) {
 
 }  // extern "C"
 
-rsg_status rsg_cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
-                                 const double* T, const double* N, double* phases, int32_t* iterations) {
+static rsg_status cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
+                                    const double* T, const double* N, double* phases, int32_t* iterations,
+                                    int32_t* cell_status) {
   if (!ctx || !fluid || n < 0 || (n > 0 && (!p || !T || !N || !phases))) return RSG_BAD_ARG;
   rsg::Context& c = ctx->c;
   return guarded(&c, [&] {
@@ -1595,7 +1596,7 @@ rsg_status rsg_cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int
     d.wvis = wvis.d;
     const int nf = 6 + 2 * f.nc;
     rsg::DeviceBuffer<double> dp(n), dT(n), dN((size_t)f.nc * n), dph((size_t)3 * nf * n);
-    rsg::DeviceBuffer<int> dit(n), derr(1);
+    rsg::DeviceBuffer<int> dit(n), derr(1), dst(cell_status ? n : 0);
     auto up = [&](double* dst, const double* src, size_t cnt) {
       RSG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * cnt, cudaMemcpyHostToDevice, c.stream));
     };
@@ -1606,14 +1607,16 @@ rsg_status rsg_cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int
     const int big = INT32_MAX;
     RSG_CUDA(cudaMemcpyAsync(derr.get(), &big, sizeof(int), cudaMemcpyHostToDevice, c.stream));
     RSG_LAUNCH(c, "cubic_phase_state", rsg::k_cubic_phase_state, rsg::blocks_for(n, 128), 128, 0, d, n, dp.get(),
-               dT.get(), dN.get(), dph.get(), dit.get(), derr.get());
+               dT.get(), dN.get(), dph.get(), dit.get(), derr.get(), cell_status ? dst.get() : nullptr);
+    if (cell_status)
+      RSG_CUDA(cudaMemcpyAsync(cell_status, dst.get(), sizeof(int) * n, cudaMemcpyDeviceToHost, c.stream));
     RSG_CUDA(cudaMemcpyAsync(phases, dph.get(), sizeof(double) * 3 * nf * n, cudaMemcpyDeviceToHost, c.stream));
     if (iterations)
       RSG_CUDA(cudaMemcpyAsync(iterations, dit.get(), sizeof(int) * n, cudaMemcpyDeviceToHost, c.stream));
     int herr = 0;
     RSG_CUDA(cudaMemcpyAsync(&herr, derr.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     c.sync();
-    if (herr != INT32_MAX) {
+    if (herr != INT32_MAX && !cell_status) {
       const int code = herr >> 24, cell = herr & ((1 << 24) - 1);
       static const char* what[] = {"", "Z <= 0", "MatrixSingularException", "Rachford-Rice did not converge",
                                    "flash did not converge", "negative water density derivative"};
@@ -1623,3 +1626,14 @@ rsg_status rsg_cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int
   });
 }
 
+rsg_status rsg_cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
+                                 const double* T, const double* N, double* phases, int32_t* iterations) {
+  return cubic_phase_state(ctx, fluid, n, p, T, N, phases, iterations, nullptr);
+}
+
+rsg_status rsg_cubic_phase_state_cells(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
+                                       const double* T, const double* N, double* phases, int32_t* iterations,
+                                       int32_t* cell_status) {
+  if (n > 0 && !cell_status) return RSG_BAD_ARG;
+  return cubic_phase_state(ctx, fluid, n, p, T, N, phases, iterations, cell_status);
+}
