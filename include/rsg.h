@@ -383,6 +383,14 @@ rsg_status rsg_cubic_phase_state_cells(rsg_ctx* ctx, const rsg_cubic_fluid* flui
                                        const double* T, const double* N, double* phases, int32_t* iterations,
                                        int32_t* cell_status);
 
+/* rsg_sim_create with the cubic equation of state as the fluid model
+ * (compositional runs): CV.calculateFluidProperties calls
+ * CubicEquationOfState.calculatePhaseState for every cell. */
+rsg_status rsg_sim_create_cubic(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_cubic_fluid* fluid, const rsg_corey* rf,
+                                const double* porosity, const double* compaction, int32_t nsources,
+                                const rsg_source* sources, const rsg_initial* init, const rsg_runspec* spec,
+                                rsg_sim** out);
+
 /* Ensembles: rsg_sim_step on every member, concurrently.  Each member must
  * own its context (its own stream); members are driven from up to
  * max_concurrent host threads (0: one per member), so their kernels overlap

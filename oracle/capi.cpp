@@ -293,6 +293,42 @@ void* orc_sim_create(void* mesh, const rsg_blackoil* fluid, const rsg_corey* rf,
   }
 }
 
+void* orc_sim_create_cubic(void* mesh, const rsg_cubic_fluid* fluid, const rsg_corey* rf, const double* poro,
+                           const double* cr, int ns, const rsg_source* src, const rsg_initial* init,
+                           const rsg_runspec* spec, int* status, char* err, int errlen) {
+  // the black-oil record carries the component count, molecular weights and
+  // grouping; its functions are not evaluated
+  rsg_blackoil carrier{};
+  carrier.nc = fluid->nc;
+  for (int i = 0; i < fluid->nc && i < RSG_MAX_COMPONENTS; ++i) {
+    carrier.molecular_weight[i] = fluid->Mw[i];
+    carrier.group[i] = i == 0 ? 0 : 1;
+  }
+  rsg_function one{};
+  one.kind = RSG_FN_CONSTANT;
+  one.dim = 3;
+  one.value = 1.0;
+  rsg_function zero = one;
+  zero.value = 0.0;
+  carrier.water_density = fluid->water_density;
+  carrier.water_viscosity = fluid->water_viscosity;
+  carrier.water_enthalpy = zero;
+  carrier.bubble_point = zero;
+  carrier.dew_point = zero;
+  carrier.oil_density = carrier.gas_density = one;
+  carrier.oil_viscosity = carrier.gas_viscosity = one;
+  carrier.oil_enthalpy = carrier.gas_enthalpy = zero;
+  try {
+    auto* s = new Simulator(*(Mesh*)mesh, carrier, *rf, poro, cr, ns, src, *init, *spec, fluid);
+    *status = 0;
+    return s;
+  } catch (Failure& f) {
+    *status = f.status;
+    put_err(err, errlen, f.what());
+    return nullptr;
+  }
+}
+
 void orc_sim_destroy(void* s) { delete (Simulator*)s; }
 
 int orc_sim_step(void* h, double dt, rsg_step_info* info, char* err, int errlen) {

@@ -56,6 +56,9 @@ def _declare(L):
     L.orc_sim_create.argtypes = [vp, P(abi.rsg_blackoil), P(abi.rsg_corey), P(d), P(d), i, P(abi.rsg_source),
                                  P(abi.rsg_initial), P(abi.rsg_runspec), P(i), C.c_char_p, i]
     L.orc_sim_destroy.argtypes = [vp]
+    L.orc_sim_create_cubic.restype = vp
+    L.orc_sim_create_cubic.argtypes = [vp, P(abi.rsg_cubic_fluid), P(abi.rsg_corey), P(d), P(d), i,
+                                       P(abi.rsg_source), P(abi.rsg_initial), P(abi.rsg_runspec), P(i), C.c_char_p, i]
     L.orc_sim_step.argtypes = [vp, d, P(abi.rsg_step_info), C.c_char_p, i]
     L.orc_sim_retract.argtypes = [vp]
     L.orc_sim_state.argtypes = [vp, P(d), P(d), P(d)]
@@ -270,9 +273,9 @@ class Simulator:
         self._keep = (fluid, corey, _f64(porosity), _f64(compaction), sources, init, spec)
         st = C.c_int(0)
         err = C.create_string_buffer(512)
-        self.h = lib().orc_sim_create(mesh.h, C.byref(fluid), C.byref(corey), abi.dptr(self._keep[2]),
-                                      abi.dptr(self._keep[3]), len(sources), sources, C.byref(init), C.byref(spec),
-                                      C.byref(st), err, 512)
+        create = lib().orc_sim_create_cubic if isinstance(fluid, abi.rsg_cubic_fluid) else lib().orc_sim_create
+        self.h = create(mesh.h, C.byref(fluid), C.byref(corey), abi.dptr(self._keep[2]), abi.dptr(self._keep[3]),
+                        len(sources), sources, C.byref(init), C.byref(spec), C.byref(st), err, 512)
         if not self.h:
             raise OracleError(st.value, err.value.decode())
         self.n = mesh.counts()["elements"]

@@ -443,8 +443,14 @@ double Corey::pcgo(const double* S) const {
 // ---------------------------------------------------------- Simulator ----
 Simulator::Simulator(const Mesh& m, const rsg_blackoil& fluid, const rsg_corey& rf, const double* poro,
                      const double* comp, int nsources, const rsg_source* src, const rsg_initial& init,
-                     const rsg_runspec& sp)
+                     const rsg_runspec& sp, const rsg_cubic_fluid* cubicFluid)
     : mesh(&m), eos(fluid), spec(sp) {
+  if (cubicFluid) {
+    useCubic = true;
+    cubic = *cubicFluid;
+    cubicWden = Function(cubic.water_density);
+    cubicWvis = Function(cubic.water_viscosity);
+  }
   rockFluid.c = rf;
   nc = eos.nc;
   const int n = m.numElements();
@@ -503,7 +509,8 @@ void Simulator::cvSecondaries(int i) {
   CVState& s = cv[i];
   const double V = mesh->evolume[i];
   // calculateFluidProperties (:403-441)
-  eos.calculatePhaseState(s.p, s.N, s.T, s.eos);
+  if (useCubic) cubic_phase_state(cubic, cubicWden, cubicWvis, s.p, s.T, s.N, s.eos);
+  else eos.calculatePhaseState(s.p, s.N, s.T, s.eos);
   s.delta = V * heatCap[i];
   for (int ph = 0; ph < 3; ++ph) {
     const EOSData& e = s.eos[ph];

@@ -115,8 +115,14 @@ struct Simulator {
   double time = 0, lastDt = 0;  // Field.t, the last attempted step
   int pressureIterations = 0;   // PressureNewtonRaphson.pressureIterations
 
+  // compositional runs: the cubic equation of state replaces the black-oil one
+  bool useCubic = false;
+  rsg_cubic_fluid cubic{};
+  Function cubicWden, cubicWvis;
+
   Simulator(const Mesh& mesh, const rsg_blackoil& fluid, const rsg_corey& rf, const double* poro, const double* comp,
-            int nsources, const rsg_source* src, const rsg_initial& init, const rsg_runspec& spec);
+            int nsources, const rsg_source* src, const rsg_initial& init, const rsg_runspec& spec,
+            const rsg_cubic_fluid* cubicFluid = nullptr);
 
   double bodyForce(int el) const;
   void cvSecondaries(int i);

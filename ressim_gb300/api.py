@@ -107,6 +107,8 @@ def _declare(L):
         "rsg_sim_create": (i32, [vp, vp, P(abi.rsg_blackoil), P(abi.rsg_corey), P(d), P(d), i32, P(abi.rsg_source),
                                  P(abi.rsg_initial), P(abi.rsg_runspec), PP()]),
         "rsg_sim_destroy": (i32, [vp]),
+        "rsg_sim_create_cubic": (i32, [vp, vp, P(abi.rsg_cubic_fluid), P(abi.rsg_corey), P(d), P(d), i32,
+                                       P(abi.rsg_source), P(abi.rsg_initial), P(abi.rsg_runspec), PP()]),
         "rsg_sim_step": (i32, [vp, d, P(abi.rsg_step_info)]),
         "rsg_sim_retract": (i32, [vp]),
         "rsg_sim_get_state": (i32, [vp, P(d), P(d), P(d)]),
@@ -463,9 +465,9 @@ class Discretisation:
         self.mesh = mesh
         self._keep = (fluid, corey, _f64(porosity), _f64(compaction), sources, init, spec)
         h = C.c_void_p()
-        ctx.check(lib().rsg_sim_create(ctx.h, mesh.h, C.byref(fluid), C.byref(corey), abi.dptr(self._keep[2]),
-                                       abi.dptr(self._keep[3]), len(sources), sources, C.byref(init), C.byref(spec),
-                                       C.byref(h)), "sim_create")
+        create = lib().rsg_sim_create_cubic if isinstance(fluid, abi.rsg_cubic_fluid) else lib().rsg_sim_create
+        ctx.check(create(ctx.h, mesh.h, C.byref(fluid), C.byref(corey), abi.dptr(self._keep[2]), abi.dptr(self._keep[3]),
+                         len(sources), sources, C.byref(init), C.byref(spec), C.byref(h)), "sim_create")
         self.h = h
         ctx.adopt(self)
         self.n = mesh.counts()["elements"]

@@ -191,7 +191,8 @@ __device__ double mole_fraction(const double* N, int nc, int nu) {
 }
 
 // Flags raised by the property chain (first one wins)
-enum { FL_NONE = 0, FL_DRDP = 1, FL_DENSITY = 2, FL_WATER_DERIV = 3, FL_BLACKOIL_CHECK = 4, FL_ENTHALPY = 5, FL_PATTERN = 6 };
+enum { FL_NONE = 0, FL_DRDP = 1, FL_DENSITY = 2, FL_WATER_DERIV = 3, FL_BLACKOIL_CHECK = 4, FL_ENTHALPY = 5, FL_PATTERN = 6,
+       FL_CUBIC = 16 };  // FL_CUBIC + CUBIC_* code
 
 __device__ void blackoil_state(const DFluid& fl, double p, const double* N, double T, Phase* ph, int* flag) {
   const int nc = fl.nc;
@@ -378,8 +379,12 @@ struct CellOut {
   int present;
 };
 
+struct DCubic;
+__device__ int cubic_phase_state(const DCubic& c, double p, double T, const double* Nin, Phase* ph, int* iters);
+
 struct SimDev {
   int n, nc, nconn;
+  const DCubic* cub;  // cubic equation of state (nullptr: black-oil)
   DFluid fl;
   DCorey co;
   const double* phi0;
@@ -422,7 +427,13 @@ __device__ void cv_cell(const SimDev& d, int i, double p, double p0, double T, c
       ph[a].dVdN[nu] = d.phdVdN[((int64_t)nu * 3 + a) * n + i];
     }
   }
-  blackoil_state(d.fl, p, N, T, ph, d.flag);
+  if (d.cub) {
+    int it = 0;
+    const int e = cubic_phase_state(*d.cub, p, T, N, ph, &it);
+    if (e) atomicCAS(d.flag, 0, FL_CUBIC + e);
+  } else {
+    blackoil_state(d.fl, p, N, T, ph, d.flag);
+  }
   const double V = d.vol[i];
   // calculateFluidProperties: rho = kg / V_l for present phases
   double rho[3];
@@ -919,6 +930,8 @@ struct Sim {
   DeviceBuffer<double> dp0;
   rsg_csr A;
   SolverPtr solver;
+  DeviceBuffer<DCubic> cubic;     // compositional fluid (empty: black-oil)
+  HostFunc cubic_w[2];
   double time = 0, last_dt = 0;  // Field.t and the last attempted step
   int last_newton = 0;           // PressureNewtonRaphson.pressureIterations
   DeviceBuffer<unsigned long long> dt_terms;
@@ -932,6 +945,7 @@ struct Sim {
     d.nconn = nconn;
     d.fl = fl;
     d.co = co;
+    d.cub = cubic.size() ? cubic.get() : nullptr;
     d.phi0 = phi0.get();
     d.cr = cr.get();
     d.vol = mesh->evol.get();
@@ -971,6 +985,8 @@ struct Sim {
     RSG_CUDA(cudaMemcpyAsync(&h, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
     if (h == FL_DRDP) throw Error(RSG_PHYSICS, "dR/dp must be positive (check PVT data or datum depth/pressure)");
+    if (h == FL_CUBIC + 2) throw Error(RSG_SINGULAR, "MatrixSingularException in the flash");
+    if (h > FL_CUBIC) throw Error(RSG_PHYSICS, "cubic equation of state failed (code " + std::to_string(h - FL_CUBIC) + ")");
     if (h) throw Error(RSG_PHYSICS, "equation-of-state data check failed (code " + std::to_string(h) + ")");
   }
 
@@ -1196,9 +1212,12 @@ using rsg::guarded;
 
 extern "C" {
 
-rsg_status rsg_sim_create(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_blackoil* fluid, const rsg_corey* rf,
-                          const double* porosity, const double* compaction, int32_t nsources,
-                          const rsg_source* sources, const rsg_initial* init, const rsg_runspec* spec, rsg_sim** out) {
+static rsg::DCubic make_dcubic(rsg::Context& c, const rsg_cubic_fluid& f, rsg::HostFunc* w);
+
+static rsg_status sim_create(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_blackoil* fluid, const rsg_cubic_fluid* cubic,
+                             const rsg_corey* rf, const double* porosity, const double* compaction, int32_t nsources,
+                             const rsg_source* sources, const rsg_initial* init, const rsg_runspec* spec,
+                             rsg_sim** out) {
   if (!ctx || !mesh || !fluid || !rf || !porosity || !compaction || !init || !spec || !out) return RSG_BAD_ARG;
   if (nsources < 0 || (nsources > 0 && !sources)) return RSG_BAD_ARG;
   if (!mesh->m.have_md) return RSG_BAD_ARG;
@@ -1243,6 +1262,12 @@ rsg_status rsg_sim_create(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_blackoil* flui
     DFunc* dst[11] = {&fl.wden, &fl.wvis, &fl.went, &fl.bub, &fl.dew, &fl.oden,
                       &fl.gden, &fl.ovis, &fl.gvis, &fl.oent, &fl.gent};
     for (int q = 0; q < 11; ++q) *dst[q] = S.funcs[q].d;
+    if (cubic) {
+      const DCubic dc = make_dcubic(c, *cubic, S.cubic_w);
+      S.cubic.resize(1);
+      RSG_CUDA(cudaMemcpyAsync(S.cubic.get(), &dc, sizeof(DCubic), cudaMemcpyHostToDevice, c.stream));
+      c.sync();
+    }
     for (int a = 0; a < 3; ++a) {
       S.co.Sr[a] = rf->Sr[a];
       S.co.n[a] = rf->n[a];
@@ -1398,6 +1423,42 @@ rsg_status rsg_sim_create(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_blackoil* flui
   return RSG_OK;
 }
 
+rsg_status rsg_sim_create(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_blackoil* fluid, const rsg_corey* rf,
+                          const double* porosity, const double* compaction, int32_t nsources,
+                          const rsg_source* sources, const rsg_initial* init, const rsg_runspec* spec, rsg_sim** out) {
+  return sim_create(ctx, mesh, fluid, nullptr, rf, porosity, compaction, nsources, sources, init, spec, out);
+}
+
+rsg_status rsg_sim_create_cubic(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_cubic_fluid* fluid, const rsg_corey* rf,
+                                const double* porosity, const double* compaction, int32_t nsources,
+                                const rsg_source* sources, const rsg_initial* init, const rsg_runspec* spec,
+                                rsg_sim** out) {
+  if (!fluid) return RSG_BAD_ARG;
+  // the black-oil record carries what the simulator shares between fluids:
+  // component count, molecular weights, grouping; its functions are unused
+  rsg_blackoil carrier{};
+  carrier.nc = fluid->nc;
+  for (int i = 0; i < fluid->nc && i < RSG_MAX_COMPONENTS; ++i) {
+    carrier.molecular_weight[i] = fluid->Mw[i];
+    carrier.group[i] = i == 0 ? 0 : 1;
+  }
+  rsg_function one{};
+  one.kind = RSG_FN_CONSTANT;
+  one.dim = 3;
+  one.value = 1.0;
+  rsg_function zero = one;
+  zero.value = 0.0;
+  carrier.water_density = fluid->water_density;
+  carrier.water_viscosity = fluid->water_viscosity;
+  carrier.water_enthalpy = zero;
+  carrier.bubble_point = zero;
+  carrier.dew_point = zero;
+  carrier.oil_density = carrier.gas_density = one;
+  carrier.oil_viscosity = carrier.gas_viscosity = one;
+  carrier.oil_enthalpy = carrier.gas_enthalpy = zero;
+  return sim_create(ctx, mesh, &carrier, fluid, rf, porosity, compaction, nsources, sources, init, spec, out);
+}
+
 rsg_status rsg_sim_destroy(rsg_sim* s) {
   if (!s) return RSG_BAD_ARG;
   if (s->s) cudaStreamSynchronize(s->s->ctx->stream);
@@ -1536,6 +1597,58 @@ rsg_status rsg_sim_get_residual_volume(rsg_sim* s, double* R, double* dRdp) {
 
 }  // extern "C"
 
+// EOS constants, ComponentParameters() and HydrocarbonViscosity(), on the host
+// in the Java operand order; the water functions go to the device
+static rsg::DCubic make_dcubic(rsg::Context& c, const rsg_cubic_fluid& f, rsg::HostFunc* w) {
+  if (f.nc < 2 || f.nc > RSG_MAX_COMPONENTS)
+    throw rsg::Error(RSG_BAD_ARG, "a cubic fluid has 2..RSG_MAX_COMPONENTS components");
+  if (f.eos != RSG_EOS_PR && f.eos != RSG_EOS_SRK) throw rsg::Error(RSG_BAD_ARG, "unknown cubic equation of state");
+  if (f.flash_tolerance <= 0) throw rsg::Error(RSG_BAD_ARG, "FlashTolerance must be positive");
+  rsg::DCubic d{};
+  d.nc = f.nc;
+  d.eos = f.eos;
+  d.maxit = f.flash_max_iterations > 0 ? f.flash_max_iterations : 1000;
+  d.criteria = f.flash_criteria;
+  d.tol = f.flash_tolerance;
+  if (f.eos == RSG_EOS_PR) {
+    d.d1 = -(1 + std::sqrt(2.));
+    d.d2 = -(1 - std::sqrt(2.));
+    d.OmegaA = 0.457235529;
+    d.OmegaB = 0.077796074;
+  } else {
+    d.d1 = -1;
+    d.d2 = 0;
+    d.OmegaA = 0.42748;
+    d.OmegaB = 0.08664;
+  }
+  for (int i = 0; i < f.nc; ++i) {
+    d.Tc[i] = f.Tc[i];
+    d.pc[i] = f.pc[i];
+    d.omega[i] = f.omega[i];
+    d.Mw[i] = f.Mw[i];
+    d.Vc[i] = f.Vc[i];
+    d.s[i] = f.shift[i];
+    for (int j = 0; j < f.nc; ++j) d.dij[i][j] = f.bic[i * RSG_MAX_COMPONENTS + j];
+  }
+  for (int i = 1; i < f.nc; ++i) {
+    const double w = f.omega[i];
+    if (f.eos == RSG_EOS_PR)
+      d.mi[i] = w > 0.49 ? 0.379642 + 1.48503 * w - 0.164423 * w * w + 0.016666 * w * w * w
+                         : 0.37464 + 1.53226 * w - 0.26992 * w * w;
+    else
+      d.mi[i] = 0.48508 + 1.55171 * w - 0.15613 * w * w;
+    d.bi[i] = d.OmegaB * rsg::CUBIC_R * f.Tc[i] / f.pc[i];
+    d.sqrtM[i] = std::sqrt(f.Mw[i]);
+    d.zeta_inv[i] = d.sqrtM[i] * std::pow(f.pc[i], 2. / 3) / std::pow(f.Tc[i], 1. / 6);
+  }
+  for (int k = 0; k < 5; ++k) d.lbc[k] = f.lbc[k];
+  rsg::upload_func(c, f.water_density, w[0]);
+  rsg::upload_func(c, f.water_viscosity, w[1]);
+  d.wden = w[0].d;
+  d.wvis = w[1].d;
+  return d;
+}
+
 static rsg_status cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, int32_t n, const double* p,
                                     const double* T, const double* N, double* phases, int32_t* iterations,
                                     int32_t* cell_status) {
@@ -1543,57 +1656,10 @@ static rsg_status cubic_phase_state(rsg_ctx* ctx, const rsg_cubic_fluid* fluid, 
   rsg::Context& c = ctx->c;
   return guarded(&c, [&] {
     const rsg_cubic_fluid& f = *fluid;
-    if (f.nc < 2 || f.nc > RSG_MAX_COMPONENTS)
-      throw rsg::Error(RSG_BAD_ARG, "a cubic fluid has 2..RSG_MAX_COMPONENTS components");
-    if (f.eos != RSG_EOS_PR && f.eos != RSG_EOS_SRK) throw rsg::Error(RSG_BAD_ARG, "unknown cubic equation of state");
-    if (f.flash_tolerance <= 0) throw rsg::Error(RSG_BAD_ARG, "FlashTolerance must be positive");
     if (n >= (1 << 24)) throw rsg::Error(RSG_UNSUPPORTED, "at most 2^24 - 1 cells per call");
+    rsg::HostFunc w[2];
+    rsg::DCubic d = make_dcubic(c, f, w);
     if (n == 0) return;
-    // EOS constants, ComponentParameters() and HydrocarbonViscosity(), on the
-    // host in the Java operand order
-    rsg::DCubic d{};
-    d.nc = f.nc;
-    d.eos = f.eos;
-    d.maxit = f.flash_max_iterations > 0 ? f.flash_max_iterations : 1000;
-    d.criteria = f.flash_criteria;
-    d.tol = f.flash_tolerance;
-    if (f.eos == RSG_EOS_PR) {
-      d.d1 = -(1 + std::sqrt(2.));
-      d.d2 = -(1 - std::sqrt(2.));
-      d.OmegaA = 0.457235529;
-      d.OmegaB = 0.077796074;
-    } else {
-      d.d1 = -1;
-      d.d2 = 0;
-      d.OmegaA = 0.42748;
-      d.OmegaB = 0.08664;
-    }
-    for (int i = 0; i < f.nc; ++i) {
-      d.Tc[i] = f.Tc[i];
-      d.pc[i] = f.pc[i];
-      d.omega[i] = f.omega[i];
-      d.Mw[i] = f.Mw[i];
-      d.Vc[i] = f.Vc[i];
-      d.s[i] = f.shift[i];
-      for (int j = 0; j < f.nc; ++j) d.dij[i][j] = f.bic[i * RSG_MAX_COMPONENTS + j];
-    }
-    for (int i = 1; i < f.nc; ++i) {
-      const double w = f.omega[i];
-      if (f.eos == RSG_EOS_PR)
-        d.mi[i] = w > 0.49 ? 0.379642 + 1.48503 * w - 0.164423 * w * w + 0.016666 * w * w * w
-                           : 0.37464 + 1.53226 * w - 0.26992 * w * w;
-      else
-        d.mi[i] = 0.48508 + 1.55171 * w - 0.15613 * w * w;
-      d.bi[i] = d.OmegaB * rsg::CUBIC_R * f.Tc[i] / f.pc[i];
-      d.sqrtM[i] = std::sqrt(f.Mw[i]);
-      d.zeta_inv[i] = d.sqrtM[i] * std::pow(f.pc[i], 2. / 3) / std::pow(f.Tc[i], 1. / 6);
-    }
-    for (int k = 0; k < 5; ++k) d.lbc[k] = f.lbc[k];
-    rsg::HostFunc wden, wvis;
-    rsg::upload_func(c, f.water_density, wden);
-    rsg::upload_func(c, f.water_viscosity, wvis);
-    d.wden = wden.d;
-    d.wvis = wvis.d;
     const int nf = 6 + 2 * f.nc;
     rsg::DeviceBuffer<double> dp(n), dT(n), dN((size_t)f.nc * n), dph((size_t)3 * nf * n);
     rsg::DeviceBuffer<int> dit(n), derr(1), dst(cell_status ? n : 0);

@@ -316,3 +316,55 @@ def compositional_cells(n, nc, seed=5, p_range=(60 * BAR, 400 * BAR), T_range=(3
         if g.random() < 0.15:
             N[1 + g.integers(nc - 1), i] = 0.0
     return p, T, N
+
+
+def compositional_case(ni, nj, nk, seed=1, perturb=0.1, corr_len=8.0, kz_ratio=0.1, dt=8640.0,
+                       rate_mol_per_s=2.0e-3, fractions=(0.3, 0.4, 0.25, 0.05)):
+    """Compositional line drive on the compositional fluid: the last
+    hydrocarbon (the CO2 stand-in) injected into the column (0, 0) as a
+    Regular source, a Fixed producer column at (ni-1, nj-1); initial moles
+    from the given overall mole fractions (water first) at 200 bar, 350 K."""
+    n = ni * nj * nk
+    nodes = perturbed_nodes(ni, nj, nk, 1.0, 1.0, -1.0, perturb, seed)
+    logk = grf((ni, nj, nk), corr_len, 2.0, 1.0, seed + 1000)
+    kx = _cells_ijk_to_linear(10.0 ** logk) * MILLIDARCY
+    perm = np.zeros((n, 6))
+    perm[:, 0] = kx
+    perm[:, 1] = kx
+    perm[:, 2] = kz_ratio * kx
+    poro = rng(seed + 2000).uniform(0.20, 0.30, n)
+
+    def column(i, j):
+        return np.array([i + j * ni + k * ni * nj for k in range(nk)], dtype=np.int32)
+
+    return dict(dim=3, ni=ni, nj=nj, nk=nk, nodes=nodes, perm=np.ascontiguousarray(perm), porosity=poro,
+                compaction=np.zeros(n), injector=column(0, 0), producer=column(ni - 1, nj - 1),
+                fractions=tuple(fractions), q_inject=rate_mol_per_s, temperature=350.0,
+                datum_pressure=200 * BAR, datum_depth=0.0, dt=dt, seed=seed)
+
+
+def build_compositional_sources(keep, case, nc):
+    srcs = (abi.rsg_source * 2)()
+    arr = keep.i32(case["injector"])
+    srcs[0].type = abi.SOURCE_REGULAR
+    srcs[0].num_elements = len(arr)
+    srcs[0].elements = abi.iptr(arr)
+    srcs[0].q[nc - 1] = case["q_inject"]
+    arr = keep.i32(case["producer"])
+    srcs[1].type = abi.SOURCE_FIXED
+    srcs[1].num_elements = len(arr)
+    srcs[1].elements = abi.iptr(arr)
+    srcs[1].temperature = case["temperature"]
+    for nu in range(nc):
+        srcs[1].fraction[nu] = case["fractions"][nu]
+    return srcs
+
+
+def build_compositional_initial(case, nc):
+    init = abi.rsg_initial()
+    init.datum_depth = case["datum_depth"]
+    init.datum_pressure = case["datum_pressure"]
+    init.temperature = abi.constant(case["temperature"], 1)
+    for nu in range(abi.MAX_COMPONENTS):
+        init.fraction[nu] = abi.constant(case["fractions"][nu] if nu < nc else 0.0, 1)
+    return init

@@ -357,3 +357,31 @@ def test_cubic_phase_state_matches_oracle(ctx):
     rel2 = np.abs(gph2 - oph2) / np.maximum(np.abs(oph2), 1e-300)
     rel2[np.abs(oph2) < 1e-200] = 0
     assert np.max(rel2[:, :, same2]) <= 1e-6
+
+
+def test_compositional_steps_match_oracle(ctx):
+    """Compositional line drive with the Peng-Robinson fluid model in the
+    property chain: steps on the GPU against the oracle (1e-8 relative: the
+    flash's stopping tolerance bounds the agreement), mass balance 1e-12."""
+    keep = abi.Keep()
+    f = W.compositional_fluid(keep)
+    nc = f.nc
+    case = W.compositional_case(12, 12, 4)
+    gm, om = _mpfa_pair(ctx, 3, 12, 12, 4, case["perm"], case["nodes"])
+    srcs = W.build_compositional_sources(keep, case, nc)
+    init = W.build_compositional_initial(case, nc)
+    spec = W.runspec(rtol=1e-12)
+    gs = api.Discretisation(ctx, gm, f, W.corey(), case["porosity"], case["compaction"], srcs, init, spec)
+    os_ = O.Simulator(om, f, W.corey(), case["porosity"], case["compaction"], srcs, init, spec)
+    for a, b in zip(gs.state(), os_.state()):
+        assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)) <= 1e-10
+    for _ in range(3):
+        gi = gs.step(case["dt"])
+        oi = os_.step(case["dt"])
+        assert gi.newton_iterations == oi.newton_iterations
+        assert gi.mass_balance_error <= 1e-12
+        gp, gN, gS = gs.state()
+        op, oN, oS = os_.state()
+        assert np.max(np.abs(gp - op) / np.abs(op)) <= 1e-8
+        assert np.max(np.abs(gS - oS)) <= 1e-8
+        assert np.max(np.abs(gN - oN) / np.maximum(np.abs(oN), 1e-30)) <= 1e-8
