@@ -206,6 +206,8 @@ def run_resgpu(args, rank, world, local_rank):
         leg("ensemble", lambda: ensemble_leg(args))
     if args.flash_cells > 0 and rank == 0:
         leg("flash", lambda: flash_leg(args))
+    if args.comp_steps > 0 and rank == 0:
+        leg("compositional", lambda: compositional_leg(args))
     return res
 
 
@@ -400,6 +402,56 @@ def flash_leg(args):
     return out
 
 
+def compositional_leg(args):
+    """Compositional steps end to end (Peng-Robinson flash in every cell's
+    property evaluation, FP64 BiCGstab + ILU(0) pressure solve, explicit
+    molar update) on a line drive of the compositional fluid, 64x64x16 by
+    default, dt = 2000 s with negative moles truncated; against the oracle
+    on the same grid and steps."""
+    from oracle import oracle as O
+    from ressim_gb300 import api
+
+    ni, nj, nk = args.comp_grid
+    keep = abi.Keep()
+    f = W.compositional_fluid(keep)
+    case = W.compositional_case(ni, nj, nk, dt=2000.0)
+    srcs = W.build_compositional_sources(keep, case, f.nc)
+    init = W.build_compositional_initial(case, f.nc)
+    spec = W.runspec(rtol=args.rtol)
+    spec.truncate_negative_moles = 1  # RunSpec TruncateNegativeMoles: the explicit update overshoots in a few cells
+    ctx = api.Context(0)
+    try:
+        mesh = api.Mesh(ctx, 3, ni, nj, nk, case["perm"], coords=case["nodes"])
+        mesh.compute_mpfa()
+        sim = api.Discretisation(ctx, mesh, f, W.corey(), case["porosity"], case["compaction"], srcs, init, spec)
+        sim.step(case["dt"])  # warm-up
+        ctx.synchronize()
+        newton = 0
+        t0 = time.perf_counter()
+        for _ in range(args.comp_steps):
+            newton += sim.step(case["dt"]).newton_iterations
+        ctx.synchronize()
+        secs = time.perf_counter() - t0
+    finally:
+        ctx.close()
+    n = ni * nj * nk
+    out = {"grid": f"{ni}x{nj}x{nk}", "components": f.nc, "steps": args.comp_steps, "newton_iterations": newton,
+           "dt_s": case["dt"],
+           "value": n * newton / secs, "unit": METRIC}
+    if not args.no_cpu_baseline:
+        om = O.Mesh(3, ni, nj, nk, coords=case["nodes"], perm=case["perm"])
+        om.mpfa()
+        osim = O.Simulator(om, f, W.corey(), case["porosity"], case["compaction"], srcs, init, spec)
+        osim.step(case["dt"])
+        on = 0
+        t0 = time.perf_counter()
+        for _ in range(args.comp_steps):
+            on += osim.step(case["dt"]).newton_iterations
+        out["cpu_oracle_value"] = n * on / (time.perf_counter() - t0)
+        out["cpu_cores"] = 1
+    return out
+
+
 def oracle_full(args):
     """The oracle (single-threaded C++ restatement of RS + MTJ) on the full
     workload, set to take one Newton iteration per time step (pressure
@@ -525,6 +577,8 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=1)
     ap.add_argument("--flash-cells", type=int, default=1048576,
                     help="cells of the Peng-Robinson flash leg (0: skip)")
+    ap.add_argument("--comp-steps", type=int, default=1, help="timed steps of the compositional leg (0: skip)")
+    ap.add_argument("--comp-grid", type=int, nargs=3, default=[64, 64, 16])
     ap.add_argument("--inner", type=float, nargs=2, default=[10, 1e-3],
                     help="mixed solver: FP32 inner iterations and inner relative tolerance")
     args = ap.parse_args()
