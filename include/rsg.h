@@ -222,6 +222,30 @@ rsg_status rsg_mesh_get_pattern(rsg_mesh* m, int32_t which, int32_t* row_ptr, in
  * A(here,k) += t_k, A(there,k) -= t_k (numerics/PotentialCalculator.java:319-333). */
 rsg_status rsg_mesh_assemble_potential(rsg_mesh* m, rsg_csr* A);
 
+/* ------------------------------------------------ discrete adjoint ------ */
+/* No reference counterpart: reverse-mode derivatives of the MPFA-O
+ * transmissibilities (T = C A^-1 B - D of O_MPFA.java:193-239) with respect
+ * to the natural logarithm of each element's permeability tensor (K_e scaled
+ * by exp(theta_e)).  For npairs pairs of connection weights mu_k
+ * (npairs x connections) and element potentials phi_k (npairs x elements),
+ *   dlogk[e] = sum_k sum_c mu_k[c] d(sum_m t_cm phi_k[el_m]) / d theta_e.
+ * Valid after rsg_mesh_compute_mpfa; host arrays. */
+rsg_status rsg_mesh_transmissibility_adjoint(rsg_mesh* m, int32_t npairs, const double* conn_weights,
+                                             const double* cell_potentials, double* dlogk);
+/* Discrete adjoint of the steady potential problem of PotentialCalculator
+ * (numerics/PotentialCalculator.java:319-333): A(theta) p = b with A
+ * assembled by rsg_mesh_assemble_potential and the nfixed rows in fixed
+ * replaced by identity rows (rsg_csr_zero_rows with diagonal 1), p its
+ * solution.  For J(p) with gradient dJdp, solves A^T lambda = dJdp with the
+ * given solver (its preconditioner and monitor), then
+ *   dJ/dtheta_e = -sum_c (lambda~_here - lambda~_there) dF_c/dtheta_e,
+ * lambda~ being lambda with the fixed rows zeroed and F_c = sum_m t_cm p_m
+ * the connection flux.  lambda (may be NULL) receives the adjoint solution,
+ * dJ_dlogk the gradient; info the transposed solve. */
+rsg_status rsg_potential_adjoint(rsg_mesh* m, rsg_solver* solver, rsg_csr* A, int32_t nfixed, const int32_t* fixed,
+                                 const double* p, const double* dJdp, double* lambda, double* dJ_dlogk,
+                                 rsg_solve_info* info);
+
 /* -------------------------------------------- fluid / rock / sources --- */
 enum { RSG_FN_CONSTANT = 0, RSG_FN_TABLE = 1, RSG_FN_EVEN_TABLE = 2 };
 /* util/Function: ConstantValue, LookupTable (1-3D) or EvenLookupTable. */

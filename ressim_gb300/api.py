@@ -104,6 +104,8 @@ def _declare(L):
         "rsg_mesh_get_transmissibilities": (i32, [vp, P(i32), P(i32), P(d)]),
         "rsg_mesh_get_pattern": (i32, [vp, i32, P(i32), P(i32), P(i64)]),
         "rsg_mesh_assemble_potential": (i32, [vp, vp]),
+        "rsg_mesh_transmissibility_adjoint": (i32, [vp, i32, P(d), P(d), P(d)]),
+        "rsg_potential_adjoint": (i32, [vp, vp, vp, i32, P(i32), P(d), P(d), P(d), P(d), P(abi.rsg_solve_info)]),
         "rsg_sim_create": (i32, [vp, vp, P(abi.rsg_blackoil), P(abi.rsg_corey), P(d), P(d), i32, P(abi.rsg_source),
                                  P(abi.rsg_initial), P(abi.rsg_runspec), PP()]),
         "rsg_sim_destroy": (i32, [vp]),
@@ -455,6 +457,33 @@ class Mesh:
 
     def assemble_potential(self, A):
         self.ctx.check(lib().rsg_mesh_assemble_potential(self.h, A.h), "assemble_potential")
+
+    def transmissibility_adjoint(self, conn_weights, cell_potentials):
+        """sum_k sum_c mu_k[c] d(sum_m t_cm phi_k[el_m]) / d log K_e for every element e."""
+        mu = np.ascontiguousarray(np.atleast_2d(_f64(conn_weights)))
+        phi = np.ascontiguousarray(np.atleast_2d(_f64(cell_potentials)))
+        if mu.shape[0] != phi.shape[0]:
+            raise ValueError("one potential vector per weight vector")
+        out = np.zeros(self.counts()["elements"])
+        self.ctx.check(lib().rsg_mesh_transmissibility_adjoint(self.h, mu.shape[0], abi.dptr(mu), abi.dptr(phi),
+                                                               abi.dptr(out)), "transmissibility_adjoint")
+        return out
+
+    def potential_adjoint(self, solver, A, fixed, p, dJdp):
+        """Gradient of J(p) with respect to per-element log-permeability for the
+        steady potential problem A(theta) p = b (fixed rows identity).
+        Returns (dJ/dlogk, lambda); solver.last_info holds the transposed solve."""
+        fixed = np.ascontiguousarray(fixed, dtype=np.int32)
+        n = self.counts()["elements"]
+        p, w = _f64(p), _f64(dJdp)
+        lam = np.zeros(n)
+        grad = np.zeros(n)
+        info = abi.rsg_solve_info()
+        st = lib().rsg_potential_adjoint(self.h, solver.h, A.h, len(fixed), abi.iptr(fixed), abi.dptr(p),
+                                         abi.dptr(w), abi.dptr(lam), abi.dptr(grad), C.byref(info))
+        solver.last_info = info
+        self.ctx.check(st, "potential_adjoint")
+        return grad, lam
 
 
 class Discretisation:

@@ -81,7 +81,39 @@ __global__ void k_zero_rows(int nrows, const int* __restrict__ rows, const int* 
   for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) val[q] = (col[q] == r) ? diagonal : 0.0;
 }
 
+__global__ void k_gather_values(int64_t nnz, const int* __restrict__ src, const double* __restrict__ val,
+                                double* __restrict__ out) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < nnz) out[q] = val[src[q]];
+}
+
 }  // namespace
+
+void CsrTranspose::update(Csr& A) {
+  if (A.h_rowptr != for_rowptr || A.h_col != for_col) {
+    std::vector<int> tptr(A.n + 1, 0), tcol(std::max(A.nnz, 1)), tsrc(std::max(A.nnz, 1));
+    for (int q = 0; q < A.nnz; ++q) tptr[A.h_col[q] + 1]++;
+    for (int c = 0; c < A.n; ++c) tptr[c + 1] += tptr[c];
+    std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+    for (int r = 0; r < A.n; ++r)
+      for (int q = A.h_rowptr[r]; q < A.h_rowptr[r + 1]; ++q) {
+        const int c = A.h_col[q];
+        tcol[fill[c]] = r;  // rows ascend, so each transposed row is sorted
+        tsrc[fill[c]] = q;
+        fill[c]++;
+      }
+    AT.build(A.ctx, A.n, A.nnz, tptr.data(), tcol.data());
+    src.resize(std::max(A.nnz, 1));
+    RSG_CUDA(cudaMemcpyAsync(src.get(), tsrc.data(), sizeof(int) * A.nnz, cudaMemcpyHostToDevice, A.ctx->stream));
+    A.ctx->sync();
+    for_rowptr = A.h_rowptr;
+    for_col = A.h_col;
+  }
+  if (A.nnz)
+    RSG_LAUNCH(*A.ctx, "gather_values", k_gather_values, blocks_for(A.nnz, 256), 256, 0, (int64_t)A.nnz, src.get(),
+               A.val.get(), AT.val.get());
+  AT.sell_dirty = true;
+}
 
 void Csr::build(Context* c, int n_, int nnz_, const int* rp, const int* cl) {
   ctx = c;

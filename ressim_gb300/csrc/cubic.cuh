@@ -483,7 +483,7 @@ __device__ double lbc_viscosity(const DCubic& c, double T, const CComp& N, doubl
 
 // CubicEquationOfState.calculatePhaseState + WaterEquationOfState for one
 // cell; ph = {water, oil, gas} in/out.  Returns a CUBIC_* code.
-__device__ int cubic_phase_state(const DCubic& c, double p, double T, const double* Nin, Phase* ph, int* iters) {
+__device__ __noinline__ int cubic_phase_state(const DCubic& c, double p, double T, const double* Nin, Phase* ph, int* iters) {
   const int nc = c.nc;
   CComp N;
   for (int i = 0; i < NCM; ++i) N.N[i] = i < nc ? Nin[i] : 0;

@@ -914,10 +914,6 @@ void solver_set_inner(Solver& s, int iterations, double rtol) {
 
 }  // namespace rsg
 
-struct rsg_solver {
-  rsg::SolverPtr s;
-};
-
 using rsg::guarded;
 
 extern "C" {

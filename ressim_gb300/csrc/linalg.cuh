@@ -102,6 +102,16 @@ void solver_setup(Solver& s, Csr& A);
 void solver_solve(Solver& s, Csr& A, const double* b, double* x, rsg_solve_info* info);
 void solver_set_inner(Solver& s, int iterations, double rtol);
 
+// Explicit transpose of a CSR matrix with a fixed position map: the pattern
+// of A^T is built on the host once per pattern of A, after which update()
+// gathers A's current values into A^T with one kernel.
+struct CsrTranspose {
+  Csr AT;
+  DeviceBuffer<int> src;  // AT.val[q] = A.val[src[q]]
+  std::vector<int> for_rowptr, for_col;
+  void update(Csr& A);
+};
+
 // Launches of BLAS-1 style kernels shared by the drivers.
 void launch_spmv(Context& ctx, Csr& A, const double* x, double* y, const int* active);
 void launch_spmv_f32(Context& ctx, Csr& A, const float* x, float* y, const int* active);
@@ -110,4 +120,8 @@ void launch_spmv_f32(Context& ctx, Csr& A, const float* x, float* y, const int* 
 
 struct rsg_csr {
   rsg::Csr m;
+};
+
+struct rsg_solver {
+  rsg::SolverPtr s;
 };

@@ -506,6 +506,203 @@ __global__ void __launch_bounds__(128) k_mpfa_point(Grid g, const double* __rest
     }
 }
 
+// ------------------------------------------------------------- adjoint ----
+// LU with partial pivoting in dgetf2's order, keeping the pivots so that the
+// adjoint can solve with both A and A^T of one interaction region.
+__device__ int d_getrf(int n, double* A, int lda, int* ipiv) {
+  for (int j = 0; j < n; ++j) {
+    int jp = j;
+    double amax = fabs(A[j + j * lda]);
+    for (int i = j + 1; i < n; ++i)
+      if (fabs(A[i + j * lda]) > amax) {
+        amax = fabs(A[i + j * lda]);
+        jp = i;
+      }
+    ipiv[j] = jp;
+    if (A[jp + j * lda] == 0.0) return j + 1;
+    if (jp != j)
+      for (int c = 0; c < n; ++c) {
+        double t = A[j + c * lda];
+        A[j + c * lda] = A[jp + c * lda];
+        A[jp + c * lda] = t;
+      }
+    const double rp = 1.0 / A[j + j * lda];
+    for (int i = j + 1; i < n; ++i) A[i + j * lda] *= rp;
+    for (int c = j + 1; c < n; ++c) {
+      const double yv = A[j + c * lda];
+      if (yv != 0.0)
+        for (int i = j + 1; i < n; ++i) A[i + c * lda] -= A[i + j * lda] * yv;
+    }
+  }
+  return 0;
+}
+
+// x = A^{-1} x with P A = L U from d_getrf
+__device__ void d_getrs_n(int n, const double* LU, int lda, const int* ipiv, double* x) {
+  for (int j = 0; j < n; ++j)
+    if (ipiv[j] != j) {
+      double t = x[j];
+      x[j] = x[ipiv[j]];
+      x[ipiv[j]] = t;
+    }
+  for (int k = 0; k < n; ++k)
+    for (int i = k + 1; i < n; ++i) x[i] -= x[k] * LU[i + k * lda];
+  for (int k = n - 1; k >= 0; --k) {
+    x[k] /= LU[k + k * lda];
+    for (int i = 0; i < k; ++i) x[i] -= x[k] * LU[i + k * lda];
+  }
+}
+
+// x = A^{-T} x: A^T = U^T L^T P, so solve U^T, then L^T, then undo the swaps
+__device__ void d_getrs_t(int n, const double* LU, int lda, const int* ipiv, double* x) {
+  for (int k = 0; k < n; ++k) {
+    double s = x[k];
+    for (int i = 0; i < k; ++i) s -= LU[i + k * lda] * x[i];
+    x[k] = s / LU[k + k * lda];
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    double s = x[k];
+    for (int i = k + 1; i < n; ++i) s -= LU[i + k * lda] * x[i];
+    x[k] = s;
+  }
+  for (int j = n - 1; j >= 0; --j)
+    if (ipiv[j] != j) {
+      double t = x[j];
+      x[j] = x[ipiv[j]];
+      x[ipiv[j]] = t;
+    }
+}
+
+// Reverse-mode derivative of the corner-point transmissibilities
+// T = C A^{-1} B - D (O_MPFA.java:193-239) with respect to the logarithm of
+// each element's permeability tensor.  Every local matrix is a sum of element
+// contributions linear in that element's K, so d(.)/d log K_a is element a's
+// own contribution (A_a, B_a, C_a, D_a), and
+//   dT/dlogK_a = C_a X - D_a + C A^{-1} (B_a - A_a X),   X = A^{-1} B.
+// For npairs weight/potential pairs (mu_k per connection, phi_k per element)
+// the kernel forms  G_a = sum_k mu_k^T (dT/dlogK_a) phi_k  without building
+// dT: with y = X phi and nu = A^{-T} C^T mu,
+//   G_a = sum_{faces i of a} (here_i mu_i - nu_i) s_i,
+// s_i being the flux of element a's linear potential through face i.  The
+// result goes to corner slot (di + 2 dj + 4 dk) of element a, one writer per
+// slot, so the per-element sum is deterministic.
+__global__ void __launch_bounds__(128) k_mpfa_adjoint_point(
+    Grid g, const double* __restrict__ pts, const double* __restrict__ perm, const double* __restrict__ ecenter,
+    const double* __restrict__ icenter, const double* __restrict__ inormal, const double* __restrict__ iarea,
+    double continuity, int npairs, const double* __restrict__ mu, const double* __restrict__ phi,
+    double* __restrict__ Gcorner, int* flag) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  PointTopo t;
+  point_topology(g, p, t);
+  const int nc = t.nconn, ne = t.ne;
+  const int per = g.dim == 3 ? 3 : 2;
+  double A[TLD * TLD], C[TLD * TLD], fv[8][3][4];
+  for (int q = 0; q < TLD * TLD; ++q) A[q] = C[q] = 0;
+  const V3 corner = ld3(pts, p);
+  for (int a = 0; a < ne; ++a) {
+    const int el = t.el[a];
+    const int f0 = a * per;
+    const int n = per + 1;
+    double Ab[16], Psi[16];
+    for (int q = 0; q < 16; ++q) Ab[q] = Psi[q] = 0;
+    V3 ec = ld3(ecenter, el);
+    Ab[0] = 1;
+    Ab[0 + 1 * n] = ec.x;
+    Ab[0 + 2 * n] = ec.y;
+    if (n == 4) Ab[0 + 3 * n] = ec.z;
+    for (int i = 0; i < per; ++i) {
+      V3 cp = ld3(icenter, t.face[f0 + i]);
+      if (continuity != 1)
+        cp = {(cp.x - corner.x) * continuity + corner.x, (cp.y - corner.y) * continuity + corner.y,
+              (cp.z - corner.z) * continuity + corner.z};
+      Ab[(i + 1)] = 1;
+      Ab[(i + 1) + 1 * n] = cp.x;
+      Ab[(i + 1) + 2 * n] = cp.y;
+      if (n == 4) Ab[(i + 1) + 3 * n] = cp.z;
+    }
+    for (int i = 0; i < n; ++i) Psi[i + i * n] = 1;
+    if (d_dgesv(n, n, Ab, n, Psi, n) != 0) {
+      atomicCAS(flag, 0, 1);
+      return;
+    }
+    V3 grad[4];
+    for (int i = 0; i < n; ++i) grad[i] = {Psi[1 + i * n], Psi[2 + i * n], n == 4 ? Psi[3 + i * n] : 0.0};
+    const double* K = perm + 6 * (int64_t)el;
+    const double kxx = K[0], kyy = K[1], kzz = K[2], kxy = K[3], kxz = K[4], kyz = K[5];
+    for (int i = 0; i < per; ++i) {
+      V3 v = normal_area(g, t, f0 + i, p, pts, inormal, iarea);
+      V3 Kn = {kxx * v.x + kxy * v.y + kxz * v.z, kxy * v.x + kyy * v.y + kyz * v.z, kxz * v.x + kyz * v.y + kzz * v.z};
+      const int fi = f0 + i;
+      const int is = t.lidx[fi];
+      const bool isHere = t.boundary[fi] ? true : (t.fo[fi] & 1);
+      for (int j = 0; j < per + 1; j++) {
+        const double f = vdot(Kn, grad[j]);
+        fv[a][i][j] = f;
+        if (j == 0) continue;
+        const int js = t.lidx[f0 + j - 1];
+        A[is + js * TLD] += f;
+        if (isHere) C[is + js * TLD] += f;
+      }
+    }
+  }
+  int ipiv[TLD];
+  if (d_getrf(nc, A, TLD, ipiv) != 0) {
+    atomicCAS(flag, 0, 2);
+    return;
+  }
+  double G[8];
+  for (int a = 0; a < ne; ++a) G[a] = 0;
+  for (int k = 0; k < npairs; ++k) {
+    const double* muk = mu + (int64_t)k * g.nconn;
+    const double* phik = phi + (int64_t)k * g.nel;
+    double m[TLD], y[TLD], v[TLD], ph[8];
+    for (int i = 0; i < nc; ++i) m[i] = y[i] = 0;
+    // connection weights on the local rows: the here-side face of each
+    // interior local connection names its connection
+    for (int f = 0; f < t.nf; ++f)
+      if (!t.boundary[f] && (t.fo[f] & 1)) {
+        const int a = t.fel[f];
+        m[t.lidx[f]] = muk[face_connection(g, t.eijk[a][0], t.eijk[a][1], t.eijk[a][2], t.fo[f])];
+      }
+    for (int a = 0; a < ne; ++a) {
+      ph[a] = phik[t.el[a]];
+      for (int i = 0; i < per; ++i) y[t.lidx[a * per + i]] -= fv[a][i][0] * ph[a];  // B phi
+    }
+    d_getrs_n(nc, A, TLD, ipiv, y);
+    for (int j = 0; j < nc; ++j) {
+      double s = 0;
+      for (int i = 0; i < nc; ++i) s += C[i + j * TLD] * m[i];
+      v[j] = s;
+    }
+    d_getrs_t(nc, A, TLD, ipiv, v);
+    for (int a = 0; a < ne; ++a)
+      for (int i = 0; i < per; ++i) {
+        const int fi = a * per + i;
+        const int is = t.lidx[fi];
+        const bool isHere = t.boundary[fi] ? true : (t.fo[fi] & 1);
+        double s = fv[a][i][0] * ph[a];
+        for (int j = 1; j < per + 1; ++j) s += fv[a][i][j] * y[t.lidx[a * per + j - 1]];
+        G[a] += ((isHere ? m[is] : 0.0) - v[is]) * s;
+      }
+  }
+  const int pi = p % g.npi, pj = (p / g.npi) % g.npj, pk = p / (g.npi * g.npj);
+  for (int a = 0; a < ne; ++a) {
+    const int slot = (pi - t.eijk[a][0]) + 2 * (pj - t.eijk[a][1]) + (g.dim == 3 ? 4 * (pk - t.eijk[a][2]) : 0);
+    Gcorner[8 * (int64_t)t.el[a] + slot] = G[a];
+  }
+}
+
+// dJ/dlogK per element: scale * sum of its corner slots (+ out when accumulating)
+__global__ void k_corner_sum(int nel, int ncorner, const double* __restrict__ Gcorner, double scale, int accumulate,
+                             double* __restrict__ out) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  double s = 0;
+  for (int q = 0; q < ncorner; ++q) s += Gcorner[8 * (int64_t)e + q];
+  out[e] = (accumulate ? out[e] : 0.0) + scale * s;
+}
+
 // storeTransmissibilities (O_MPFA.java:88-112) gathered per connection over
 // its corner points in ascending point order, then Connection.check
 // (geometry/Connection.java:80-107).
@@ -718,6 +915,26 @@ static void scan_lengths(const std::vector<int>& len, std::vector<int>& ptr) {
   for (size_t i = 0; i < len.size(); ++i) ptr[i + 1] = ptr[i] + len[i];
 }
 
+void mpfa_adjoint(Mesh& m, int npairs, const double* mu, const double* phi, double scale, bool accumulate,
+                  double* out) {
+  if (!m.have_md) throw Error(RSG_BAD_ARG, "transmissibilities have not been computed");
+  Context& c = *m.ctx;
+  const Grid& g = m.g;
+  DeviceBuffer<double> corner((size_t)g.nel * 8);
+  DeviceBuffer<int> flag(1);
+  RSG_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), c.stream));
+  RSG_CUDA(cudaMemsetAsync(corner.get(), 0, sizeof(double) * g.nel * 8, c.stream));
+  RSG_LAUNCH(c, "mpfa_adjoint_point", k_mpfa_adjoint_point, blocks_for(g.npts, 128), 128, 0, g, m.pts.get(),
+             m.perm.get(), m.ecenter.get(), m.icenter.get(), m.inormal.get(), m.iarea.get(), m.continuity, npairs, mu,
+             phi, corner.get(), flag.get());
+  RSG_LAUNCH(c, "corner_sum", k_corner_sum, blocks_for(g.nel, 128), 128, 0, g.nel, g.dim == 3 ? 8 : 4, corner.get(),
+             scale, accumulate ? 1 : 0, out);
+  int hf = 0;
+  RSG_CUDA(cudaMemcpyAsync(&hf, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  c.sync();
+  if (hf) throw Error(RSG_SINGULAR, "singular interaction region in the transmissibility adjoint");
+}
+
 void Mesh::build_patterns() {
   Context& c = *ctx;
   const int n = g.nel;
@@ -830,6 +1047,7 @@ rsg_status rsg_mesh_compute_mpfa(rsg_mesh* mh, double continuity) {
   return guarded(m.ctx, [&] {
     rsg::Context& c = *m.ctx;
     const rsg::Grid& g = m.g;
+    m.continuity = continuity;
     rsg::DeviceBuffer<double> T((size_t)g.npts * rsg::TSZ);
     rsg::DeviceBuffer<int> flag(1), mdlen(g.nconn), mdel((size_t)g.nconn * m.maxmd);
     rsg::DeviceBuffer<double> mdk((size_t)g.nconn * m.maxmd);

@@ -26,6 +26,7 @@ struct Mesh {
   DeviceBuffer<double> md_k;
   std::vector<int> h_md_ptr, h_md_elem, h_conn;
   bool have_md = false;
+  double continuity = 1.0;           // continuity point used by the last MPFA-O computation
   // pressure pattern (LinearSolver) and potential pattern (PotentialCalculator)
   std::vector<int> h_prow, h_pcol, h_qrow, h_qcol;
   // per MD entry: CSR position in the here row and in the there row of the
@@ -33,6 +34,12 @@ struct Mesh {
   DeviceBuffer<int> md_pos_here, md_pos_there, cell_conn_ptr, cell_conn;
   void build_patterns();
 };
+
+// d(sum_k mu_k^T T phi_k)/d log K per element (scale times the sum over the
+// npairs pairs; mu_k per connection, phi_k per element, all device arrays),
+// written to out or added to it.
+void mpfa_adjoint(Mesh& m, int npairs, const double* mu, const double* phi, double scale, bool accumulate,
+                  double* out);
 
 }  // namespace rsg
 
