@@ -208,7 +208,41 @@ def run_resgpu(args, rank, world, local_rank):
         leg("flash", lambda: flash_leg(args))
     if args.comp_steps > 0 and rank == 0:
         leg("compositional", lambda: compositional_leg(args))
+    if args.adj_steps > 0:
+        leg("adjoint", lambda: adjoint_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world))
     return res
+
+
+def adjoint_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world):
+    """Discrete adjoint on the same grid and physics: a recorded forward run
+    of args.adj_steps steps from the initial state (Newton converged to a
+    largest relative pressure change of 1e-8, so that the pressure equation
+    holds at each step's end), checkpoints every args.adj_every steps,
+    objective = oil moles produced into the producer column; then the
+    backward sweep (recomputing every block but the last from its
+    checkpoint) to dJ/dlog k of every cell.  Device time of both sweeps with
+    CUDA events; the gradient's cost is backward / forward."""
+    from ressim_gb300 import api
+
+    spec = W.runspec(rtol=args.rtol, atol=1e-50, ptol=1e-8, stop_rule=1, max_newton=30)
+    sim = api.Discretisation(ctx, mesh, fluid, co, case["porosity"], case["compaction"], srcs, init, spec)
+    dts = [case["dt"]] * args.adj_steps
+    barrier(world)
+    ctx.synchronize()
+    ctx.timer_record(4)
+    J, finfo = sim.forward(dts, args.adj_every, case["producer"], [0.0, 1.0])
+    ctx.timer_record(5)
+    grad, _, _, binfo = sim.backward(rtol=args.adj_rtol)
+    ctx.timer_record(6)
+    ctx.synchronize()
+    fwd = max_over_ranks(ctx.timer_elapsed_ms(4, 5) / 1e3, world)
+    bwd = max_over_ranks(ctx.timer_elapsed_ms(5, 6) / 1e3, world)
+    return {"grid": f"{args.ni}x{args.nj}x{args.nk}", "parameters": n, "steps": args.adj_steps,
+            "checkpoint_every": args.adj_every, "objective_oil_mol": J, "forward_s": fwd, "backward_s": bwd,
+            "backward_over_forward": bwd / fwd, "newton_iterations": finfo.newton_iterations,
+            "forward_linear_iterations": finfo.linear_iterations, "recomputed_steps": binfo.recomputed_steps,
+            "adjoint_linear_iterations": binfo.adjoint_linear_iterations, "adjoint_rtol": args.adj_rtol,
+            "grad_abs_max": float(np.max(np.abs(grad))), "grad_finite": bool(np.all(np.isfinite(grad)))}
 
 
 def mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, fp64_sim, n, dt, fp64_ms, world):
@@ -579,6 +613,9 @@ def main():
                     help="cells of the Peng-Robinson flash leg (0: skip)")
     ap.add_argument("--comp-steps", type=int, default=1, help="timed steps of the compositional leg (0: skip)")
     ap.add_argument("--comp-grid", type=int, nargs=3, default=[64, 64, 16])
+    ap.add_argument("--adj-steps", type=int, default=4, help="steps of the adjoint leg (0: skip)")
+    ap.add_argument("--adj-every", type=int, default=2, help="adjoint leg: steps per checkpoint")
+    ap.add_argument("--adj-rtol", type=float, default=1e-8, help="adjoint leg: transposed-solve tolerance")
     ap.add_argument("--inner", type=float, nargs=2, default=[10, 1e-3],
                     help="mixed solver: FP32 inner iterations and inner relative tolerance")
     args = ap.parse_args()

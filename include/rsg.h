@@ -337,6 +337,36 @@ rsg_status rsg_sim_destroy(rsg_sim* s);
  * (Field.retract). */
 rsg_status rsg_sim_step(rsg_sim* s, double dt, rsg_step_info* info);
 rsg_status rsg_sim_retract(rsg_sim* s);
+/* Discrete adjoint of a simulator run (Discretisation's sequential pressure
+ * Newton step and explicit molar update, numerics/Discretisation.java:280-919;
+ * black-oil fluids with at most 3 components).  rsg_sim_forward runs nsteps
+ * steps of sizes dt[] from the current state, keeping a state checkpoint
+ * every checkpoint_every steps, and accumulates the objective
+ *   J = sum over steps, over the ncells listed cells and the components of
+ *       cell_weights[j] * component_weights[nu] * dN
+ * (dN: the step's molar change of that cell before locking, so for a Fixed
+ * (locked) producer cell the moles produced into it).  rsg_sim_backward then
+ * sweeps the steps in reverse, recomputing each block of steps from its
+ * checkpoint, solving the transposed exact pressure Jacobian per step with
+ * the simulator's Krylov method and preconditioner to relative tolerance
+ * rtol, and returns dJ/dlog k per element (through the MPFA-O
+ * transmissibilities), optionally dJ/dp and dJ/dN of the initial state.  The
+ * Newton iterations of the forward run are taken as converged (F = 0).  The
+ * simulator is left at the end state of the forward run. */
+typedef struct {
+  int32_t steps;                     /* forward steps */
+  int32_t newton_iterations;         /* forward Newton iterations */
+  int32_t linear_iterations;         /* forward linear iterations */
+  int32_t recomputed_steps;          /* steps re-run from checkpoints */
+  int32_t backward_steps;
+  int32_t adjoint_linear_iterations; /* iterations of the transposed solves */
+  double objective;                  /* J of the forward run */
+} rsg_adjoint_info;
+rsg_status rsg_sim_forward(rsg_sim* s, int32_t nsteps, const double* dt, int32_t checkpoint_every, int32_t ncells,
+                           const int32_t* cells, const double* cell_weights, const double* component_weights,
+                           double* objective, rsg_adjoint_info* info);
+rsg_status rsg_sim_backward(rsg_sim* s, double rtol, double* dJ_dlogk, double* dJ_dp0, double* dJ_dN0,
+                            rsg_adjoint_info* info);
 /* p: n; N: nc*n (component major); S: 3*n (phase major) — any may be NULL */
 rsg_status rsg_sim_get_state(rsg_sim* s, double* p, double* N, double* S);
 rsg_status rsg_sim_set_state(rsg_sim* s, const double* p, const double* N);

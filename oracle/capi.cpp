@@ -393,6 +393,13 @@ int orc_cubic_phase_state(const rsg_cubic_fluid* fl, int n, const double* p, con
 
 double orc_sim_time(void* h) { return ((Simulator*)h)->time; }
 
+// the last step's molar changes before the locks (nc * n)
+int orc_sim_last_dn(void* h, double* dN) {
+  Simulator* s = (Simulator*)h;
+  std::copy(s->dNfull.begin(), s->dNfull.end(), dN);
+  return (int)s->dNfull.size();
+}
+
 int orc_sim_calculate_dt(void* h, double dt, const rsg_dt_control* c, double* dt_new, rsg_dt_factors* f) {
   *dt_new = ((Simulator*)h)->calculateDt(dt, *c, f);
   return 0;

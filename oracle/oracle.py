@@ -66,6 +66,7 @@ def _declare(L):
     L.orc_sim_residual_volume.argtypes = [vp, P(d), P(d)]
     L.orc_sim_time.restype = d
     L.orc_sim_time.argtypes = [vp]
+    L.orc_sim_last_dn.argtypes = [vp, P(d)]
     L.orc_sim_calculate_dt.argtypes = [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_dt_factors)]
     L.orc_sim_throughput_factor.restype = d
     L.orc_sim_throughput_factor.argtypes = [vp, P(abi.rsg_dt_control)]
@@ -296,6 +297,12 @@ class Simulator:
 
     def time(self):
         return lib().orc_sim_time(self.h)
+
+    def last_dn(self):
+        """The last step's molar changes (nc x n) before the locked cells are reset."""
+        out = np.zeros((self.nc, self.n))
+        lib().orc_sim_last_dn(self.h, abi.dptr(out))
+        return out
 
     def calculate_dt(self, dt, ctl):
         out = C.c_double(0)

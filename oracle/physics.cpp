@@ -821,6 +821,7 @@ void Simulator::molarMass(double dt) {
       if (sources[q].type == RSG_SOURCE_REGULAR) s -= dt * sources[q].q[nu] * (double)sourceElements[q].size();
     if (tot > 0) massBalance = std::max(massBalance, std::fabs(s) / tot);
   }
+  dNfull = dN;  // before the locks: moles flowing into locked (Fixed) cells
   for (int l : locked)
     for (int nu = 0; nu < nc; ++nu) dN[(size_t)nu * n + l] = 0;
   for (int i = 0; i < n; ++i)

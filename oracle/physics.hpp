@@ -108,6 +108,7 @@ struct Simulator {
   std::vector<double> p_prev, T_prev, R_prev, N_prev;
   std::vector<double> dp;
   std::vector<double> dN;  // nc * n
+  std::vector<double> dNfull;  // nc * n, the last step's dN before the locks
   // diagnostics of the last assembled system
   Vec lastJ, lastRhs;
   int lastLinearIterations = 0;

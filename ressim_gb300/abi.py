@@ -188,6 +188,18 @@ class rsg_dt_factors(C.Structure):
     ]
 
 
+class rsg_adjoint_info(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int32),
+        ("newton_iterations", C.c_int32),
+        ("linear_iterations", C.c_int32),
+        ("recomputed_steps", C.c_int32),
+        ("backward_steps", C.c_int32),
+        ("adjoint_linear_iterations", C.c_int32),
+        ("objective", C.c_double),
+    ]
+
+
 class rsg_step_to_info(C.Structure):
     _fields_ = [
         ("steps", C.c_int32),

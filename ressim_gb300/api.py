@@ -118,6 +118,8 @@ def _declare(L):
         "rsg_sim_get_jacobian": (i32, [vp, P(d), P(d)]),
         "rsg_sim_get_residual_volume": (i32, [vp, P(d), P(d)]),
         "rsg_sim_get_time": (i32, [vp, P(d)]),
+        "rsg_sim_forward": (i32, [vp, i32, P(d), i32, i32, P(i32), P(d), P(d), P(d), P(abi.rsg_adjoint_info)]),
+        "rsg_sim_backward": (i32, [vp, d, P(d), P(d), P(d), P(abi.rsg_adjoint_info)]),
         "rsg_ensemble_step": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
         "rsg_cubic_phase_state": (i32, [vp, P(abi.rsg_cubic_fluid), i32, P(d), P(d), P(d), P(d), P(i32)]),
         "rsg_cubic_phase_state_cells": (i32, [vp, P(abi.rsg_cubic_fluid), i32, P(d), P(d), P(d), P(d), P(i32),
@@ -551,6 +553,32 @@ class Discretisation:
         if st not in (0, 1, 2, 3, 7, 8, 13):
             self.ctx.check(st, "stepTo")
         return st, d.value, info
+
+    def forward(self, dts, checkpoint_every, cells, component_weights, cell_weights=None):
+        """Recorded forward run for the adjoint: returns (J, rsg_adjoint_info),
+        J = sum over steps, listed cells and components of
+        cell_weight * component_weight * dN (moles into the cell before locking)."""
+        dts = _f64(np.atleast_1d(dts))
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        cw = _f64(np.ones(len(cells)) if cell_weights is None else cell_weights)
+        comp = np.zeros(self.nc)
+        comp[:len(component_weights)] = component_weights
+        J = C.c_double(0)
+        info = abi.rsg_adjoint_info()
+        self.ctx.check(lib().rsg_sim_forward(self.h, len(dts), abi.dptr(dts), checkpoint_every, len(cells),
+                                             abi.iptr(cells), abi.dptr(cw), abi.dptr(comp), C.byref(J),
+                                             C.byref(info)), "forward")
+        return J.value, info
+
+    def backward(self, rtol=1e-12):
+        """Adjoint sweep of the last forward(): (dJ/dlogk, dJ/dp0, dJ/dN0, rsg_adjoint_info)."""
+        grad = np.zeros(self.mesh.counts()["elements"])
+        dp0 = np.zeros(self.n)
+        dN0 = np.zeros((self.nc, self.n))
+        info = abi.rsg_adjoint_info()
+        self.ctx.check(lib().rsg_sim_backward(self.h, rtol, abi.dptr(grad), abi.dptr(dp0), abi.dptr(dN0),
+                                              C.byref(info)), "backward")
+        return grad, dp0, dN0, info
 
     def state(self):
         p = np.zeros(self.n)

@@ -19,6 +19,7 @@
 #include <limits>
 #include <cmath>
 
+#include "dual.cuh"
 #include "mesh.cuh"
 
 namespace rsg {
@@ -58,23 +59,26 @@ __device__ int f_index(const DFunc& f, int d, double x) {
   return begin - 1;
 }
 
-__device__ double f_weight(const DFunc& f, int d, int index, double x) {
+template <class S>
+__device__ S f_weight(const DFunc& f, int d, int index, S x) {
   double mn = f.coord[d][index], mx = f.coord[d][index + 1];
-  if (x <= mn) return 0;
-  if (x >= mx) return 1;
+  if (x <= mn) return S(0);
+  if (x >= mx) return S(1);
   return (x - mn) / (mx - mn);
 }
 
-// LookupTable.evaluate (:217-357); nd = -1 value, else partial derivative
-__device__ double f_eval(const DFunc& f, int nd, const double* x) {
-  if (f.kind == RSG_FN_CONSTANT) return nd < 0 ? f.value : 0.0;
-  if (nd >= 0 && !(x[nd] >= f.coord[nd][0] && x[nd] <= f.coord[nd][f.n[nd] - 1])) return 0;
+// LookupTable.evaluate (:217-357); nd = -1 value, else partial derivative.
+// S is double, or a dual number carrying derivatives through the weights.
+template <class S>
+__device__ S f_eval(const DFunc& f, int nd, const S* x) {
+  if (f.kind == RSG_FN_CONSTANT) return S(nd < 0 ? f.value : 0.0);
+  if (nd >= 0 && !(x[nd] >= f.coord[nd][0] && x[nd] <= f.coord[nd][f.n[nd] - 1])) return S(0);
   const double* D = f.data;
   const int nx = f.n[0], ny = f.n[1];
   if (f.dim == 1) {
-    int xi = f_index(f, 0, x[0]);
-    double xw = f_weight(f, 0, xi, x[0]);
-    double phi1, phi2;
+    int xi = f_index(f, 0, val(x[0]));
+    S xw = f_weight(f, 0, xi, x[0]);
+    S phi1, phi2;
     if (nd == -1) {
       phi1 = 1 - xw;
       phi2 = xw;
@@ -86,9 +90,10 @@ __device__ double f_eval(const DFunc& f, int nd, const double* x) {
     return phi1 * D[xi] + phi2 * D[xi + 1];
   }
   if (f.dim == 2) {
-    int xi = f_index(f, 0, x[0]), yi = f_index(f, 1, x[1]);
-    double xw = f_weight(f, 0, xi, x[0]), yw = f_weight(f, 1, yi, x[1]);
-    double phi1, phi2, phi3, phi4, dl;
+    int xi = f_index(f, 0, val(x[0])), yi = f_index(f, 1, val(x[1]));
+    S xw = f_weight(f, 0, xi, x[0]), yw = f_weight(f, 1, yi, x[1]);
+    S phi1, phi2, phi3, phi4;
+    double dl;
     if (nd == -1) {
       phi1 = (1 - xw) * (1 - yw);
       phi2 = xw * (1 - yw);
@@ -110,9 +115,10 @@ __device__ double f_eval(const DFunc& f, int nd, const double* x) {
     return phi1 * D[xi + yi * nx] + phi2 * D[xi + 1 + yi * nx] + phi3 * D[xi + (yi + 1) * nx] +
            phi4 * D[xi + 1 + (yi + 1) * nx];
   }
-  int xi = f_index(f, 0, x[0]), yi = f_index(f, 1, x[1]), zi = f_index(f, 2, x[2]);
-  double xw = f_weight(f, 0, xi, x[0]), yw = f_weight(f, 1, yi, x[1]), zw = f_weight(f, 2, zi, x[2]);
-  double p1, p2, p3, p4, p5, p6, p7, p8, dl;
+  int xi = f_index(f, 0, val(x[0])), yi = f_index(f, 1, val(x[1])), zi = f_index(f, 2, val(x[2]));
+  S xw = f_weight(f, 0, xi, x[0]), yw = f_weight(f, 1, yi, x[1]), zw = f_weight(f, 2, zi, x[2]);
+  S p1, p2, p3, p4, p5, p6, p7, p8;
+  double dl;
   if (nd == -1) {
     p1 = (1 - xw) * (1 - yw) * (1 - zw);
     p2 = xw * (1 - yw) * (1 - zw);
@@ -172,78 +178,84 @@ struct DCorey {
 };
 
 // Per-phase EOS record (EquationOfStateData)
-struct Phase {
+template <class S>
+struct PhaseT {
   bool present;
-  double V, xi, dVdp, dVdT, h, dhdT, mu;
-  double N[NCM], dVdN[NCM];
+  S V, xi, dVdp, dVdT, h, dhdT, mu;
+  S N[NCM], dVdN[NCM];
 };
+using Phase = PhaseT<double>;
 
-__device__ void phase_clear(Phase& e, int nc) {
+template <class S>
+__device__ void phase_clear(PhaseT<S>& e, int nc) {
   e.present = false;
-  e.V = e.xi = e.dVdp = e.dVdT = e.h = e.dhdT = e.mu = 0;
-  for (int i = 0; i < nc; ++i) e.N[i] = e.dVdN[i] = 0;
+  e.V = e.xi = e.dVdp = e.dVdT = e.h = e.dhdT = e.mu = S(0);
+  for (int i = 0; i < nc; ++i) e.N[i] = e.dVdN[i] = S(0);
 }
 
-__device__ double mole_fraction(const double* N, int nc, int nu) {
-  double NT = 0;
+template <class S>
+__device__ S mole_fraction(const S* N, int nc, int nu) {
+  S NT = 0;
   for (int i = 0; i < nc; ++i) NT += N[i];
-  return NT > 0 ? N[nu] / NT : 0;
+  return NT > 0 ? N[nu] / NT : S(0);
 }
 
 // Flags raised by the property chain (first one wins)
 enum { FL_NONE = 0, FL_DRDP = 1, FL_DENSITY = 2, FL_WATER_DERIV = 3, FL_BLACKOIL_CHECK = 4, FL_ENTHALPY = 5, FL_PATTERN = 6,
        FL_CUBIC = 16 };  // FL_CUBIC + CUBIC_* code
 
-__device__ void blackoil_state(const DFluid& fl, double p, const double* N, double T, Phase* ph, int* flag) {
+// S = double for the simulator; a dual number for the adjoint's local derivatives
+template <class S>
+__device__ void blackoil_state(const DFluid& fl, S p, const S* N, double T, PhaseT<S>* ph, int* flag) {
   const int nc = fl.nc;
-  double pT[2] = {p, T};
+  S pT[2] = {p, S(T)};
   {
-    Phase& w = ph[0];
-    double Nw = N[0];
+    PhaseT<S>& w = ph[0];
+    S Nw = N[0];
     if (Nw > 0) {
       w.present = true;
-      double xiw = f_eval(fl.wden, -1, pT);
-      double Vw = Nw / xiw;
+      S xiw = f_eval(fl.wden, -1, pT);
+      S Vw = Nw / xiw;
       if (xiw <= 0) atomicCAS(flag, 0, FL_DENSITY);
       w.xi = xiw;
       w.V = Vw;
       w.N[0] = Nw;
-      double dxiw_dp = f_eval(fl.wden, 0, pT);
-      double dxiw_dT = f_eval(fl.wden, 1, pT);
+      S dxiw_dp = f_eval(fl.wden, 0, pT);
+      S dxiw_dT = f_eval(fl.wden, 1, pT);
       if (dxiw_dp < 0) atomicCAS(flag, 0, FL_WATER_DERIV);
       w.dVdp = -(Vw / xiw) * dxiw_dp;
       w.dVdT = -(Vw / xiw) * dxiw_dT;
       w.dVdN[0] = 1 / xiw;
-      double hw = f_eval(fl.went, -1, pT);
+      S hw = f_eval(fl.went, -1, pT);
       w.h = hw * xiw;
-      double dhw_dT = f_eval(fl.went, 1, pT);
+      S dhw_dT = f_eval(fl.went, 1, pT);
       w.dhdT = dhw_dT * xiw + hw * dxiw_dT;
       w.mu = f_eval(fl.wvis, -1, pT);
     } else
       phase_clear(w, nc);
   }
-  Phase& oil = ph[1];
-  Phase& gas = ph[2];
-  double No = 0, Ng = 0;
+  PhaseT<S>& oil = ph[1];
+  PhaseT<S>& gas = ph[2];
+  S No = 0, Ng = 0;
   for (int a = 0; a < fl.ngO; ++a) No += N[fl.O[a]];
   for (int a = 0; a < fl.ngG; ++a) Ng += N[fl.G[a]];
-  double NHC = No + Ng;
-  double Nt = 0;
+  S NHC = No + Ng;
+  S Nt = 0;
   for (int i = 0; i < nc; ++i) Nt += N[i];
-  auto inverse_group = [&](double Nop, double Ngp, Phase& e) {
-    double Co = No / Nt, Cg = Ng / Nt;
+  auto inverse_group = [&](S Nop, S Ngp, PhaseT<S>& e) {
+    S Co = No / Nt, Cg = Ng / Nt;
     if (Co > 0)
       for (int a = 0; a < fl.ngO; ++a) e.N[fl.O[a]] = mole_fraction(N, nc, fl.O[a]) * Nop / Co;
     if (Cg > 0)
       for (int a = 0; a < fl.ngG; ++a) e.N[fl.G[a]] = mole_fraction(N, nc, fl.G[a]) * Ngp / Cg;
   };
-  auto enthalpy = [&](double C, double dCdT, double xi, double dxidT, double dxidC, const DFunc& fn, Phase& e) {
-    double x[3] = {p, C, T};
-    double hbar = f_eval(fn, -1, x);
+  auto enthalpy = [&](S C, S dCdT, S xi, S dxidT, S dxidC, const DFunc& fn, PhaseT<S>& e) {
+    S x[3] = {p, C, S(T)};
+    S hbar = f_eval(fn, -1, x);
     if (hbar * xi < 0) atomicCAS(flag, 0, FL_ENTHALPY);
     e.h = hbar * xi;
-    double dhbar_dT = f_eval(fn, 2, x);
-    double dhbar_dC = 0;
+    S dhbar_dT = f_eval(fn, 2, x);
+    S dhbar_dC = 0;
     if (dCdT != 0) dhbar_dC = f_eval(fn, 1, x);
     e.dhdT = (dhbar_dT + dhbar_dC * dCdT) * xi + hbar * (dxidT + dxidC * dCdT);
   };
@@ -252,27 +264,27 @@ __device__ void blackoil_state(const DFluid& fl, double p, const double* N, doub
     phase_clear(gas, nc);
     return;
   }
-  double Cb = 0, Cd = 0;
-  double Zo = No / NHC, Zg = Ng / NHC;
+  S Cb = 0, Cd = 0;
+  S Zo = No / NHC, Zg = Ng / NHC;
   if (Zg <= (Cb = f_eval(fl.bub, -1, pT))) {
     oil.present = true;
     phase_clear(gas, nc);
     inverse_group(No, Ng, oil);
-    double Cgo = Ng / NHC;
-    double x[3] = {p, Cgo, T};
-    double xio = f_eval(fl.oden, -1, x);
-    double Vo = (No + Ng) / xio;
+    S Cgo = Ng / NHC;
+    S x[3] = {p, Cgo, T};
+    S xio = f_eval(fl.oden, -1, x);
+    S Vo = (No + Ng) / xio;
     if (xio <= 0) atomicCAS(flag, 0, FL_DENSITY);
     oil.xi = xio;
     oil.V = Vo;
-    double dxio_dp = f_eval(fl.oden, 0, x), dxio_dC = f_eval(fl.oden, 1, x), dxio_dT = f_eval(fl.oden, 2, x);
-    double dCgo_dNo = -Cgo / NHC;
-    double dCgo_dNg = (1 - Cgo) / NHC;
-    double Vo_xio = Vo / xio;
+    S dxio_dp = f_eval(fl.oden, 0, x), dxio_dC = f_eval(fl.oden, 1, x), dxio_dT = f_eval(fl.oden, 2, x);
+    S dCgo_dNo = -Cgo / NHC;
+    S dCgo_dNg = (1 - Cgo) / NHC;
+    S Vo_xio = Vo / xio;
     oil.dVdp = -Vo_xio * dxio_dp;
     oil.dVdT = -Vo_xio * dxio_dT;
-    double dVodNo = (1 / xio) - Vo_xio * dxio_dC * dCgo_dNo;
-    double dVodNg = (1 / xio) - Vo_xio * dxio_dC * dCgo_dNg;
+    S dVodNo = (1 / xio) - Vo_xio * dxio_dC * dCgo_dNo;
+    S dVodNg = (1 / xio) - Vo_xio * dxio_dC * dCgo_dNg;
     for (int a = 0; a < fl.ngO; ++a) oil.dVdN[fl.O[a]] = dVodNo;
     for (int a = 0; a < fl.ngG; ++a) oil.dVdN[fl.G[a]] = dVodNg;
     enthalpy(1, 0, xio, dxio_dT, dxio_dC, fl.oent, oil);
@@ -281,21 +293,21 @@ __device__ void blackoil_state(const DFluid& fl, double p, const double* N, doub
     phase_clear(oil, nc);
     gas.present = true;
     inverse_group(No, Ng, gas);
-    double Cog = No / NHC;
-    double x[3] = {p, Cog, T};
-    double xig = f_eval(fl.gden, -1, x);
-    double Vg = (No + Ng) / xig;
+    S Cog = No / NHC;
+    S x[3] = {p, Cog, T};
+    S xig = f_eval(fl.gden, -1, x);
+    S Vg = (No + Ng) / xig;
     if (xig <= 0) atomicCAS(flag, 0, FL_DENSITY);
     gas.xi = xig;
     gas.V = Vg;
-    double dxig_dp = f_eval(fl.gden, 0, x), dxig_dC = f_eval(fl.gden, 1, x), dxig_dT = f_eval(fl.gden, 2, x);
-    double dCgo_dNo = -(1 - Cog) / NHC;
-    double dCgo_dNg = -Cog / NHC;
-    double Vg_xig = Vg / xig;
+    S dxig_dp = f_eval(fl.gden, 0, x), dxig_dC = f_eval(fl.gden, 1, x), dxig_dT = f_eval(fl.gden, 2, x);
+    S dCgo_dNo = -(1 - Cog) / NHC;
+    S dCgo_dNg = -Cog / NHC;
+    S Vg_xig = Vg / xig;
     gas.dVdp = -Vg_xig * dxig_dp;
     gas.dVdT = -Vg_xig * dxig_dT;
-    double dVgdNo = (1 / xig) - Vg_xig * dxig_dC * dCgo_dNo;
-    double dVgdNg = (1 / xig) - Vg_xig * dxig_dC * dCgo_dNg;
+    S dVgdNo = (1 / xig) - Vg_xig * dxig_dC * dCgo_dNo;
+    S dVgdNg = (1 / xig) - Vg_xig * dxig_dC * dCgo_dNg;
     for (int a = 0; a < fl.ngO; ++a) gas.dVdN[fl.O[a]] = dVgdNo;
     for (int a = 0; a < fl.ngG; ++a) gas.dVdN[fl.G[a]] = dVgdNg;
     enthalpy(1, 0, xig, dxig_dT, dxig_dC, fl.gent, gas);
@@ -303,39 +315,39 @@ __device__ void blackoil_state(const DFluid& fl, double p, const double* N, doub
   } else {
     oil.present = true;
     gas.present = true;
-    double Cgo = Cb, Cog = Cd;
-    double L = (Cog - Zo) / (Cog - (1 - Cgo));
-    double Noo = L * NHC * (1 - Cgo);
-    double Ngo = L * NHC * Cgo;
-    double Nog = (1 - L) * NHC * Cog;
-    double Ngg = (1 - L) * NHC * (1 - Cog);
+    S Cgo = Cb, Cog = Cd;
+    S L = (Cog - Zo) / (Cog - (1 - Cgo));
+    S Noo = L * NHC * (1 - Cgo);
+    S Ngo = L * NHC * Cgo;
+    S Nog = (1 - L) * NHC * Cog;
+    S Ngg = (1 - L) * NHC * (1 - Cog);
     inverse_group(Noo, Ngo, oil);
     inverse_group(Nog, Ngg, gas);
-    double xo[3] = {p, Cgo, T}, xg[3] = {p, Cog, T};
-    double xio = f_eval(fl.oden, -1, xo);
-    double xig = f_eval(fl.gden, -1, xg);
-    double Vo = (Noo + Ngo) / xio;
-    double Vg = (Nog + Ngg) / xig;
+    S xo[3] = {p, Cgo, T}, xg[3] = {p, Cog, T};
+    S xio = f_eval(fl.oden, -1, xo);
+    S xig = f_eval(fl.gden, -1, xg);
+    S Vo = (Noo + Ngo) / xio;
+    S Vg = (Nog + Ngg) / xig;
     oil.xi = xio;
     gas.xi = xig;
     oil.V = Vo;
     gas.V = Vg;
-    double dCgo_dp = f_eval(fl.bub, 0, pT), dCog_dp = f_eval(fl.dew, 0, pT);
-    double dCgo_dT = f_eval(fl.bub, 1, pT), dCog_dT = f_eval(fl.dew, 1, pT);
-    double dLdp = (1 / (Cog - (1 - Cgo))) * ((1 - L) * dCog_dp - L * (dCgo_dp));
-    double dLdT = (1 / (Cog - (1 - Cgo))) * ((1 - L) * dCog_dT - L * (dCgo_dT));
-    double dLdNo = (1 / (Cog - (1 - Cgo))) * ((Zo - 1) / NHC);
-    double dLdNg = (1 / (Cog - (1 - Cgo))) * (Zo / NHC);
-    double dxio_dp = f_eval(fl.oden, 0, xo), dxio_dC = f_eval(fl.oden, 1, xo), dxio_dT = f_eval(fl.oden, 2, xo);
-    double dxig_dp = f_eval(fl.gden, 0, xg), dxig_dC = f_eval(fl.gden, 1, xg), dxig_dT = f_eval(fl.gden, 2, xg);
-    double dVodp = (Vo / L) * dLdp - (Vo / xio) * (dxio_dp + dxio_dC * dCgo_dp);
-    double dVgdp = -(Vg / (1 - L)) * dLdp - (Vg / xig) * (dxig_dp + dxig_dC * dCog_dp);
-    double dVodT = (Vo / L) * dLdT - (Vo / xio) * (dxio_dT + dxio_dC * dCgo_dT);
-    double dVgdT = -(Vg / (1 - L)) * dLdT - (Vg / xig) * (dxig_dT + dxig_dC * dCog_dT);
-    double dVodNo = (1 / xio) * (dLdNo * NHC + L);
-    double dVodNg = (1 / xio) * (dLdNg * NHC + L);
-    double dVgdNo = (1 / xig) * (-dLdNo * NHC + (1 - L));
-    double dVgdNg = (1 / xig) * (-dLdNg * NHC + (1 - L));
+    S dCgo_dp = f_eval(fl.bub, 0, pT), dCog_dp = f_eval(fl.dew, 0, pT);
+    S dCgo_dT = f_eval(fl.bub, 1, pT), dCog_dT = f_eval(fl.dew, 1, pT);
+    S dLdp = (1 / (Cog - (1 - Cgo))) * ((1 - L) * dCog_dp - L * (dCgo_dp));
+    S dLdT = (1 / (Cog - (1 - Cgo))) * ((1 - L) * dCog_dT - L * (dCgo_dT));
+    S dLdNo = (1 / (Cog - (1 - Cgo))) * ((Zo - 1) / NHC);
+    S dLdNg = (1 / (Cog - (1 - Cgo))) * (Zo / NHC);
+    S dxio_dp = f_eval(fl.oden, 0, xo), dxio_dC = f_eval(fl.oden, 1, xo), dxio_dT = f_eval(fl.oden, 2, xo);
+    S dxig_dp = f_eval(fl.gden, 0, xg), dxig_dC = f_eval(fl.gden, 1, xg), dxig_dT = f_eval(fl.gden, 2, xg);
+    S dVodp = (Vo / L) * dLdp - (Vo / xio) * (dxio_dp + dxio_dC * dCgo_dp);
+    S dVgdp = -(Vg / (1 - L)) * dLdp - (Vg / xig) * (dxig_dp + dxig_dC * dCog_dp);
+    S dVodT = (Vo / L) * dLdT - (Vo / xio) * (dxio_dT + dxio_dC * dCgo_dT);
+    S dVgdT = -(Vg / (1 - L)) * dLdT - (Vg / xig) * (dxig_dT + dxig_dC * dCog_dT);
+    S dVodNo = (1 / xio) * (dLdNo * NHC + L);
+    S dVodNg = (1 / xio) * (dLdNg * NHC + L);
+    S dVgdNo = (1 / xig) * (-dLdNo * NHC + (1 - L));
+    S dVgdNg = (1 / xig) * (-dLdNg * NHC + (1 - L));
     oil.dVdp = dVodp;
     oil.dVdT = dVodT;
     gas.dVdp = dVgdp;
@@ -361,23 +373,20 @@ __device__ void blackoil_state(const DFluid& fl, double p, const double* N, doub
 // Math.pow as HotSpot evaluates it for an exponent of exactly 2 (x * x);
 // other exponents use CUDA's pow (within 2 ulp).
 __device__ __forceinline__ double jpow(double x, double y) { return y == 2.0 ? x * x : pow(x, y); }
+template <int K>
+__device__ __forceinline__ Dual<K> jpow(const Dual<K>& x, double y) {
+  return y == 2.0 ? x * x : dual_pow(x, y);
+}
 
-__device__ double eff_sat(const DCorey& c, int ph, double S) {
-  double Se = S;
+template <class S>
+__device__ S eff_sat(const DCorey& c, int ph, S sat) {
+  S Se = sat;
   Se -= c.Sr[ph];
   double denom = 1;
   for (int q = 0; q < 3; ++q) denom -= c.Sr[q];
   Se /= denom;
   return Se;
 }
-
-// Persistent per-cell phase records: kept across calls the way the Java CV
-// objects keep theirs (entries that a branch does not set keep old values).
-struct CellOut {
-  double S[3], rho[3], lambda[3], Cxi[NCM][3];
-  double R, dRdp, dRdN[NCM], pcow, pcgo, phi;
-  int present;
-};
 
 struct DCubic;
 __device__ int cubic_phase_state(const DCubic& c, double p, double T, const double* Nin, Phase* ph, int* iters);
@@ -414,6 +423,74 @@ struct SimDev {
   int* flag;
 };
 
+// Secondaries of one cell from its phase records: calculateFluidProperties,
+// calculateRockProperties, CoreyRockFluid, calculateResidualVolume and the
+// phase mobilities (field/CV.java:375-550).  S = double in the simulator; a
+// dual number in the adjoint, which reads the same expressions' derivatives.
+template <class S>
+struct CellVals {
+  S sat[3], rho[3], lambda[3], Cxi[NCM][3];
+  S R, dRdp, dRdN[NCM], pcow, pcgo;
+};
+
+template <class S>
+__device__ void cell_eval(const SimDev& d, int i, S p, double p0, const PhaseT<S>* ph, CellVals<S>& o) {
+  const int nc = d.nc;
+  const double V = d.vol[i];
+  // calculateFluidProperties: rho = kg / V_l for present phases
+  for (int a = 0; a < 3; ++a) {
+    if (!ph[a].present) {
+      o.rho[a] = S(0);
+      continue;
+    }
+    S kg = 0;
+    for (int nu = 0; nu < nc; ++nu) kg += d.fl.Mw[nu] * ph[a].N[nu];
+    o.rho[a] = kg / ph[a].V;
+  }
+  // calculateRockProperties
+  const double c = d.cr[i];
+  const S dpp = p - p0;
+  const S phi = d.phi0[i] * (1 + c * dpp + c * c * dpp * dpp / 2);
+  S Vf = 0;
+  for (int a = 0; a < 3; ++a) Vf += ph[a].V;
+  for (int a = 0; a < 3; ++a) o.sat[a] = ph[a].V / Vf;
+  // Corey relative permeability and capillary pressures
+  S kr[3];
+  for (int a = 0; a < 3; ++a) kr[a] = d.co.ke[a] * jpow(eff_sat(d.co, a, o.sat[a]), d.co.n[a]);
+  S pcow = 0, pcgo = 0;
+  {
+    S Sw = eff_sat(d.co, 0, o.sat[0]), So = eff_sat(d.co, 1, o.sat[1]);
+    if (Sw > 0) pcow += d.co.cw / jpow(Sw, d.co.aw);
+    if (So > 0) pcow -= d.co.cow / jpow(So, d.co.aow);
+    S Sg = eff_sat(d.co, 2, o.sat[2]);
+    if (Sg > 0) pcgo += d.co.cg / jpow(Sg, d.co.ag);
+    if (So > 0) pcgo -= d.co.cog / jpow(So, d.co.aog);
+  }
+  o.pcow = pcow;
+  o.pcgo = pcgo;
+  // calculateResidualVolume
+  S Vp = phi * V;
+  S R = Vp;
+  S dRdp = c * Vp;
+  S dRdN[NCM];
+  for (int nu = 0; nu < nc; ++nu) dRdN[nu] = S(0);
+  for (int a = 0; a < 3; ++a) {
+    R -= ph[a].V;
+    dRdp -= ph[a].dVdp;
+    for (int nu = 0; nu < nc; ++nu) dRdN[nu] -= ph[a].dVdN[nu];
+  }
+  o.R = R;
+  o.dRdp = dRdp;
+  for (int nu = 0; nu < nc; ++nu) o.dRdN[nu] = dRdN[nu];
+  // mobilities and phase-component molar densities
+  for (int a = 0; a < 3; ++a) {
+    S lam = 0;
+    if (ph[a].mu != 0) lam = kr[a] / ph[a].mu;
+    o.lambda[a] = lam;
+    for (int nu = 0; nu < nc; ++nu) o.Cxi[nu][a] = mole_fraction(ph[a].N, nc, nu) * ph[a].xi;
+  }
+}
+
 // CV.calculateSecondaries on one cell; reads p, p0, T, N and the persisted
 // phase records, writes all secondaries.
 __device__ void cv_cell(const SimDev& d, int i, double p, double p0, double T, const double* N) {
@@ -434,72 +511,28 @@ __device__ void cv_cell(const SimDev& d, int i, double p, double p0, double T, c
   } else {
     blackoil_state(d.fl, p, N, T, ph, d.flag);
   }
-  const double V = d.vol[i];
-  // calculateFluidProperties: rho = kg / V_l for present phases
-  double rho[3];
-  for (int a = 0; a < 3; ++a) {
-    if (!ph[a].present) {
-      rho[a] = 0;
-      continue;
-    }
-    double kg = 0;
-    for (int nu = 0; nu < nc; ++nu) kg += d.fl.Mw[nu] * ph[a].N[nu];
-    rho[a] = kg / ph[a].V;
-  }
-  // calculateRockProperties
-  const double c = d.cr[i];
-  const double dpp = p - p0;
-  const double phi = d.phi0[i] * (1 + c * dpp + c * c * dpp * dpp / 2);
-  double Vf = 0;
-  for (int a = 0; a < 3; ++a) Vf += ph[a].V;
-  double S[3];
-  for (int a = 0; a < 3; ++a) S[a] = ph[a].V / Vf;
-  // Corey relative permeability and capillary pressures
-  double kr[3];
-  for (int a = 0; a < 3; ++a) kr[a] = d.co.ke[a] * jpow(eff_sat(d.co, a, S[a]), d.co.n[a]);
-  double pcow = 0, pcgo = 0;
-  {
-    double Sw = eff_sat(d.co, 0, S[0]), So = eff_sat(d.co, 1, S[1]);
-    if (Sw > 0) pcow += d.co.cw / jpow(Sw, d.co.aw);
-    if (So > 0) pcow -= d.co.cow / jpow(So, d.co.aow);
-    double Sg = eff_sat(d.co, 2, S[2]);
-    if (Sg > 0) pcgo += d.co.cg / jpow(Sg, d.co.ag);
-    if (So > 0) pcgo -= d.co.cog / jpow(So, d.co.aog);
-  }
-  // calculateResidualVolume
-  double Vp = phi * V;
-  double R = Vp;
-  double dRdp = c * Vp;
-  double dRdN[NCM];
-  for (int nu = 0; nu < nc; ++nu) dRdN[nu] = 0;
-  for (int a = 0; a < 3; ++a) {
-    R -= ph[a].V;
-    dRdp -= ph[a].dVdp;
-    for (int nu = 0; nu < nc; ++nu) dRdN[nu] -= ph[a].dVdN[nu];
-  }
-  if (dRdp <= 0) atomicCAS(d.flag, 0, FL_DRDP);
-  // mobilities
+  CellVals<double> o;
+  cell_eval(d, i, p, p0, ph, o);
+  if (o.dRdp <= 0) atomicCAS(d.flag, 0, FL_DRDP);
   int mask = 0;
   for (int a = 0; a < 3; ++a) {
-    double lam = 0;
-    if (ph[a].mu != 0) lam = kr[a] / ph[a].mu;
-    d.S[(int64_t)a * n + i] = S[a];
-    d.rho[(int64_t)a * n + i] = rho[a];
-    d.lambda[(int64_t)a * n + i] = lam;
+    d.S[(int64_t)a * n + i] = o.sat[a];
+    d.rho[(int64_t)a * n + i] = o.rho[a];
+    d.lambda[(int64_t)a * n + i] = o.lambda[a];
     d.xi[(int64_t)a * n + i] = ph[a].xi;
     for (int nu = 0; nu < nc; ++nu) {
-      d.Cxi[((int64_t)nu * 3 + a) * n + i] = mole_fraction(ph[a].N, nc, nu) * ph[a].xi;
+      d.Cxi[((int64_t)nu * 3 + a) * n + i] = o.Cxi[nu][a];
       d.phN[((int64_t)nu * 3 + a) * n + i] = ph[a].N[nu];
       d.phdVdN[((int64_t)nu * 3 + a) * n + i] = ph[a].dVdN[nu];
     }
     if (ph[a].present) mask |= 1 << a;
   }
   d.present[i] = mask;
-  d.R[i] = R;
-  d.dRdp[i] = dRdp;
-  for (int nu = 0; nu < nc; ++nu) d.dRdN[(int64_t)nu * n + i] = dRdN[nu];
-  d.pcow[i] = pcow;
-  d.pcgo[i] = pcgo;
+  d.R[i] = o.R;
+  d.dRdp[i] = o.dRdp;
+  for (int nu = 0; nu < nc; ++nu) d.dRdN[(int64_t)nu * n + i] = o.dRdN[nu];
+  d.pcow[i] = o.pcow;
+  d.pcgo[i] = o.pcgo;
 }
 
 __global__ void k_cv(SimDev d) {
@@ -830,6 +863,326 @@ __global__ void k_sum_blocks(int64_t n, const double* __restrict__ a, double* pa
 }
 
 #include "cubic.cuh"
+
+// ------------------------------------------------------------ adjoint ----
+// Reverse-mode sensitivities of the sequential pressure / explicit-moles step
+// with respect to per-element log-permeability (no reference counterpart).
+// Per step n, with x_e = (p_e, N_e,0..N_e,nc-1) evaluated at (p^{n+1}, N^n):
+//   F_e = sum_nu dRdN_e,nu Q_e,nu + (R(p^n, N^n)_e + dRdp_e (p^{n+1}_e - p^n_e)) / dt
+//   Q_e,nu = sum_c s_ec cf_c,nu + q_e,nu     (net molar inflow, s = -1 here, +1 there)
+//   cf_c,nu = sum_a [present] Cxi_up,nu,a lambda_up,a D_c,a,
+//   D_c,a = sum_m t_cm (p_m + pc_m,a + rho_cs,a bf_m)
+// (Discretisation.java:365-561 and 769-919).  The pressure step solves F = 0
+// (locked rows: p = p^n), and N^{n+1} = N^n + dt Q off the locked cells.
+// Local derivatives of every cell quantity come from the dual-number
+// evaluation of the same property chain; connection terms are
+// differentiated by hand below.
+constexpr int ADJ_NC = 3;          // components the adjoint supports
+constexpr int ADJ_K = 1 + ADJ_NC;  // unknowns per cell: p and the moles
+using AD = Dual<ADJ_K>;
+
+// derivative records: quantity q, unknown k of cell i at rec[(q * K + k) * n + i]
+enum { Q_SAT = 0, Q_RHO = 3, Q_LAM = 6, Q_PCOW = 9, Q_PCGO = 10, Q_R = 11, Q_DRDP = 12, Q_DRDN = 13 };
+__host__ __device__ inline int q_cxi(int nc, int nu, int a) { return Q_DRDN + nc + nu * 3 + a; }
+__host__ __device__ inline int adj_nq(int nc) { return Q_DRDN + 4 * nc; }
+
+struct Rec {
+  const double* r;
+  int n, K;
+  __device__ double operator()(int q, int k, int i) const { return r[((int64_t)q * K + k) * n + i]; }
+};
+
+// Dual-number evaluation of the property chain of every cell at (p, N); the
+// persisted phase records enter as constants as they do in cv_cell.
+__global__ void __launch_bounds__(128) k_cell_dual(SimDev d, const double* __restrict__ pv,
+                                                   const double* __restrict__ Nv, double* __restrict__ rec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const int nc = d.nc, n = d.n, K = 1 + nc;
+  PhaseT<AD> ph[3];
+  for (int a = 0; a < 3; ++a) {
+    ph[a].present = (d.present[i] >> a) & 1;
+    ph[a].V = ph[a].xi = ph[a].dVdp = ph[a].dVdT = ph[a].h = ph[a].dhdT = ph[a].mu = AD(0);
+    for (int nu = 0; nu < nc; ++nu) {
+      ph[a].N[nu] = AD(d.phN[((int64_t)nu * 3 + a) * n + i]);
+      ph[a].dVdN[nu] = AD(d.phdVdN[((int64_t)nu * 3 + a) * n + i]);
+    }
+  }
+  AD p = AD::var(pv[i], 0);
+  AD N[NCM];
+  for (int nu = 0; nu < nc; ++nu) N[nu] = AD::var(Nv[(int64_t)nu * n + i], 1 + nu);
+  blackoil_state(d.fl, p, N, d.T[i], ph, d.flag);
+  CellVals<AD> o;
+  cell_eval(d, i, p, d.p0[i], ph, o);
+  auto put = [&](int q, const AD& x) {
+    for (int k = 0; k < K; ++k) rec[((int64_t)q * K + k) * n + i] = x.d[k];
+  };
+  for (int a = 0; a < 3; ++a) {
+    put(Q_SAT + a, o.sat[a]);
+    put(Q_RHO + a, o.rho[a]);
+    put(Q_LAM + a, o.lambda[a]);
+    for (int nu = 0; nu < nc; ++nu) put(q_cxi(nc, nu, a), o.Cxi[nu][a]);
+  }
+  put(Q_PCOW, o.pcow);
+  put(Q_PCGO, o.pcgo);
+  put(Q_R, o.R);
+  put(Q_DRDP, o.dRdp);
+  for (int nu = 0; nu < nc; ++nu) put(Q_DRDN + nu, o.dRdN[nu]);
+}
+
+// d(phase pressure of phase a at cell e)/dx_k
+__device__ __forceinline__ double dpp_dx(const Rec& r, int e, int a, int k) {
+  const double dp = k == 0 ? 1.0 : 0.0;
+  return a == 0 ? dp - r(Q_PCOW, k, e) : (a == 1 ? dp : dp + r(Q_PCGO, k, e));
+}
+
+struct AdjConn {
+  const int* md_ptr;
+  const int* md_el;
+  const double* md_k;
+  const int* conn;
+  const double* rho_cs;
+  const int* up;
+};
+
+// Derivatives of w . cf_c for one connection, w a weight per component:
+// fills, per MD entry m of c and unknown k, the derivative with respect to
+// x_k of cell el_m (to the slots of the here / there cells also go the
+// density-average and upwind terms), and the theta-pair weights
+// mu_a = [present] lambda_up,a sum_nu w_nu Cxi_up,nu,a  and
+// mu_3 = sum_a mu_a rho_cs,a (potentials p + pc_a and bf).
+__device__ void conn_vjp(const SimDev& d, const AdjConn& c, const Rec& r, int q, const double* w, int kmax,
+                         double (*out)[ADJ_K], double* mu) {
+  const int n = d.n, nc = d.nc, ncn = d.nconn;
+  const int h = c.conn[2 * q], t = c.conn[2 * q + 1];
+  const int m0 = c.md_ptr[q], m1 = c.md_ptr[q + 1];
+  for (int m = 0; m < m1 - m0; ++m)
+    for (int k = 0; k < kmax; ++k) out[m][k] = 0;
+  int mh = -1, mt = -1;
+  double B = 0;
+  for (int m = m0; m < m1; ++m) {
+    const int e = c.md_el[m];
+    if (e == h) mh = m - m0;
+    if (e == t) mt = m - m0;
+    B += c.md_k[m] * d.bf[e];
+  }
+  double mu3 = 0;
+  for (int a = 0; a < 3; ++a) {
+    const int up = c.up[(int64_t)a * ncn + q];
+    const bool pres = (d.present[up] >> a) & 1;
+    const double rcs = c.rho_cs[(int64_t)a * ncn + q];
+    const double lam = d.lambda[(int64_t)a * n + up];
+    double Mc = 0;
+    if (pres)
+      for (int nu = 0; nu < nc; ++nu) Mc += w[nu] * d.Cxi[((int64_t)nu * 3 + a) * n + up];
+    Mc *= pres ? lam : 0.0;
+    mu[a] = Mc;
+    mu3 += Mc * rcs;
+    if (!pres) continue;
+    // D_c,a and the phase-pressure terms
+    double D = 0;
+    for (int m = m0; m < m1; ++m) {
+      const int e = c.md_el[m];
+      const double pp = a == 0 ? d.p[e] - d.pcow[e] : (a == 1 ? d.p[e] : d.p[e] + d.pcgo[e]);
+      D += c.md_k[m] * (pp + rcs * d.bf[e]);
+      for (int k = 0; k < kmax; ++k) out[m - m0][k] += Mc * c.md_k[m] * dpp_dx(r, e, a, k);
+    }
+    // upwind cell: d(Cxi lambda)/dx
+    const int mu_slot = up == h ? mh : mt;
+    if (mu_slot >= 0)
+      for (int k = 0; k < kmax; ++k) {
+        double s = 0;
+        for (int nu = 0; nu < nc; ++nu)
+          s += w[nu] * (r(q_cxi(nc, nu, a), k, up) * lam + d.Cxi[((int64_t)nu * 3 + a) * n + up] * r(Q_LAM + a, k, up));
+        out[mu_slot][k] += D * s;
+      }
+    // density average: d rho_cs / dx_h and dx_t
+    const double Sh = d.S[(int64_t)a * n + h], St = d.S[(int64_t)a * n + t];
+    const double Ssum = Sh + St;
+    if (Ssum != 0 && !isnan(rcs) && Mc * B != 0) {
+      const double rh = d.rho[(int64_t)a * n + h], rt = d.rho[(int64_t)a * n + t];
+      for (int k = 0; k < kmax; ++k) {
+        const double gh = (r(Q_SAT + a, k, h) * (rh - rcs) + Sh * r(Q_RHO + a, k, h)) / Ssum;
+        const double gt = (r(Q_SAT + a, k, t) * (rt - rcs) + St * r(Q_RHO + a, k, t)) / Ssum;
+        if (mh >= 0) out[mh][k] += Mc * B * gh;
+        if (mt >= 0) out[mt][k] += Mc * B * gt;
+      }
+    }
+  }
+  mu[3] = mu3;
+}
+
+constexpr int ADJ_MAXMD = 32;
+
+// Exact pressure Jacobian of the connection terms: rows here (weights
+// -dRdN_here) and there (+dRdN_there), columns the MD cells.
+__global__ void __launch_bounds__(128) k_adj_conn_jac(SimDev d, AdjConn c, Rec r, double* __restrict__ Jh,
+                                                      double* __restrict__ Jt, int* flag) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.nconn) return;
+  const int n = d.n, nc = d.nc;
+  const int h = c.conn[2 * q], t = c.conn[2 * q + 1];
+  const int m0 = c.md_ptr[q], m1 = c.md_ptr[q + 1];
+  if (m1 - m0 > ADJ_MAXMD) {
+    atomicCAS(flag, 0, 1);
+    return;
+  }
+  double out[ADJ_MAXMD][ADJ_K], mu[4], w[NCM];
+  for (int nu = 0; nu < nc; ++nu) w[nu] = -d.dRdN[(int64_t)nu * n + h];
+  conn_vjp(d, c, r, q, w, 1, out, mu);
+  for (int m = m0; m < m1; ++m) Jh[m] = out[m - m0][0];
+  for (int nu = 0; nu < nc; ++nu) w[nu] = d.dRdN[(int64_t)nu * n + t];
+  conn_vjp(d, c, r, q, w, 1, out, mu);
+  for (int m = m0; m < m1; ++m) Jt[m] = out[m - m0][0];
+}
+
+// Vector-Jacobian product of sum_e z_e . Q_e for weights z (nc x n): per MD
+// entry the K derivatives (cmd, entry-major) and the theta-pair weights.
+__global__ void __launch_bounds__(128) k_adj_conn_vjp(SimDev d, AdjConn c, Rec r, const double* __restrict__ z,
+                                                      double* __restrict__ cmd, double* __restrict__ mu, int* flag) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.nconn) return;
+  const int n = d.n, nc = d.nc, K = 1 + nc, ncn = d.nconn;
+  const int h = c.conn[2 * q], t = c.conn[2 * q + 1];
+  const int m0 = c.md_ptr[q], m1 = c.md_ptr[q + 1];
+  if (m1 - m0 > ADJ_MAXMD) {
+    atomicCAS(flag, 0, 1);
+    return;
+  }
+  double out[ADJ_MAXMD][ADJ_K], mq[4], w[NCM];
+  for (int nu = 0; nu < nc; ++nu) w[nu] = z[(int64_t)nu * n + t] - z[(int64_t)nu * n + h];
+  conn_vjp(d, c, r, q, w, K, out, mq);
+  for (int m = m0; m < m1; ++m)
+    for (int k = 0; k < K; ++k) cmd[(int64_t)m * K + k] = out[m - m0][k];
+  for (int a = 0; a < 4; ++a) mu[(int64_t)a * ncn + q] = mq[a];
+}
+
+// Per cell: the sum of its MD-entry derivatives (ascending entry order).
+__global__ void k_adj_gather(int n, int K, const int* __restrict__ inv_ptr, const int* __restrict__ inv_q,
+                             const double* __restrict__ cmd, double* __restrict__ g) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double s[ADJ_K];
+  for (int k = 0; k < K; ++k) s[k] = 0;
+  for (int j = inv_ptr[e]; j < inv_ptr[e + 1]; ++j) {
+    const int64_t m = inv_q[j];
+    for (int k = 0; k < K; ++k) s[k] += cmd[m * K + k];
+  }
+  for (int k = 0; k < K; ++k) g[(int64_t)k * n + e] = s[k];
+}
+
+// Net molar inflow Q (no dt) in the order k_molar_cells accumulates dN.
+__global__ void k_adj_inflow(SimDev d, AsmDev a, const double* __restrict__ cf, double* __restrict__ Q) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.n) return;
+  const int n = d.n, nc = d.nc, ncn = d.nconn;
+  double s[NCM];
+  for (int nu = 0; nu < nc; ++nu) s[nu] = 0;
+  for (int k = 0; k < a.ccount[e]; ++k) {
+    const int code = a.cc[(int64_t)e * 6 + k];
+    const int c = code >> 1;
+    const bool here = !(code & 1);
+    for (int nu = 0; nu < nc; ++nu) s[nu] += here ? -cf[(int64_t)nu * ncn + c] : cf[(int64_t)nu * ncn + c];
+  }
+  for (int j = a.src_ptr[e]; j < a.src_ptr[e + 1]; ++j) {
+    const double* qs = a.src_q + (int64_t)a.src_id[j] * NCM;
+    for (int nu = 0; nu < nc; ++nu) s[nu] += qs[nu];
+  }
+  for (int nu = 0; nu < nc; ++nu) Q[(int64_t)nu * n + e] = s[nu];
+}
+
+// Exact pressure Jacobian rows: connection terms gathered as
+// k_assemble_rows gathers the Newton Jacobian, plus the cell's own
+// derivatives of dRdN and dRdp; locked rows are identity rows.
+__global__ void k_adj_rows(SimDev d, AsmDev a, Rec r, const double* __restrict__ Jh, const double* __restrict__ Jt,
+                           const double* __restrict__ Q, const double* __restrict__ p_prev, double dt,
+                           double* __restrict__ val) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.n) return;
+  const int n = d.n, nc = d.nc;
+  const int r0 = a.rowptr[e], r1 = a.rowptr[e + 1];
+  for (int q = r0; q < r1; ++q) val[q] = 0;
+  if (a.locked[e]) {
+    val[a.diag[e]] = 1.0;
+    return;
+  }
+  for (int k = 0; k < a.ccount[e]; ++k) {
+    const int code = a.cc[(int64_t)e * 6 + k];
+    const int c = code >> 1;
+    const bool here = !(code & 1);
+    for (int m = a.md_ptr[c]; m < a.md_ptr[c + 1]; ++m) {
+      const int pos = here ? a.pos_here[m] : a.pos_there[m];
+      if (pos >= r0 && pos < r1) val[pos] += here ? Jh[m] : Jt[m];
+      else atomicCAS(d.flag, 0, FL_PATTERN);
+    }
+  }
+  double diag = d.dRdp[e] / dt + (d.p[e] - p_prev[e]) / dt * r(Q_DRDP, 0, e);
+  for (int nu = 0; nu < nc; ++nu) diag += Q[(int64_t)nu * n + e] * r(Q_DRDN + nu, 0, e);
+  val[a.diag[e]] += diag;
+}
+
+// Weights on Q: z = dt (aN off the locked cells + objective weights) - y dRdN
+__global__ void k_adj_z(int n, int nc, const int* __restrict__ locked, const double* __restrict__ objw,
+                        const double* __restrict__ cw, const double* __restrict__ aN, const double* __restrict__ y,
+                        const double* __restrict__ dRdN, double dt, double* __restrict__ z) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const bool lk = locked[e];
+  for (int nu = 0; nu < nc; ++nu) {
+    double w = (lk ? 0.0 : aN[(int64_t)nu * n + e]) + objw[e] * cw[nu];
+    double v = dt * w;
+    if (y && !lk) v -= y[e] * dRdN[(int64_t)nu * n + e];
+    z[(int64_t)nu * n + e] = v;
+  }
+}
+
+__global__ void k_adj_rhs(int n, const double* __restrict__ aP, const double* __restrict__ g0, double* __restrict__ w) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) w[e] = aP[e] + g0[e];
+}
+
+// Potentials of the theta pairs: p + pc for each phase, and the body force
+__global__ void k_adj_phi(SimDev d, double* __restrict__ phi) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.n) return;
+  const int n = d.n;
+  phi[e] = d.p[e] - d.pcow[e];
+  phi[n + e] = d.p[e];
+  phi[2 * (int64_t)n + e] = d.p[e] + d.pcgo[e];
+  phi[3 * (int64_t)n + e] = d.bf[e];
+}
+
+// Adjoint state of step n from that of step n+1 (g: VJP of z^M - z^F)
+__global__ void k_adj_update(SimDev d, const int* __restrict__ locked, Rec ra, Rec rb, const double* __restrict__ y,
+                             const double* __restrict__ g, const double* __restrict__ Q,
+                             const double* __restrict__ p_prev, double dt, double* __restrict__ aP,
+                             double* __restrict__ aN) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.n) return;
+  const int n = d.n, nc = d.nc;
+  const bool lk = locked[e];
+  const double yt = lk ? 0.0 : y[e];
+  const double dpp = d.p[e] - p_prev[e];
+  for (int nu = 0; nu < nc; ++nu) {
+    const int k = 1 + nu;
+    double diag = dpp / dt * ra(Q_DRDP, k, e) + rb(Q_R, k, e) / dt;
+    for (int mu = 0; mu < nc; ++mu) diag += Q[(int64_t)mu * n + e] * ra(Q_DRDN + mu, k, e);
+    aN[(int64_t)nu * n + e] += g[(int64_t)k * n + e] - yt * diag;
+  }
+  aP[e] = lk ? y[e] : -yt * (rb(Q_R, 0, e) - d.dRdp[e]) / dt;
+}
+
+// Objective increment: sum over listed cells of sum_nu cw_nu dN (one thread,
+// fixed order)
+__global__ void k_adj_objective(int ncells, const int* __restrict__ cells, const double* __restrict__ objw_cells,
+                                const double* __restrict__ cw, int n, int nc, const double* __restrict__ dN,
+                                double* __restrict__ J) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double s = 0;
+  for (int j = 0; j < ncells; ++j)
+    for (int nu = 0; nu < nc; ++nu) s += objw_cells[j] * cw[nu] * dN[(int64_t)nu * n + cells[j]];
+  *J += s;
+}
 
 }  // namespace
 
@@ -1200,6 +1553,243 @@ struct Sim {
     secondaries();
     ctx->sync();
   }
+
+  // ---------------------------------------------------------- adjoint ----
+  struct Snapshot {
+    double time = 0;
+    DeviceBuffer<double> p, T, N, phN, phdVdN;
+    DeviceBuffer<int> present;
+  };
+  std::vector<Snapshot> ck;        // state at the first step of every block
+  Snapshot adj_end;                // state after the forward run
+  std::vector<double> adj_dt;
+  int adj_every = 0;
+  bool adj_ready = false;
+  DeviceBuffer<double> blk_p, blk_N, blk_p1;  // per step of one block: p^n, N^n, p^{n+1}
+  int blk_first = -1;                         // step held in slot 0 of the block buffers
+  DeviceBuffer<double> adj_objw, adj_cw, adj_objw_cells, adj_J;
+  DeviceBuffer<int> adj_cells;
+  int adj_ncells = 0;
+  DeviceBuffer<int> inv_ptr, inv_q;  // MD entries of every element, ascending
+
+  void snap(Snapshot& s) {
+    s.time = time;
+    s.p.resize(n);
+    s.T.resize(n);
+    s.N.resize((size_t)nc * n);
+    s.phN.resize((size_t)nc * 3 * n);
+    s.phdVdN.resize((size_t)nc * 3 * n);
+    s.present.resize(n);
+    copy(p, s.p, n);
+    copy(T, s.T, n);
+    copy(N, s.N, (int64_t)nc * n);
+    copy(phN, s.phN, (int64_t)nc * 3 * n);
+    copy(phdVdN, s.phdVdN, (int64_t)nc * 3 * n);
+    RSG_CUDA(cudaMemcpyAsync(s.present.get(), present.get(), sizeof(int) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+
+  void unsnap(Snapshot& s) {
+    time = s.time;
+    copy(s.p, p, n);
+    copy(s.T, T, n);
+    copy(s.N, N, (int64_t)nc * n);
+    copy(s.phN, phN, (int64_t)nc * 3 * n);
+    copy(s.phdVdN, phdVdN, (int64_t)nc * 3 * n);
+    RSG_CUDA(cudaMemcpyAsync(present.get(), s.present.get(), sizeof(int) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    secondaries();
+  }
+
+  // one step of the forward run, keeping p^n, N^n and p^{n+1} in slot j
+  void record_step(int j, double dt, rsg_step_info* si) {
+    RSG_CUDA(cudaMemcpyAsync(blk_p.get() + (int64_t)j * n, p.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                             ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(blk_N.get() + (int64_t)j * nc * n, N.get(), sizeof(double) * nc * n,
+                             cudaMemcpyDeviceToDevice, ctx->stream));
+    step(dt, si);
+    RSG_CUDA(cudaMemcpyAsync(blk_p1.get() + (int64_t)j * n, p.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                             ctx->stream));
+  }
+
+  void forward_record(int nsteps, const double* dts, int every, int ncells, const int* cells, const double* cellw,
+                      const double* cw, double* J, rsg_adjoint_info* info) {
+    if (cubic.size()) throw Error(RSG_UNSUPPORTED, "the adjoint covers black-oil fluids only");
+    if (nc > ADJ_NC) throw Error(RSG_UNSUPPORTED, "the adjoint supports at most 3 components");
+    if (nsteps <= 0) throw Error(RSG_BAD_ARG, "at least one step is required");
+    for (int s = 0; s < nsteps; ++s)
+      if (!(dts[s] > 0)) throw Error(RSG_BAD_ARG, "time steps must be positive");
+    if (ncells < 0 || (ncells > 0 && (!cells || !cellw)) || !cw) throw Error(RSG_BAD_ARG, "objective");
+    std::vector<double> objw(n, 0.0);
+    for (int j = 0; j < ncells; ++j) {
+      if (cells[j] < 0 || cells[j] >= n) throw Error(RSG_BAD_ARG, "objective cell out of range");
+      objw[cells[j]] += cellw[j];
+    }
+    adj_ready = false;
+    adj_every = std::max(1, std::min(every, nsteps));
+    adj_dt.assign(dts, dts + nsteps);
+    const int nblocks = (nsteps + adj_every - 1) / adj_every;
+    ck.resize(nblocks);
+    blk_p.resize((size_t)adj_every * n);
+    blk_p1.resize((size_t)adj_every * n);
+    blk_N.resize((size_t)adj_every * nc * n);
+    adj_objw.resize(n);
+    adj_cw.resize(nc);
+    adj_ncells = ncells;
+    adj_cells.resize(std::max(ncells, 1));
+    adj_objw_cells.resize(std::max(ncells, 1));
+    adj_J.resize(1);
+    RSG_CUDA(cudaMemcpyAsync(adj_objw.get(), objw.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(adj_cw.get(), cw, sizeof(double) * nc, cudaMemcpyHostToDevice, ctx->stream));
+    if (ncells) {
+      RSG_CUDA(cudaMemcpyAsync(adj_cells.get(), cells, sizeof(int) * ncells, cudaMemcpyHostToDevice, ctx->stream));
+      RSG_CUDA(cudaMemcpyAsync(adj_objw_cells.get(), cellw, sizeof(double) * ncells, cudaMemcpyHostToDevice,
+                               ctx->stream));
+    }
+    RSG_CUDA(cudaMemsetAsync(adj_J.get(), 0, sizeof(double), ctx->stream));
+    rsg_adjoint_info in{};
+    for (int s = 0; s < nsteps; ++s) {
+      if (s % adj_every == 0) snap(ck[s / adj_every]);
+      rsg_step_info si{};
+      record_step(s % adj_every, dts[s], &si);
+      in.steps++;
+      in.newton_iterations += si.newton_iterations;
+      in.linear_iterations += si.linear_iterations;
+      RSG_LAUNCH(*ctx, "adj_objective", k_adj_objective, 1, 32, 0, adj_ncells, adj_cells.get(), adj_objw_cells.get(),
+                 adj_cw.get(), n, nc, dNbuf.get(), adj_J.get());
+    }
+    blk_first = (nblocks - 1) * adj_every;
+    snap(adj_end);
+    double hJ = 0;
+    RSG_CUDA(cudaMemcpyAsync(&hJ, adj_J.get(), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    in.objective = hJ;
+    if (J) *J = hJ;
+    if (info) *info = in;
+    adj_ready = true;
+  }
+
+  void build_inverse_md() {
+    if (inv_ptr.size() == (size_t)n + 1) return;
+    const std::vector<int>& ptr = mesh->h_md_ptr;
+    const std::vector<int>& el = mesh->h_md_elem;
+    std::vector<int> ip(n + 1, 0), iq(std::max<size_t>(el.size(), 1));
+    for (size_t m = 0; m < el.size(); ++m) ip[el[m] + 1]++;
+    for (int e = 0; e < n; ++e) ip[e + 1] += ip[e];
+    std::vector<int> fill(ip.begin(), ip.end() - 1);
+    for (int c = 0; c < nconn; ++c)
+      for (int m = ptr[c]; m < ptr[c + 1]; ++m) iq[fill[el[m]]++] = m;
+    inv_ptr.resize(n + 1);
+    inv_q.resize(iq.size());
+    RSG_CUDA(cudaMemcpyAsync(inv_ptr.get(), ip.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(inv_q.get(), iq.data(), sizeof(int) * iq.size(), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->sync();
+  }
+
+  void backward(double rtol, double* grad_host, double* dJdp0, double* dJdN0, rsg_adjoint_info* info) {
+    if (!adj_ready) throw Error(RSG_BAD_ARG, "backward needs a recorded forward run");
+    build_inverse_md();
+    const int K = 1 + nc, nq = adj_nq(nc);
+    const int64_t nmd = mesh->nmd;
+    DeviceBuffer<double> aP(n), aN((size_t)nc * n), grad(mesh->g.nel), recA((size_t)nq * K * n),
+        recB((size_t)nq * K * n), Q((size_t)nc * n), z((size_t)nc * n), cmd((size_t)std::max<int64_t>(nmd, 1) * K),
+        mu((size_t)4 * nconn), g((size_t)K * n), w(n), y(n), phi((size_t)4 * n), jh(std::max<int64_t>(nmd, 1)),
+        jt(std::max<int64_t>(nmd, 1));
+    DeviceBuffer<int> aflag(1);
+    RSG_CUDA(cudaMemsetAsync(aP.get(), 0, sizeof(double) * n, ctx->stream));
+    RSG_CUDA(cudaMemsetAsync(aN.get(), 0, sizeof(double) * nc * n, ctx->stream));
+    RSG_CUDA(cudaMemsetAsync(grad.get(), 0, sizeof(double) * mesh->g.nel, ctx->stream));
+    RSG_CUDA(cudaMemsetAsync(aflag.get(), 0, sizeof(int), ctx->stream));
+    Csr jac;
+    jac.build(ctx, n, A.m.nnz, A.m.h_rowptr.data(), A.m.h_col.data());
+    CsrTranspose tr;
+    SolverPtr solver_t = make_solver(ctx, spec.linear_solver, spec.preconditioner, rtol, spec.absolute_tolerance,
+                                     spec.divergence_tolerance, spec.max_linear_iterations,
+                                     spec.gmres_restart > 0 ? spec.gmres_restart : 30);
+    if (spec.inner_iterations > 0) solver_set_inner(*solver_t, spec.inner_iterations, spec.inner_tolerance);
+    const AdjConn ac{mesh->md_ptr.get(), mesh->md_elem.get(), mesh->md_k.get(), mesh->conn.get(), rho_cs.get(), up.get()};
+    const Rec ra{recA.get(), n, K}, rb{recB.get(), n, K};
+    const int nsteps = (int)adj_dt.size();
+    const int nblocks = (nsteps + adj_every - 1) / adj_every;
+    rsg_adjoint_info in{};
+    for (int b = nblocks - 1; b >= 0; --b) {
+      const int n0 = b * adj_every, n1 = std::min(n0 + adj_every, nsteps);
+      if (blk_first != n0) {  // recompute the block from its checkpoint
+        unsnap(ck[b]);
+        for (int s = n0; s < n1; ++s) {
+          rsg_step_info si{};
+          record_step(s - n0, adj_dt[s], &si);
+          in.recomputed_steps++;
+        }
+        blk_first = n0;
+      }
+      for (int s = n1 - 1; s >= n0; --s) {
+        const int j = s - n0;
+        const double dt = adj_dt[s];
+        const double* pn = blk_p.get() + (int64_t)j * n;
+        // state (p^{n+1}, N^n) and its secondaries
+        copy_ptr(blk_p1.get() + (int64_t)j * n, p.get(), n);
+        copy_ptr(blk_N.get() + (int64_t)j * nc * n, N.get(), (int64_t)nc * n);
+        secondaries();
+        SimDev d = dev();
+        AsmDev as = adev();
+        RSG_LAUNCH(*ctx, "molar_conn", k_molar_conn, blocks_for(nconn, 128), 128, 0, d, cdev(), cf.get());
+        RSG_LAUNCH(*ctx, "adj_inflow", k_adj_inflow, blocks_for(n, 128), 128, 0, d, as, cf.get(), Q.get());
+        RSG_LAUNCH(*ctx, "cell_dual", k_cell_dual, blocks_for(n, 128), 128, 0, d, p.get(), N.get(), recA.get());
+        RSG_LAUNCH(*ctx, "cell_dual", k_cell_dual, blocks_for(n, 128), 128, 0, d, pn, N.get(), recB.get());
+        // moles and objective: weights z^M on Q, their pressure derivatives
+        RSG_LAUNCH(*ctx, "adj_z", k_adj_z, blocks_for(n, 256), 256, 0, n, nc, locked.get(), adj_objw.get(),
+                   adj_cw.get(), aN.get(), (const double*)nullptr, dRdN.get(), dt, z.get());
+        RSG_LAUNCH(*ctx, "adj_conn_vjp", k_adj_conn_vjp, blocks_for(nconn, 128), 128, 0, d, ac, ra, z.get(), cmd.get(),
+                   mu.get(), aflag.get());
+        RSG_LAUNCH(*ctx, "adj_gather", k_adj_gather, blocks_for(n, 128), 128, 0, n, K, inv_ptr.get(), inv_q.get(),
+                   cmd.get(), g.get());
+        RSG_LAUNCH(*ctx, "adj_rhs", k_adj_rhs, blocks_for(n, 256), 256, 0, n, aP.get(), g.get(), w.get());
+        // exact pressure Jacobian, transposed solve
+        RSG_LAUNCH(*ctx, "adj_conn_jac", k_adj_conn_jac, blocks_for(nconn, 128), 128, 0, d, ac, ra, jh.get(), jt.get(),
+                   aflag.get());
+        RSG_LAUNCH(*ctx, "adj_rows", k_adj_rows, blocks_for(n, 128), 128, 0, d, as, ra, jh.get(), jt.get(), Q.get(),
+                   pn, dt, jac.val.get());
+        jac.sell_dirty = true;
+        tr.update(jac);
+        RSG_CUDA(cudaMemsetAsync(y.get(), 0, sizeof(double) * n, ctx->stream));
+        rsg_solve_info si{};
+        solver_setup(*solver_t, tr.AT);
+        solver_solve(*solver_t, tr.AT, w.get(), y.get(), &si);
+        in.adjoint_linear_iterations += si.iterations;
+        // weights z^M - z^F: moles, objective and pressure equation together
+        RSG_LAUNCH(*ctx, "adj_z", k_adj_z, blocks_for(n, 256), 256, 0, n, nc, locked.get(), adj_objw.get(),
+                   adj_cw.get(), aN.get(), (const double*)y.get(), dRdN.get(), dt, z.get());
+        RSG_LAUNCH(*ctx, "adj_conn_vjp", k_adj_conn_vjp, blocks_for(nconn, 128), 128, 0, d, ac, ra, z.get(), cmd.get(),
+                   mu.get(), aflag.get());
+        RSG_LAUNCH(*ctx, "adj_gather", k_adj_gather, blocks_for(n, 128), 128, 0, n, K, inv_ptr.get(), inv_q.get(),
+                   cmd.get(), g.get());
+        RSG_LAUNCH(*ctx, "adj_phi", k_adj_phi, blocks_for(n, 256), 256, 0, d, phi.get());
+        mpfa_adjoint(*mesh, 4, mu.get(), phi.get(), 1.0, true, grad.get());
+        RSG_LAUNCH(*ctx, "adj_update", k_adj_update, blocks_for(n, 256), 256, 0, d, locked.get(), ra, rb, y.get(),
+                   g.get(), Q.get(), pn, dt, aP.get(), aN.get());
+        in.backward_steps++;
+      }
+    }
+    int hf = 0;
+    RSG_CUDA(cudaMemcpyAsync(&hf, aflag.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    if (hf) throw Error(RSG_UNSUPPORTED, "a connection has more transmissibilities than the adjoint handles");
+    check_flag();
+    RSG_CUDA(cudaMemcpyAsync(grad_host, grad.get(), sizeof(double) * mesh->g.nel, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    if (dJdp0) RSG_CUDA(cudaMemcpyAsync(dJdp0, aP.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (dJdN0)
+      RSG_CUDA(cudaMemcpyAsync(dJdN0, aN.get(), sizeof(double) * nc * n, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    // leave the simulator at the end of the forward run
+    unsnap(adj_end);
+    blk_first = -1;
+    ctx->sync();
+    if (info) *info = in;
+  }
+
+  void copy_ptr(const double* a, double* b, int64_t count) {
+    RSG_LAUNCH(*ctx, "copy", k_copy, blocks_for(count, 256), 256, 0, count, a, b);
+  }
 };
 
 }  // namespace rsg
@@ -1535,6 +2125,21 @@ rsg_status rsg_sim_step_to(rsg_sim* s, double end_time, const rsg_dt_control* c,
     return g;
   }
   return (rsg_status)st;
+}
+
+rsg_status rsg_sim_forward(rsg_sim* s, int32_t nsteps, const double* dt, int32_t checkpoint_every, int32_t ncells,
+                           const int32_t* cells, const double* cell_weights, const double* component_weights,
+                           double* objective, rsg_adjoint_info* info) {
+  if (!s || !dt || nsteps <= 0 || checkpoint_every <= 0 || !component_weights) return RSG_BAD_ARG;
+  return guarded(s->s->ctx, [&] {
+    s->s->forward_record(nsteps, dt, checkpoint_every, ncells, cells, cell_weights, component_weights, objective, info);
+  });
+}
+
+rsg_status rsg_sim_backward(rsg_sim* s, double rtol, double* dJ_dlogk, double* dJ_dp0, double* dJ_dN0,
+                            rsg_adjoint_info* info) {
+  if (!s || !dJ_dlogk || !(rtol > 0)) return RSG_BAD_ARG;
+  return guarded(s->s->ctx, [&] { s->s->backward(rtol, dJ_dlogk, dJ_dp0, dJ_dN0, info); });
 }
 
 rsg_status rsg_sim_retract(rsg_sim* s) {

@@ -1,0 +1,196 @@
+"""Discrete adjoint of the two-phase simulator run (sequential pressure
+Newton step and explicit molar update, Discretisation.java:280-919) with
+respect to per-element log-permeability, checked against central finite
+differences of the GPU forward and of the oracle forward, with the objective
+"oil moles produced into the Fixed producer cells".
+
+Every difference quotient carries the forward run's own rounding: with the
+Newton and Krylov tolerances at 1e-13, J is reproducible to about 1e-12 |J|
+(GPU) to 1e-11 |J| (oracle) under a perturbation, i.e. that much over h in
+the quotient, and each check allows FD_NOISE * |J| / h for it.  At h = 1e-3 in log k that noise and the
+O(h^2) truncation are both near 1e-6 of the gradient, so that check is the
+tight one; at the step h = 1e-6 the noise is about 1e-6 |J|.  Measured on
+the 8 x 8 x 3 case: the adjoint agrees with h = 1e-4 differences to 5
+digits wherever the gradient is above 1e-2 of its largest entry."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from ressim_gb300 import abi, api
+from ressim_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-6        # the check step
+H_FINE = 1e-3   # the accuracy step
+FD_NOISE = 2e-11
+TIGHT = dict(rtol=1e-13, ptol=1e-13, stop_rule=1, max_newton=60)
+
+
+def _sim(ctx, case, perm, spec_kw=TIGHT):
+    keep = abi.Keep()
+    gm = api.Mesh(ctx, 3, case["ni"], case["nj"], case["nk"], perm, coords=case["nodes"])
+    gm.compute_mpfa()
+    gs = api.Discretisation(ctx, gm, W.two_phase_fluid(keep), W.corey(), case["porosity"], case["compaction"],
+                            W.build_sources(keep, case), W.build_initial(case), W.runspec(**spec_kw))
+    gs._adj_keep = (keep, gm)
+    return gs
+
+
+def _objective(ctx, case, perm, dts):
+    gs = _sim(ctx, case, perm)
+    J, _ = gs.forward(dts, len(dts), case["producer"], [0.0, 1.0])
+    return J
+
+
+def _oracle_objective(case, perm, dts):
+    keep = abi.Keep()
+    om = O.Mesh(3, case["ni"], case["nj"], case["nk"], coords=case["nodes"], perm=perm)
+    om.mpfa()
+    os_ = O.Simulator(om, W.two_phase_fluid(keep), W.corey(), case["porosity"], case["compaction"],
+                      W.build_sources(keep, case), W.build_initial(case), W.runspec(**TIGHT))
+    J = 0.0
+    for dt in dts:
+        os_.step(dt)
+        J += float(np.sum(os_.last_dn()[1, case["producer"]]))
+    return J
+
+
+def _scaled(perm, e, s):
+    p = perm.copy()
+    p[e] *= np.exp(s)
+    return p
+
+
+def _case(ni=8, nj=8, nk=3):
+    return W.two_phase_case(ni=ni, nj=nj, nk=nk, seed=3, dt=4 * 8640.0)
+
+
+def _cells(case, count, seed):
+    n = case["ni"] * case["nj"] * case["nk"]
+    g = np.random.Generator(np.random.PCG64(seed))
+    near = [int(case["producer"][0]) + d for d in (1, -1, case["ni"], -case["ni"])]
+    return np.unique(np.concatenate([g.choice(n, size=count, replace=False), near]))
+
+
+@pytest.mark.parametrize("nsteps", [1, 3])
+def test_adjoint_gradient_matches_gpu_fd(ctx, nsteps):
+    case = _case()
+    dts = [case["dt"]] * nsteps
+    gs = _sim(ctx, case, case["perm"])
+    J, finfo = gs.forward(dts, 2, case["producer"], [0.0, 1.0])
+    assert finfo.steps == nsteps and J > 0
+    grad, dp0, dN0, binfo = gs.backward(rtol=1e-13)
+    assert binfo.backward_steps == nsteps
+    assert binfo.recomputed_steps == (nsteps - 1) // 2 * 2
+    scale = np.max(np.abs(grad))
+    assert scale > 0
+    for e in _cells(case, 10, 5):
+        fd = (_objective(ctx, case, _scaled(case["perm"], e, H_FINE), dts) -
+              _objective(ctx, case, _scaled(case["perm"], e, -H_FINE), dts)) / (2 * H_FINE)
+        assert abs(fd - grad[e]) <= FD_NOISE * J / H_FINE + 1e-5 * scale, (e, fd, grad[e], scale)
+        fd = (_objective(ctx, case, _scaled(case["perm"], e, H), dts) -
+              _objective(ctx, case, _scaled(case["perm"], e, -H), dts)) / (2 * H)
+        assert abs(fd - grad[e]) <= FD_NOISE * J / H + 1e-4 * abs(fd), (e, fd, grad[e], J)
+
+
+def test_adjoint_checkpointing_is_exact(ctx):
+    case = _case()
+    dts = [case["dt"]] * 4
+    grads = []
+    for every in (4, 2, 1):
+        gs = _sim(ctx, case, case["perm"])
+        J, _ = gs.forward(dts, every, case["producer"], [0.0, 1.0])
+        g, dp0, dN0, info = gs.backward(rtol=1e-13)
+        assert info.recomputed_steps == {4: 0, 2: 2, 1: 3}[every]
+        grads.append((J, g, dp0, dN0))
+        # the simulator is left at the end of the forward run
+        p, N, S = gs.state()
+        ref = _sim(ctx, case, case["perm"])
+        for dt in dts:
+            ref.step(dt)
+        rp, rN, rS = ref.state()
+        assert np.array_equal(p, rp) and np.array_equal(N, rN)
+    for J, g, dp0, dN0 in grads[1:]:
+        assert J == grads[0][0]
+        assert np.array_equal(g, grads[0][1])
+        assert np.array_equal(dN0, grads[0][3])
+
+
+def test_adjoint_initial_state_sensitivity(ctx):
+    """dJ/dN0 of the adjoint recursion against FD of the initial moles."""
+    case = _case()
+    dts = [case["dt"]] * 2
+    gs = _sim(ctx, case, case["perm"])
+    gs.forward(dts, 2, case["producer"], [0.0, 1.0])
+    grad, dp0, dN0, _ = gs.backward(rtol=1e-13)
+    base = _sim(ctx, case, case["perm"])
+    p0, N0, _ = base.state()
+    locked = set(int(c) for c in case["producer"])
+    for e in _cells(case, 4, 9):
+        if int(e) in locked:
+            continue
+        for nu in range(2):
+            h = 1e-6 * N0[nu, e]
+            vals = []
+            for s in (h, -h):
+                N = N0.copy()
+                N[nu, e] += s
+                sim = _sim(ctx, case, case["perm"])
+                sim.set_state(p0, N)
+                vals.append(sim.forward(dts, 2, case["producer"], [0.0, 1.0])[0])
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(fd - dN0[nu, e]) <= 1e-5 * np.max(np.abs(dN0)) + 1e-4 * abs(fd), (e, nu, fd, dN0[nu, e])
+
+
+def test_adjoint_gradient_matches_oracle_fd(ctx):
+    """Finite differences of the oracle forward on a 16 x 16 x 4 grid."""
+    case = _case(16, 16, 4)
+    dts = [case["dt"]] * 2
+    gs = _sim(ctx, case, case["perm"])
+    J, _ = gs.forward(dts, 1, case["producer"], [0.0, 1.0])
+    assert abs(J - _oracle_objective(case, case["perm"], dts)) <= 1e-9 * abs(J)
+    grad, _, _, _ = gs.backward(rtol=1e-13)
+    scale = np.max(np.abs(grad))
+    for e in _cells(case, 6, 13):
+        fd = (_oracle_objective(case, _scaled(case["perm"], e, H_FINE), dts) -
+              _oracle_objective(case, _scaled(case["perm"], e, -H_FINE), dts)) / (2 * H_FINE)
+        assert abs(fd - grad[e]) <= FD_NOISE * J / H_FINE + 1e-5 * scale, (e, fd, grad[e], scale)
+        fd = (_oracle_objective(case, _scaled(case["perm"], e, H), dts) -
+              _oracle_objective(case, _scaled(case["perm"], e, -H), dts)) / (2 * H)
+        assert abs(fd - grad[e]) <= FD_NOISE * J / H + 1e-4 * abs(fd), (e, fd, grad[e], J)
+
+
+def test_adjoint_autograd_directional(ctx):
+    """torch.autograd.Function over the forward/backward pair (harness only):
+    the gradient along a random direction of all log k against central
+    differences of the GPU forward."""
+    torch = pytest.importorskip("torch")
+    case = _case()
+    dts = [case["dt"]] * 2
+    n = case["ni"] * case["nj"] * case["nk"]
+
+    class CumulativeOil(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx_, theta):
+            perm = case["perm"] * np.exp(theta.detach().numpy())[:, None]
+            gs = _sim(ctx, case, perm)
+            J, _ = gs.forward(dts, 1, case["producer"], [0.0, 1.0])
+            grad, _, _, _ = gs.backward(rtol=1e-13)
+            ctx_.save_for_backward(torch.from_numpy(grad))
+            return torch.tensor(J, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx_, gout):
+            (grad,) = ctx_.saved_tensors
+            return gout * grad
+
+    theta = torch.zeros(n, dtype=torch.float64, requires_grad=True)
+    J = CumulativeOil.apply(theta)
+    J.backward()
+    grad = theta.grad.numpy()
+    v = np.random.Generator(np.random.PCG64(2)).standard_normal(n)
+    jp = _objective(ctx, case, case["perm"] * np.exp(H_FINE * v)[:, None], dts)
+    jm = _objective(ctx, case, case["perm"] * np.exp(-H_FINE * v)[:, None], dts)
+    fd = (jp - jm) / (2 * H_FINE)
+    assert abs(fd - grad @ v) <= FD_NOISE * float(J.detach()) / H_FINE + 1e-5 * np.linalg.norm(grad) * np.linalg.norm(v)
