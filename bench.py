@@ -359,11 +359,16 @@ def ensemble_leg(args):
     """Config-4-style ensemble: members with grids drawn uniformly between
     32x32x8 and 96x96x24 and their own seeded permeability, each on its own
     context; one rsg_ensemble_step steps all of them concurrently.  Reported
-    against stepping the same members one after another (plain FP64 path)."""
+    against stepping the same members one after another (plain FP64 path),
+    for FP64 members and for members with the mixed-precision pressure
+    solver (config 4's Krylov stack)."""
     from ressim_gb300 import api
 
     sizes = W.ensemble_sizes(args.ensemble)
     members = []
+    mixed = []
+    mixed_units = 0.0
+    t_mixed = None
     try:
         for k, (ni, nj, nk) in enumerate(sizes):
             c = api.Context(0)
@@ -386,13 +391,32 @@ def ensemble_leg(args):
             for c, sim, case, n in members:
                 units_s += n * sim.step(case["dt"]).newton_iterations
         t_ser = time.perf_counter() - t0
-    finally:
         for m in members:
             m[0].close()
-    return {"members": len(sizes), "cells": int(sum(m[3] for m in members)),
+        members = []
+        for k, (ni, nj, nk) in enumerate(sizes):
+            c = api.Context(0)
+            sim, case = W.build_two_phase_sim(c, ni, nj, nk, seed=100 + k, rtol=args.rtol, method=abi.FGMRES_MIXED,
+                                              inner_iterations=int(args.inner[0]), inner_tolerance=args.inner[1])
+            mixed.append((c, sim, case, ni * nj * nk))
+        msims = [m[1] for m in mixed]
+        api.ensemble_step(msims, dts)  # warm-up
+        t0 = time.perf_counter()
+        for _ in range(args.ensemble_steps):
+            infos, sts = api.ensemble_step(msims, dts)
+            if sts.any():
+                raise RuntimeError(f"mixed ensemble member failed: {sts.tolist()}")
+            mixed_units += sum(m[3] * inf.newton_iterations for m, inf in zip(mixed, infos))
+        t_mixed = time.perf_counter() - t0
+    finally:
+        for m in members + mixed:
+            m[0].close()
+    serial = units_s / t_ser
+    return {"members": len(sizes), "cells": int(sum(n for (_, _, _, n) in mixed)) if mixed else None,
             "grids": "each axis uniform in 32..96 x 32..96 x 8..24 (seeded)", "steps": args.ensemble_steps,
-            "value": units / t_conc, "unit": METRIC, "serial_value": units_s / t_ser,
-            "speedup_vs_serial": (units / t_conc) / (units_s / t_ser)}
+            "value": units / t_conc, "unit": METRIC, "serial_value": serial,
+            "speedup_vs_serial": (units / t_conc) / serial,
+            "mixed_value": mixed_units / t_mixed, "mixed_speedup_vs_serial_fp64": (mixed_units / t_mixed) / serial}
 
 
 def flash_leg(args):
@@ -466,12 +490,28 @@ def compositional_leg(args):
             newton += sim.step(case["dt"]).newton_iterations
         ctx.synchronize()
         secs = time.perf_counter() - t0
+        # the same steps with the mixed-precision pressure solver (FP64 flash
+        # and Rachford-Rice, FP32 inner Krylov stage)
+        mspec = W.runspec(rtol=args.rtol, method=abi.FGMRES_MIXED, inner_iterations=int(args.inner[0]),
+                          inner_tolerance=args.inner[1])
+        mspec.truncate_negative_moles = 1
+        msim = api.Discretisation(ctx, mesh, f, W.corey(), case["porosity"], case["compaction"], srcs, init, mspec)
+        msim.step(case["dt"])  # warm-up
+        ctx.synchronize()
+        mnewton = 0
+        t0 = time.perf_counter()
+        for _ in range(args.comp_steps):
+            mnewton += msim.step(case["dt"]).newton_iterations
+        ctx.synchronize()
+        msecs = time.perf_counter() - t0
+        pm, pd = msim.state()[0], sim.state()[0]
     finally:
         ctx.close()
     n = ni * nj * nk
     out = {"grid": f"{ni}x{nj}x{nk}", "components": f.nc, "steps": args.comp_steps, "newton_iterations": newton,
            "dt_s": case["dt"],
-           "value": n * newton / secs, "unit": METRIC}
+           "value": n * newton / secs, "unit": METRIC, "mixed_value": n * mnewton / msecs,
+           "mixed_max_rel_pressure_diff_vs_fp64": float(np.max(np.abs(pm - pd) / np.abs(pd)))}
     if not args.no_cpu_baseline:
         om = O.Mesh(3, ni, nj, nk, coords=case["nodes"], perm=case["perm"])
         om.mpfa()

@@ -205,6 +205,10 @@ rsg_status rsg_mesh_destroy(rsg_mesh* m);
 /* O_MPFA.calculateTransmissibilities + Connection.setDarcyTransmissibilities,
  * on the GPU.  continuity in (0, 1] (O_MPFA "Continuity" key). */
 rsg_status rsg_mesh_compute_mpfa(rsg_mesh* m, double continuity);
+/* TPFA.calculateTransmissibilities (geometry/flux/TPFA.java:31-72), the
+ * reference's two-point alternative, on the GPU: two MD entries per
+ * connection, (here, t) and (there, -t), with TPFA's distance weighting. */
+rsg_status rsg_mesh_compute_tpfa(rsg_mesh* m);
 /* counts[0] elements, [1] connections, [2] MD entries, [3] corner points,
  * [4] pressure-pattern nnz (valid after MPFA) */
 rsg_status rsg_mesh_get_counts(rsg_mesh* m, int64_t* counts);

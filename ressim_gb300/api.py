@@ -98,6 +98,7 @@ def _declare(L):
         "rsg_mesh_create_structured": (i32, [vp, i32, i32, i32, i32, P(d), d, d, d, d, d, d, P(d), PP()]),
         "rsg_mesh_destroy": (i32, [vp]),
         "rsg_mesh_compute_mpfa": (i32, [vp, d]),
+        "rsg_mesh_compute_tpfa": (i32, [vp]),
         "rsg_mesh_get_counts": (i32, [vp, P(i64)]),
         "rsg_mesh_get_geometry": (i32, [vp, P(d), P(d)]),
         "rsg_mesh_get_connections": (i32, [vp, P(i32)]),
@@ -418,6 +419,10 @@ class Mesh:
 
     def compute_mpfa(self, continuity=1.0):
         self.ctx.check(lib().rsg_mesh_compute_mpfa(self.h, continuity), "compute_mpfa")
+
+    def compute_tpfa(self):
+        """TPFA.calculateTransmissibilities: the two-point alternative to MPFA-O."""
+        self.ctx.check(lib().rsg_mesh_compute_tpfa(self.h), "compute_tpfa")
 
     def counts(self):
         c = (C.c_int64 * 5)()

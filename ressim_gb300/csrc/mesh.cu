@@ -850,6 +850,72 @@ __global__ void k_rows(int nel, int with_diag, const int* __restrict__ cc, const
   if (!FILL) row_len[e] = m;
 }
 
+// TPFA.calculateTransmissibility (geometry/flux/TPFA.java:50-72), with its
+// use of ||K_j n_j|| for both distances: MD = {(here, t), (there, -t)}.
+__global__ void k_tpfa(Grid g, const int* __restrict__ conn, const double* __restrict__ perm,
+                       const double* __restrict__ ecenter, const double* __restrict__ iarea,
+                       const double* __restrict__ icenter, const double* __restrict__ inormal, int* md_ptr, int* md_el,
+                       double* md_k) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c == 0) md_ptr[g.nconn] = 2 * g.nconn;
+  if (c >= g.nconn) return;
+  const int ei = conn[2 * c], ej = conn[2 * c + 1];
+  int i, j, k;
+  el_ijk(g, ei, i, j, k);
+  const int nfe = g.dim == 3 ? 6 : 4;
+  int o = -1, oj = -1;
+  for (int q = 1; q < nfe; q += 2) {
+    int ne, no;
+    if (face_neighbour(g, i, j, k, q, ne, no) && ne == ej) {
+      o = q;
+      oj = no;
+      break;
+    }
+  }
+  const int is = ei * nfe + o, js = ej * nfe + oj;
+  auto mult_norm = [&](int el, V3 v) {
+    const double* K = perm + 6 * (int64_t)el;
+    const double xx = K[0], yy = K[1], zz = K[2], xy = K[3], xz = K[4], yz = K[5];
+    const double x = xx * v.x + xy * v.y + xz * v.z;
+    const double y = xy * v.x + yy * v.y + yz * v.z;
+    const double z = xz * v.x + yz * v.y + zz * v.z;
+    return sqrt(x * x + y * y + z * z);
+  };
+  const double Kin = mult_norm(ei, ld3(inormal, is));
+  const double Kjn = mult_norm(ej, ld3(inormal, js));
+  const double A = iarea[is];
+  double t = 0;
+  if (Kin != 0 && Kjn != 0)
+    t = Kin * Kjn * A /
+        (Kjn * vnorm(vsub(ld3(icenter, is), ld3(ecenter, ei))) + Kjn * vnorm(vsub(ld3(icenter, js), ld3(ecenter, ej))));
+  md_ptr[c] = 2 * c;
+  md_el[2 * c] = ei;
+  md_k[2 * c] = t * 1.0;  // connection multiplier (1 on structured grids)
+  md_el[2 * c + 1] = ej;
+  md_k[2 * c + 1] = -t * 1.0;
+}
+
+// Adjoint of the TPFA transmissibilities: t_c = ||K_here n|| A / (d_here + d_there)
+// (||K_there n|| cancels), so d t_c / d log K_here = t_c and the there side
+// has no derivative: out[e] (+)= scale * sum_k sum_{c here at e} mu_k,c F_k,c.
+__global__ void k_tpfa_adjoint(int nel, int nconn, int npairs, const int* __restrict__ cc,
+                               const int* __restrict__ ccount, const int* __restrict__ conn,
+                               const double* __restrict__ md_k, const double* __restrict__ mu,
+                               const double* __restrict__ phi, double scale, int accumulate, double* __restrict__ out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  double s = 0;
+  for (int a = 0; a < ccount[e]; ++a) {
+    const int code = cc[(int64_t)e * 6 + a];
+    if (code & 1) continue;  // there side
+    const int c = code >> 1;
+    const int t = conn[2 * c + 1];
+    for (int k = 0; k < npairs; ++k)
+      s += mu[(int64_t)k * nconn + c] * md_k[2 * c] * (phi[(int64_t)k * nel + e] - phi[(int64_t)k * nel + t]);
+  }
+  out[e] = (accumulate ? out[e] : 0.0) + scale * s;
+}
+
 __device__ int bsearch_pos(const int* col, int lo, int hi, int key) {
   hi -= 1;
   while (lo <= hi) {
@@ -920,6 +986,13 @@ void mpfa_adjoint(Mesh& m, int npairs, const double* mu, const double* phi, doub
   if (!m.have_md) throw Error(RSG_BAD_ARG, "transmissibilities have not been computed");
   Context& c = *m.ctx;
   const Grid& g = m.g;
+  if (m.tpfa) {
+    RSG_LAUNCH(c, "tpfa_adjoint", k_tpfa_adjoint, blocks_for(g.nel, 128), 128, 0, g.nel, g.nconn, npairs,
+               m.cell_conn.get(), m.cell_conn_ptr.get(), m.conn.get(), m.md_k.get(), mu, phi, scale,
+               accumulate ? 1 : 0, out);
+    c.sync();
+    return;
+  }
   DeviceBuffer<double> corner((size_t)g.nel * 8);
   DeviceBuffer<int> flag(1);
   RSG_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), c.stream));
@@ -1080,6 +1153,33 @@ rsg_status rsg_mesh_compute_mpfa(rsg_mesh* mh, double continuity) {
                              c.stream));
     c.sync();
     m.have_md = true;
+    m.tpfa = false;
+    m.build_patterns();
+  });
+}
+
+rsg_status rsg_mesh_compute_tpfa(rsg_mesh* mh) {
+  if (!mh) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  return guarded(m.ctx, [&] {
+    rsg::Context& c = *m.ctx;
+    const rsg::Grid& g = m.g;
+    m.nmd = 2 * (int64_t)g.nconn;
+    m.md_ptr.resize(g.nconn + 1);
+    m.md_elem.resize(std::max<int64_t>(m.nmd, 1));
+    m.md_k.resize(std::max<int64_t>(m.nmd, 1));
+    RSG_LAUNCH(c, "tpfa", rsg::k_tpfa, rsg::blocks_for(std::max(g.nconn, 1), 128), 128, 0, g, m.conn.get(),
+               m.perm.get(), m.ecenter.get(), m.iarea.get(), m.icenter.get(), m.inormal.get(), m.md_ptr.get(),
+               m.md_elem.get(), m.md_k.get());
+    m.h_md_ptr.resize(g.nconn + 1);
+    m.h_md_elem.resize(m.nmd);
+    RSG_CUDA(cudaMemcpyAsync(m.h_md_ptr.data(), m.md_ptr.get(), sizeof(int) * (g.nconn + 1), cudaMemcpyDeviceToHost,
+                             c.stream));
+    RSG_CUDA(cudaMemcpyAsync(m.h_md_elem.data(), m.md_elem.get(), sizeof(int) * m.nmd, cudaMemcpyDeviceToHost,
+                             c.stream));
+    c.sync();
+    m.have_md = true;
+    m.tpfa = true;
     m.build_patterns();
   });
 }

@@ -209,3 +209,24 @@ def test_potential_adjoint_matches_gpu_fd_and_autograd(ctx):
         jp = w @ _gpu_forward(ctx, case, _scaled(perm, e, H))[3]
         jm = w @ _gpu_forward(ctx, case, _scaled(perm, e, -H))[3]
         assert abs((jp - jm) / (2 * H) - grad[e]) <= 2e-6 * np.max(np.abs(grad))
+
+
+def test_tpfa_transmissibility_adjoint_matches_fd(ctx):
+    dim, ni, nj, nk, n, perm, coords = _case("3d_6x5x4")
+    gm = api.Mesh(ctx, dim, ni, nj, nk, perm, coords=coords)
+    gm.compute_tpfa()
+    nconn = gm.counts()["connections"]
+    g = np.random.Generator(np.random.PCG64(12))
+    mu = g.standard_normal((2, nconn))
+    phi = g.standard_normal((2, n)) * 1e5
+    grad = gm.transmissibility_adjoint(mu, phi)
+    scale = np.max(np.abs(grad))
+    for e in g.choice(n, size=12, replace=False):
+        vals = []
+        for s in (H, -H):
+            om = O.Mesh(dim, ni, nj, nk, coords=coords, perm=_scaled(perm, e, s))
+            om.mpfa(tpfa=True)
+            ptr, el, kk = om.transmissibilities()
+            vals.append(sum(_flux_functional(ptr, el, kk, mu[k], phi[k]) for k in range(2)))
+        fd = (vals[0] - vals[1]) / (2 * H)
+        assert abs(fd - grad[e]) <= 1e-6 * scale + 1e-6 * abs(fd), (e, fd, grad[e])
