@@ -478,11 +478,6 @@ __global__ void k_gm_xupdate(int n, double* __restrict__ x, const double* __rest
 
 __global__ void k_iter_inc(KState* s) { s->iter++; }
 
-__global__ void k_copy_vec(int n, const double* __restrict__ a, double* __restrict__ b) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = a[i];
-}
-
 // ---- FP32 inner BiCGstab for the mixed-precision solver.  Vectors and the
 // preconditioner are FP32; dot products accumulate in FP64 and the scalar
 // recurrences (KState) stay FP64.

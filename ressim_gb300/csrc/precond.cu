@@ -52,7 +52,7 @@ __device__ __forceinline__ void sweep_row(const SweepArgs<T>& a, int slot, int r
   const int base = a.slice_base[s] + (slot & 31);
   const int len = a.len[slot];
   T sum = 0;
-  if (KIND == SW_SSOR_FWD || KIND == SW_SSOR_BWD) {
+  if constexpr (KIND == SW_SSOR_FWD || KIND == SW_SSOR_BWD) {
     // sigma over the full row without the diagonal, CSR order; lower
     // columns read the half iterate xx, upper columns read x.
 #pragma unroll 4
@@ -71,15 +71,15 @@ __device__ __forceinline__ void sweep_row(const SweepArgs<T>& a, int slot, int r
       T xh = ld_l2(a.xx + row);
       st_l2(a.x + row, xh + a.omega * (sigma - xh));
     }
-    return;
-  }
+  } else {
 #pragma unroll 4
-  for (int k = 0; k < len; ++k) {
-    int q = base + 32 * k;
-    sum += a.val[q] * ld_l2(a.x + a.col[q]);
+    for (int k = 0; k < len; ++k) {
+      int q = base + 32 * k;
+      sum += a.val[q] * ld_l2(a.x + a.col[q]);
+    }
+    if (KIND == SW_ILU_LOWER) st_l2(a.x + row, a.b[row] - sum);
+    else st_l2(a.x + row, (a.b[row] - sum) / a.diag[slot]);
   }
-  if (KIND == SW_ILU_LOWER) st_l2(a.x + row, a.b[row] - sum);
-  else st_l2(a.x + row, (a.b[row] - sum) / a.diag[slot]);
 }
 
 // One cluster walks all levels.  Every CTA of the cluster evaluates the same
