@@ -166,8 +166,35 @@ def run_resgpu(args, rank, world, local_rank):
 
     # end to end through the public API with page-locked host staging
     nc = sim.nc
-    if args.no_e2e:
-        return finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, None, rank)
+    e2e = None if args.no_e2e else e2e_pass(args, ctx, sim, n, nc, dt, world)
+    res = finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, e2e, rank)
+    # the secondary legs report their failure instead of ending the run
+    def leg(name, fn):
+        try:
+            res[name] = fn()
+        except Exception as e:  # noqa: BLE001
+            res[name] = {"error": f"{type(e).__name__}: {e}"}
+
+    if args.mixed_steps > 0:
+        leg("mixed", lambda: mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, sim, n, dt, res["ms_per_step"],
+                                       world))
+    if args.ensemble > 0 and rank == 0:
+        leg("ensemble", lambda: ensemble_leg(args))
+    if args.flash_cells > 0 and rank == 0:
+        leg("flash", lambda: flash_leg(args))
+    if args.comp_steps > 0 and rank == 0:
+        leg("compositional", lambda: compositional_leg(args))
+    if args.adj_steps > 0:
+        leg("adjoint", lambda: adjoint_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world))
+    return res
+
+
+def e2e_pass(args, ctx, sim, n, nc, dt, world):
+    """The timed steps again through the public API with the state staged
+    through page-locked host memory every step (host -> device before the
+    step, device -> host after it)."""
+    from ressim_gb300 import api
+
     hp = api.PinnedArray(n)
     hN = api.PinnedArray(nc * n)
     hS = api.PinnedArray(3 * n)
@@ -190,27 +217,7 @@ def run_resgpu(args, rank, world, local_rank):
     e2e_units = sum_over_ranks(float(n) * e2e_newton, world)
     h2d = (1 + nc) * n * 8
     d2h = (1 + nc + 3) * n * 8
-    e2e = {"value": e2e_units / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
-    res = finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, e2e, rank)
-    # the secondary legs report their failure instead of ending the run
-    def leg(name, fn):
-        try:
-            res[name] = fn()
-        except Exception as e:  # noqa: BLE001
-            res[name] = {"error": f"{type(e).__name__}: {e}"}
-
-    if args.mixed_steps > 0:
-        leg("mixed", lambda: mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, sim, n, dt, res["ms_per_step"],
-                                       world))
-    if args.ensemble > 0 and rank == 0:
-        leg("ensemble", lambda: ensemble_leg(args))
-    if args.flash_cells > 0 and rank == 0:
-        leg("flash", lambda: flash_leg(args))
-    if args.comp_steps > 0 and rank == 0:
-        leg("compositional", lambda: compositional_leg(args))
-    if args.adj_steps > 0:
-        leg("adjoint", lambda: adjoint_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world))
-    return res
+    return {"value": e2e_units / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
 
 def adjoint_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world):
@@ -274,15 +281,33 @@ def mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, fp64_sim, n, dt, fp6
     p, N, _ = sim.state()
     sim.set_state(p, N)
     fp64_sim.set_state(p, N)
+    # the comparison step is also the event-profiled one (per-kernel times)
+    ctx.set_profiling(True)
+    ctx.profile_reset()
     sim.step(dt)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
     fp64_sim.step(dt)
     pm = sim.state()[0]
     pd = fp64_sim.state()[0]
     ms = dev_s * 1e3 / args.mixed_steps
+    # FP32 SpMV of the inner solver: 4 B value + 4 B column per entry, row
+    # length, x, y and the dot operand per row
+    rp, col = mesh.pattern(0)
+    f32_bytes = 8 * len(col) + 16 * n
+    hbm, peak_kind = peaks()
+    inner = None
+    if "inner_spmv_dot" in prof:
+        t_ms, cnt = prof["inner_spmv_dot"]
+        gbs = f32_bytes / (t_ms / cnt / 1e3) / 1e9
+        inner = {"kernel": "k_f32_spmv_dot", "launches": cnt, "avg_launch_us": round(t_ms / cnt * 1e3, 2),
+                 "bytes_per_launch": f32_bytes, "achieved_gbs": round(gbs, 1), "peak": hbm,
+                 "frac": round(gbs / hbm, 4), "peak_source": peak_kind}
     return {"value": units / dev_s, "unit": METRIC, "ms_per_step": ms, "steps": args.mixed_steps,
             "speedup_vs_fp64_per_step": fp64_ms / ms, "newton_iterations": newton, "outer_iterations": linear,
             "inner": {"iterations": int(args.inner[0]), "rtol": args.inner[1]},
-            "max_rel_pressure_diff_vs_fp64": float(np.max(np.abs(pm - pd) / np.abs(pd)))}
+            "max_rel_pressure_diff_vs_fp64": float(np.max(np.abs(pm - pd) / np.abs(pd))),
+            "inner_spmv": inner}
 
 
 def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, e2e, rank=0):
