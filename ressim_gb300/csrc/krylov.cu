@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(RT) k_resid(int n, const int* __restrict__ sb,
 // The Krylov iterates therefore differ from MTJ's in the last bits, within
 // the solver parity bound; rsg_csr_mult keeps MTJ's unfused arithmetic.
 template <int K>
-__global__ void __launch_bounds__(RT) k_spmv_dot(int n, const int* __restrict__ sb, const int* __restrict__ rl,
+__global__ void __launch_bounds__(RT, 8) k_spmv_dot(int n, const int* __restrict__ sb, const int* __restrict__ rl,
                                                  const int* __restrict__ col, const double* __restrict__ val,
                                                  const double* __restrict__ x, double* __restrict__ y,
                                                  const double* __restrict__ w, RedArgs ra, int epi) {
@@ -523,7 +523,7 @@ __global__ void k_f32_bicg_p(int n, const float* __restrict__ r, const float* __
 }
 
 template <int K>
-__global__ void __launch_bounds__(RT) k_f32_spmv_dot(int n, const int* __restrict__ sb, const int* __restrict__ rl,
+__global__ void __launch_bounds__(RT, 8) k_f32_spmv_dot(int n, const int* __restrict__ sb, const int* __restrict__ rl,
                                                      const int* __restrict__ col, const float* __restrict__ val,
                                                      const float* __restrict__ x, float* __restrict__ y,
                                                      const float* __restrict__ w, RedArgs ra, int epi) {
