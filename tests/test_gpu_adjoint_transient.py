@@ -6,12 +6,14 @@ differences of the GPU forward and of the oracle forward, with the objective
 
 Every difference quotient carries the forward run's own rounding: with the
 Newton and Krylov tolerances at 1e-13, J is reproducible to about 1e-12 |J|
-(GPU) to 1e-11 |J| (oracle) under a perturbation, i.e. that much over h in
-the quotient, and each check allows FD_NOISE * |J| / h for it.  At h = 1e-3 in log k that noise and the
-O(h^2) truncation are both near 1e-6 of the gradient, so that check is the
-tight one; at the step h = 1e-6 the noise is about 1e-6 |J|.  Measured on
-the 8 x 8 x 3 case: the adjoint agrees with h = 1e-4 differences to 5
-digits wherever the gradient is above 1e-2 of its largest entry."""
+(GPU) to a few 1e-11 |J| (oracle, and the GPU on 32 x 32 x 8) under a
+perturbation, i.e. that much over h in the quotient; each check allows
+FD_NOISE * |J| / h (h = 1e-3) or FD_NOISE_H * |J| / h (h = 1e-6) for it.  At
+h = 1e-3 in log k that noise and the O(h^2) truncation are both near 1e-6 of
+the gradient, so that check is the tight one; at the step h = 1e-6 the noise
+is a few 1e-5 |J|.  Measured on the 8 x 8 x 3 case: the adjoint agrees with
+h = 1e-4 differences to 5 digits wherever the gradient is above 1e-2 of its
+largest entry."""
 import numpy as np
 import pytest
 
@@ -23,8 +25,9 @@ pytestmark = pytest.mark.gpu
 
 H = 1e-6        # the check step
 H_FINE = 1e-3   # the accuracy step
-FD_NOISE = 2e-11
-TIGHT = dict(rtol=1e-13, ptol=1e-13, stop_rule=1, max_newton=60)
+FD_NOISE = 2e-11     # rounding of J under a perturbation, relative, at h = 1e-3
+FD_NOISE_H = 5e-11   # the same at h = 1e-6 (measured up to 2.4e-11 on 32 x 32 x 8)
+TIGHT = dict(rtol=1e-13, atol=1e-24, ptol=1e-13, stop_rule=1, max_newton=60)  # atol: a converged Newton leaves a zero right-hand side
 
 
 def _sim(ctx, case, perm, spec_kw=TIGHT):
@@ -91,7 +94,7 @@ def test_adjoint_gradient_matches_gpu_fd(ctx, nsteps):
         assert abs(fd - grad[e]) <= FD_NOISE * J / H_FINE + 1e-5 * scale, (e, fd, grad[e], scale)
         fd = (_objective(ctx, case, _scaled(case["perm"], e, H), dts) -
               _objective(ctx, case, _scaled(case["perm"], e, -H), dts)) / (2 * H)
-        assert abs(fd - grad[e]) <= FD_NOISE * J / H + 1e-4 * abs(fd), (e, fd, grad[e], J)
+        assert abs(fd - grad[e]) <= FD_NOISE_H * J / H + 1e-4 * abs(fd), (e, fd, grad[e], J)
 
 
 def test_adjoint_checkpointing_is_exact(ctx):
@@ -144,21 +147,42 @@ def test_adjoint_initial_state_sensitivity(ctx):
 
 
 def test_adjoint_gradient_matches_oracle_fd(ctx):
-    """Finite differences of the oracle forward on a 16 x 16 x 4 grid."""
-    case = _case(16, 16, 4)
-    dts = [case["dt"]] * 2
+    """Finite differences of the oracle forward on a 32 x 32 x 8 grid."""
+    case = _case(32, 32, 8)
+    dts = [case["dt"]]
     gs = _sim(ctx, case, case["perm"])
     J, _ = gs.forward(dts, 1, case["producer"], [0.0, 1.0])
     assert abs(J - _oracle_objective(case, case["perm"], dts)) <= 1e-9 * abs(J)
     grad, _, _, _ = gs.backward(rtol=1e-13)
     scale = np.max(np.abs(grad))
-    for e in _cells(case, 6, 13):
+    for e in _cells(case, 4, 13):
         fd = (_oracle_objective(case, _scaled(case["perm"], e, H_FINE), dts) -
               _oracle_objective(case, _scaled(case["perm"], e, -H_FINE), dts)) / (2 * H_FINE)
         assert abs(fd - grad[e]) <= FD_NOISE * J / H_FINE + 1e-5 * scale, (e, fd, grad[e], scale)
         fd = (_oracle_objective(case, _scaled(case["perm"], e, H), dts) -
               _oracle_objective(case, _scaled(case["perm"], e, -H), dts)) / (2 * H)
-        assert abs(fd - grad[e]) <= FD_NOISE * J / H + 1e-4 * abs(fd), (e, fd, grad[e], J)
+        assert abs(fd - grad[e]) <= FD_NOISE_H * J / H + 1e-4 * abs(fd), (e, fd, grad[e], J)
+
+
+def test_adjoint_gpu_fd_64_cells(ctx):
+    """Central differences with step 1e-6 of the GPU forward on 64 seeded
+    cells of a 32 x 32 x 8 grid (noise-bounded, see the module docstring)."""
+    case = _case(32, 32, 8)
+    dts = [case["dt"]]
+    gs = _sim(ctx, case, case["perm"])
+    J, _ = gs.forward(dts, 1, case["producer"], [0.0, 1.0])
+    grad, _, _, _ = gs.backward(rtol=1e-13)
+    n = case["ni"] * case["nj"] * case["nk"]
+    scale = np.max(np.abs(grad))
+    cells = np.random.Generator(np.random.PCG64(64)).choice(n, size=64, replace=False)
+    for q, e in enumerate(cells):
+        if q % 4 == 0:  # the tight step on every fourth cell
+            fd = (_objective(ctx, case, _scaled(case["perm"], e, H_FINE), dts) -
+                  _objective(ctx, case, _scaled(case["perm"], e, -H_FINE), dts)) / (2 * H_FINE)
+            assert abs(fd - grad[e]) <= FD_NOISE * J / H_FINE + 1e-5 * scale, (e, fd, grad[e], scale)
+        fd = (_objective(ctx, case, _scaled(case["perm"], e, H), dts) -
+              _objective(ctx, case, _scaled(case["perm"], e, -H), dts)) / (2 * H)
+        assert abs(fd - grad[e]) <= FD_NOISE_H * J / H + 1e-4 * abs(fd), (e, fd, grad[e], J)
 
 
 def test_adjoint_autograd_directional(ctx):
