@@ -245,7 +245,9 @@ rsg_status rsg_mesh_transmissibility_adjoint(rsg_mesh* m, int32_t npairs, const 
  *   dJ/dtheta_e = -sum_c (lambda~_here - lambda~_there) dF_c/dtheta_e,
  * lambda~ being lambda with the fixed rows zeroed and F_c = sum_m t_cm p_m
  * the connection flux.  lambda (may be NULL) receives the adjoint solution,
- * dJ_dlogk the gradient; info the transposed solve. */
+ * dJ_dlogk the gradient; info the transposed solve.  The solver is set up on
+ * A^T inside the call and left without a matrix: call rsg_solver_setup again
+ * before its next solve. */
 rsg_status rsg_potential_adjoint(rsg_mesh* m, rsg_solver* solver, rsg_csr* A, int32_t nfixed, const int32_t* fixed,
                                  const double* p, const double* dJdp, double* lambda, double* dJ_dlogk,
                                  rsg_solve_info* info);

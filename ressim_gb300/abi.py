@@ -30,6 +30,9 @@ STATUS = {
     14: "SINGULAR",
     15: "PHYSICS",
 }
+(OK, NOT_CONVERGED_ITERATIONS, NOT_CONVERGED_DIVERGENCE, NOT_CONVERGED_BREAKDOWN, ZERO_PIVOT, MISSING_DIAGONAL,
+ OUT_OF_PATTERN, NONPOSITIVE_PRESSURE, NEGATIVE_MOLES, BAD_ARG, CUDA_ERROR, TIMEOUT, UNSUPPORTED,
+ NEWTON_NOT_CONVERGED, SINGULAR, PHYSICS) = range(16)
 
 CG, BICGSTAB, GMRES, FGMRES_MIXED = 0, 1, 2, 3
 PC_NONE, PC_DIAGONAL, PC_ILU, PC_SSOR, PC_AMG = 0, 1, 2, 3, 4

@@ -75,6 +75,11 @@ rsg_status rsg_potential_adjoint(rsg_mesh* mh, rsg_solver* solver, rsg_csr* A, i
     RSG_CUDA(cudaMemcpyAsync(w.get(), dJdp, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
     RSG_CUDA(cudaMemcpyAsync(dmask.get(), mask.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
     RSG_CUDA(cudaMemsetAsync(lam.get(), 0, sizeof(double) * n, c.stream));
+    // the transpose lives only for this call: the solver must not keep it
+    struct Forget {
+      rsg::Solver& s;
+      ~Forget() { rsg::solver_forget_matrix(s); }
+    } forget{*solver->s};
     rsg::solver_setup(*solver->s, tr.AT);
     rsg::solver_solve(*solver->s, tr.AT, w.get(), lam.get(), info);
     RSG_LAUNCH(c, "conn_difference", rsg::k_conn_difference, rsg::blocks_for(m.g.nconn, 256), 256, 0, m.g.nconn,

@@ -895,6 +895,8 @@ SolverPtr make_solver(Context* ctx, int method, int precond, double rtol, double
   return s;
 }
 
+void solver_forget_matrix(Solver& s) { s.setup_for = nullptr; }
+
 void solver_setup(Solver& s, Csr& A) {
   s.pc->setup(A);
   s.setup_for = &A;

@@ -101,6 +101,8 @@ SolverPtr make_solver(Context* ctx, int method, int precond, double rtol, double
 void solver_setup(Solver& s, Csr& A);
 void solver_solve(Solver& s, Csr& A, const double* b, double* x, rsg_solve_info* info);
 void solver_set_inner(Solver& s, int iterations, double rtol);
+// the solver no longer refers to the matrix of its last setup (rsg_solver_setup is needed again)
+void solver_forget_matrix(Solver& s);
 
 // Explicit transpose of a CSR matrix with a fixed position map: the pattern
 // of A^T is built on the host once per pattern of A, after which update()

@@ -1787,6 +1787,18 @@ struct Sim {
     if (info) *info = in;
   }
 
+  // after a failed backward sweep: the simulator returns to the end of the
+  // forward run (the record stays usable); errors here are not reported over
+  // the original one
+  void abandon_backward() {
+    try {
+      if (adj_ready) unsnap(adj_end);
+      blk_first = -1;
+      ctx->sync();
+    } catch (...) {
+    }
+  }
+
   void copy_ptr(const double* a, double* b, int64_t count) {
     RSG_LAUNCH(*ctx, "copy", k_copy, blocks_for(count, 256), 256, 0, count, a, b);
   }
@@ -2139,7 +2151,14 @@ rsg_status rsg_sim_forward(rsg_sim* s, int32_t nsteps, const double* dt, int32_t
 rsg_status rsg_sim_backward(rsg_sim* s, double rtol, double* dJ_dlogk, double* dJ_dp0, double* dJ_dN0,
                             rsg_adjoint_info* info) {
   if (!s || !dJ_dlogk || !(rtol > 0)) return RSG_BAD_ARG;
-  return guarded(s->s->ctx, [&] { s->s->backward(rtol, dJ_dlogk, dJ_dp0, dJ_dN0, info); });
+  return guarded(s->s->ctx, [&] {
+    try {
+      s->s->backward(rtol, dJ_dlogk, dJ_dp0, dJ_dN0, info);
+    } catch (...) {
+      s->s->abandon_backward();  // back to the end of the forward run, then report
+      throw;
+    }
+  });
 }
 
 rsg_status rsg_sim_retract(rsg_sim* s) {

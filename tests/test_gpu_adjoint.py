@@ -230,3 +230,18 @@ def test_tpfa_transmissibility_adjoint_matches_fd(ctx):
             vals.append(sum(_flux_functional(ptr, el, kk, mu[k], phi[k]) for k in range(2)))
         fd = (vals[0] - vals[1]) / (2 * H)
         assert abs(fd - grad[e]) <= 1e-6 * scale + 1e-6 * abs(fd), (e, fd, grad[e])
+
+
+def test_potential_adjoint_releases_the_solver(ctx):
+    """The transposed system exists only inside the call: afterwards the
+    solver has no matrix and asks for rsg_solver_setup again."""
+    case, perm = _potential_problem(ctx, 12, 10)
+    gm, A, s, p = _gpu_forward(ctx, case, perm, rtol=1e-12)
+    w = np.ones(len(p))
+    gm.potential_adjoint(s, A, case["dirichlet_cells"], p, w)
+    with pytest.raises(api.RSGError) as e:
+        s.solve(A, W.potential_rhs(case), np.zeros(len(p)))
+    assert e.value.status == abi.BAD_ARG
+    s.set_matrix(A)
+    x = s.solve(A, W.potential_rhs(case), np.zeros(len(p)))
+    assert np.max(np.abs(x - p)) <= 1e-9 * np.max(np.abs(p))

@@ -218,3 +218,29 @@ def test_adjoint_autograd_directional(ctx):
     jm = _objective(ctx, case, case["perm"] * np.exp(-H_FINE * v)[:, None], dts)
     fd = (jp - jm) / (2 * H_FINE)
     assert abs(fd - grad @ v) <= FD_NOISE * float(J.detach()) / H_FINE + 1e-5 * np.linalg.norm(grad) * np.linalg.norm(v)
+
+
+def test_adjoint_contract(ctx):
+    """Backward needs a recorded forward run; a second backward gives the same
+    gradient; fluids with a cubic equation of state are refused."""
+    case = _case()
+    gs = _sim(ctx, case, case["perm"])
+    with pytest.raises(api.RSGError) as e:
+        gs.backward()
+    assert e.value.status == abi.BAD_ARG
+    dts = [case["dt"]] * 2
+    gs.forward(dts, 1, case["producer"], [0.0, 1.0])
+    g1 = gs.backward(rtol=1e-13)[0]
+    g2 = gs.backward(rtol=1e-13)[0]
+    assert np.array_equal(g1, g2)
+    keep = abi.Keep()
+    f = W.compositional_fluid(keep)
+    cc = W.compositional_case(6, 6, 2, dt=2000.0)
+    m = api.Mesh(ctx, 3, 6, 6, 2, cc["perm"], coords=cc["nodes"])
+    m.compute_mpfa()
+    cs = api.Discretisation(ctx, m, f, W.corey(), cc["porosity"], cc["compaction"],
+                            W.build_compositional_sources(keep, cc, f.nc), W.build_compositional_initial(cc, f.nc),
+                            W.runspec())
+    with pytest.raises(api.RSGError) as e:
+        cs.forward([2000.0], 1, [0], [1.0])
+    assert e.value.status == abi.UNSUPPORTED
