@@ -122,8 +122,13 @@ inline void check_launch(const char* what) {
   if (e != cudaSuccess) throw Error(RSG_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// an empty grid (nothing to do, e.g. a mesh without connections) launches nothing
+inline bool grid_empty(int g) { return g <= 0; }
+inline bool grid_empty(const dim3& g) { return g.x == 0 || g.y == 0 || g.z == 0; }
+
 #define RSG_LAUNCH(ctx, name, kernel, grid, block, smem, ...)                    \
   do {                                                                           \
+    if (::rsg::grid_empty(grid)) break;                                          \
     ::rsg::LaunchScope scope_(ctx, name);                                        \
     kernel<<<(grid), (block), (smem), (ctx).stream>>>(__VA_ARGS__);              \
     ::rsg::check_launch(name);                                                   \
