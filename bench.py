@@ -381,12 +381,12 @@ def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, ne
 
 
 def ensemble_leg(args):
-    """Config-4-style ensemble: members with grids drawn uniformly between
-    32x32x8 and 96x96x24 and their own seeded permeability, each on its own
-    context; one rsg_ensemble_step steps all of them concurrently.  Reported
-    against stepping the same members one after another (plain FP64 path),
-    for FP64 members and for members with the mixed-precision pressure
-    solver (config 4's Krylov stack)."""
+    """Ensemble of two-phase realisations: members with grids drawn uniformly
+    between 32x32x8 and 96x96x24 and their own seeded permeability, each on
+    its own context; one rsg_ensemble_step steps all of them concurrently.
+    Reported against stepping the same members one after another (plain FP64
+    path), for FP64 members and for members with the mixed-precision
+    pressure solver."""
     from ressim_gb300 import api
 
     sizes = W.ensemble_sizes(args.ensemble)
