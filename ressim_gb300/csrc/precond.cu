@@ -289,6 +289,22 @@ __device__ __forceinline__ void push_value(unsigned remote, float v, unsigned rb
                : "memory");
 }
 
+// two neighbouring values (16 or 8 bytes) in one push: the even lane of a
+// lane pair sends its own and its odd neighbour's value, which halves the
+// number of transfers each receiving mbarrier counts
+__device__ __forceinline__ void push_pair(unsigned remote, double v0, double v1, unsigned rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b64 [%0], {%1, %2}, [%3];" ::"r"(remote),
+               "l"((unsigned long long)__double_as_longlong(v0)), "l"((unsigned long long)__double_as_longlong(v1)),
+               "r"(rbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void push_pair(unsigned remote, float v0, float v1, unsigned rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b32 [%0], {%1, %2}, [%3];" ::"r"(remote),
+               "r"(__float_as_uint(v0)), "r"(__float_as_uint(v1)), "r"(rbar)
+               : "memory");
+}
+
 template <int KIND, typename T, int MAXW>
 __device__ __forceinline__ void load_ring_coeffs(const SweepArgs<T>& a, const RingArgs& g, const int* ls,
                                                  const SlotMeta& m, int l, int gwarp, int lane,
@@ -372,7 +388,10 @@ __global__ void __launch_bounds__(RING_SLICES / RING_CTAS * 32) k_sweep_ring(Swe
         if (c != (int)rank)
           push_b64(cluster_addr(tok0, c) + RING_TOKEN_BYTES * rank, (unsigned long long)l, rbar[c] + 8 * slot_l);
     }
-    if (cur.row >= 0) {
+    const bool act = cur.row >= 0;
+    T v = 0;
+    const int own = slot_l * g.slot + gwarp * 32 + lane;
+    if (act) {
       T sum = 0;
 #pragma unroll
       for (int k = 0; k < MAXW; ++k)
@@ -381,14 +400,19 @@ __global__ void __launch_bounds__(RING_SLICES / RING_CTAS * 32) k_sweep_ring(Swe
         const int q = cur.base + 32 * k;
         sum += a.val[q] * ring[g.ridx[q]];
       }
-      const T v = (KIND == SW_ILU_LOWER) ? cur.b - sum : (cur.b - sum) / cur.d;
-      const int own = slot_l * g.slot + gwarp * 32 + lane;
+      v = (KIND == SW_ILU_LOWER) ? cur.b - sum : (cur.b - sum) / cur.d;
       ring[own] = v;
+      a.x[cur.row] = v;
+    }
+    // the even lane of each pair pushes both values (rows of a level are
+    // packed from its first slot, so a pair with an active odd lane has an
+    // active even lane; an unused odd slot is never read)
+    const T v_odd = __shfl_down_sync(0xffffffffu, v, 1);
+    if (act && !(lane & 1)) {
       const unsigned off = (unsigned)(own * sizeof(T)), boff = (unsigned)(8 * slot_l);
 #pragma unroll
       for (int c = 0; c < RING_CTAS; ++c)
-        if (c != (int)rank) push_value(rring[c] + off, v, rbar[c] + boff);
-      a.x[cur.row] = v;
+        if (c != (int)rank) push_pair(rring[c] + off, v, v_odd, rbar[c] + boff);
     }
     cur = nxt;
     m1 = m2;
@@ -677,11 +701,16 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
         auto& ex = expect[e];
         ex.assign((size_t)nlev * C, 0);
         for (int l = 0; l < nlev; ++l) {
-          int rows = cnt[l + 1] - cnt[l];
+          const int rows = cnt[l + 1] - cnt[l];
+          // values pushed by each CTA: its rows, rounded up to whole lane pairs
+          int total = 0;
+          std::vector<int> sent(C);
           for (int c = 0; c < C; ++c) {
-            int own = std::min(std::max(rows - c * W * 32, 0), W * 32);
-            ex[(size_t)l * C + c] = rows - own;
+            const int own = std::min(std::max(rows - c * W * 32, 0), W * 32);
+            sent[c] = 2 * ((own + 1) / 2);
+            total += sent[c];
           }
+          for (int c = 0; c < C; ++c) ex[(size_t)l * C + c] = total - sent[c];
         }
       }
     }
