@@ -88,3 +88,39 @@ def test_ilu_27pt_pipelined_walk_bitexact():
                        text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "mode 1 bitexact True" in r.stdout
+
+
+SCRIPT_CTAS = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r}); sys.path.insert(0, {tests!r})
+from test_gpu_sweeps import pattern27
+from oracle import oracle as O
+from ressim_gb300 import abi, api
+ctx = api.Context(0)
+rp, col, val = pattern27(48, 40, 12, seed=7)
+n = len(rp) - 1
+A = api.CompRowMatrix(ctx, n, rp, col, val)
+s = api.BiCGstab(ctx, abi.PC_ILU)
+s.set_matrix(A)
+b = np.random.Generator(np.random.PCG64(5)).standard_normal(n)
+_, xo = O.ilu(rp, col, val, b)
+ok64 = np.array_equal(s.apply(b), xo)
+m = api.MixedFGMRES(ctx, abi.PC_ILU, rtol=1e-10)  # FP32 level walks inside
+m.set_matrix(A)
+x = m.solve(A, b, np.zeros(n))
+res = np.linalg.norm(b - A.mult(x)) / np.linalg.norm(b)
+print("mode", api.lib().rsg_sweep_mode(), "fp64 bitexact", ok64, "fp32 residual", res)
+m.release(); s.release(); A.release(); ctx.close()
+sys.exit(0 if ok64 and res <= 1e-9 else 1)
+"""
+
+
+@pytest.mark.parametrize("ctas", ["8", "16"])
+def test_ring_walk_cluster_sizes(ctas):
+    """FP64 and FP32 walks on 8- and 16-CTA clusters, each with its table of
+    expected pushed values (values travel two at a time)."""
+    env = dict(os.environ, RSG_RING_CTAS=ctas)
+    r = subprocess.run([sys.executable, "-c", SCRIPT_CTAS.format(root=ROOT, tests=HERE)], env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "mode 2 fp64 bitexact True" in r.stdout, r.stdout
