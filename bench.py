@@ -112,7 +112,7 @@ def build_case(args):
 # DRAM bytes (read + write) per launch of the ILU(0) level walks, from one ncu
 # capture of this workload (profiles/ilu_sweep_ring_two_phase_128x128x32.md);
 # keyed by grid size and kernel family.
-NCU_TRAFFIC = {(128, 128, 32): {"ilu_lower": 91_904_000, "ilu_upper": 95_707_136}}
+NCU_TRAFFIC = {(128, 128, 32): {"ilu_lower": 91_788_288, "ilu_upper": 95_744_256}}
 
 
 def sweep_bytes(rp, col):
