@@ -248,6 +248,29 @@ def test_two_phase_mass_balance_and_retract():
     assert np.array_equal(p0, p2) and np.array_equal(N0, N2)
 
 
+def test_locked_cell_inflow_closes_the_balance():
+    """The moles flowing into the Fixed producer cells in a step (the
+    adjoint's objective, last_dn before the locks) close the component
+    balance: what left the other cells, plus the injected moles, went there."""
+    case, keep, m, sim = _two_phase(rtol=1e-12)
+    n = case["ni"] * case["nj"] * case["nk"]
+    locked = np.zeros(n, bool)
+    locked[case["producer"]] = True
+    injected = np.zeros(2)
+    injected[0] = case["q_water"] * sum(len(c) for c in case["injectors"])
+    for _ in range(2):
+        _, N_before, _ = sim.state()
+        sim.step(case["dt"])
+        _, N_after, _ = sim.state()
+        dn = sim.last_dn()
+        assert np.array_equal(N_after[:, locked], N_before[:, locked])  # locked cells keep their moles
+        into_locked = dn[:, locked].sum(axis=1)
+        change_elsewhere = (N_after - N_before)[:, ~locked].sum(axis=1)
+        balance = change_elsewhere + into_locked - case["dt"] * injected
+        assert np.all(np.abs(balance) <= 1e-12 * N_before.sum(axis=1)), balance
+        assert into_locked[1] > 0  # oil is produced
+
+
 def test_newton_stop_rules():
     # RS stops when dp[0] < tol (signed, element 0; Discretisation.java:324);
     # the alternative rule uses max |dp/p|.
