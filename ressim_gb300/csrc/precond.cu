@@ -279,16 +279,6 @@ __device__ __forceinline__ void push_b64(unsigned remote, unsigned long long v, 
                : "memory");
 }
 
-__device__ __forceinline__ void push_value(unsigned remote, double v, unsigned rbar) {
-  push_b64(remote, (unsigned long long)__double_as_longlong(v), rbar);
-}
-
-__device__ __forceinline__ void push_value(unsigned remote, float v, unsigned rbar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(remote),
-               "r"(__float_as_uint(v)), "r"(rbar)
-               : "memory");
-}
-
 // two neighbouring values (16 or 8 bytes) in one push: the even lane of a
 // lane pair sends its own and its odd neighbour's value, which halves the
 // number of transfers each receiving mbarrier counts
