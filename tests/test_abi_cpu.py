@@ -67,3 +67,49 @@ def test_context_fails_loudly_without_gpu(lib):
         lib.rsg_context_destroy(h)
         pytest.skip("a GPU is present")
     assert st == 10  # RSG_CUDA_ERROR
+
+
+def test_status_codes_match_the_header(lib):
+    from ressim_gb300 import abi
+
+    text = open(HEADER).read()
+    start = text.index("RSG_OK = 0")
+    block = text[start:text.index("};", start)]  # the status enum
+    codes = {int(v): k for k, v in re.findall(r"\bRSG_(\w+)\s*=\s*(\d+)", block)}
+    assert codes == abi.STATUS
+    lib.rsg_status_string.restype = C.c_char_p
+    for code, name in abi.STATUS.items():
+        assert getattr(abi, name) == code
+        assert lib.rsg_status_string(code).decode() == name
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes structure in ressim_gb300.abi has the size and field
+    offsets of the C struct of the same name (compiled against rsg.h)."""
+    from ressim_gb300 import abi
+
+    structs = {n: t for n, t in vars(abi).items()
+               if n.startswith("rsg_") and isinstance(t, type) and issubclass(t, C.Structure)}
+    assert "rsg_adjoint_info" in structs and "rsg_runspec" in structs
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "rsg.h"', "int main(void) {"]
+    for name, t in sorted(structs.items()):
+        lines.append(f'  printf("{name} size %zu\\n", sizeof({name}));')
+        for f in t._fields_:  # a trailing "_" avoids a Python keyword (lambda_)
+            lines.append(f'  printf("{name} {f[0]} %zu\\n", offsetof({name}, {f[0].rstrip("_")}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            name, field, value = line.split()
+            got[(name, field)] = int(value)
+    for name, t in structs.items():
+        assert got[(name, "size")] == C.sizeof(t), name
+        for f in t._fields_:
+            assert got[(name, f[0])] == getattr(t, f[0]).offset, (name, f[0])
