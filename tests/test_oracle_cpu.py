@@ -288,3 +288,34 @@ def test_nonpositive_pressure_is_reported():
     # makes Newton fail; either way a SolverFailure status comes back
     with pytest.raises(O.OracleError):
         sim.step(1e12)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_two_point_values_on_an_orthogonal_grid(dim):
+    """On a uniform grid with a diagonal K, TPFA gives t = K A / d for every
+    connection (TPFA.java:50-72), and MPFA-O reduces to the same two-point
+    flux: the here / there entries are +-t and the others vanish."""
+    ni, nj, nk = (5, 4, 3) if dim == 3 else (5, 4, 0)
+    dx, dy, dz = 2.0, 3.0, -0.5
+    n = ni * nj * (nk if dim == 3 else 1)
+    K = np.tile([4.0, 9.0, 1.0, 0.0, 0.0, 0.0], (n, 1))
+    conn = None
+    for tpfa in (True, False):
+        m = O.Mesh(dim, ni, nj, nk, perm=K, dx=dx, dy=dy, dz=dz)
+        m.mpfa(tpfa=tpfa)
+        ptr, el, kk = m.transmissibilities()
+        conn = m.connections()
+        for c, (h, t) in enumerate(conn):
+            # direction of the connection from the element indices
+            d = t - h
+            if d == 1:
+                expect = K[h, 0] * (abs(dy) * (abs(dz) if dim == 3 else 1.0)) / dx
+            elif d == ni:
+                expect = K[h, 1] * (dx * (abs(dz) if dim == 3 else 1.0)) / dy
+            else:
+                expect = K[h, 2] * (dx * dy) / abs(dz)
+            entries = dict(zip(el[ptr[c]:ptr[c + 1]], kk[ptr[c]:ptr[c + 1]]))
+            assert abs(entries[h] - expect) <= 1e-12 * expect, (tpfa, c, entries, expect)
+            assert abs(entries[t] + expect) <= 1e-12 * expect
+            others = [v for e, v in entries.items() if e not in (h, t)]
+            assert all(abs(v) <= 1e-12 * expect for v in others)
