@@ -393,6 +393,13 @@ int orc_cubic_phase_state(const rsg_cubic_fluid* fl, int n, const double* p, con
 
 double orc_sim_time(void* h) { return ((Simulator*)h)->time; }
 
+// util/Function.get (nd < 0) or deriv(nd, x) at m points x (m x dim, row major)
+int orc_function_eval(const rsg_function* f, int nd, int m, const double* x, double* out) {
+  Function fn(*f);
+  for (int i = 0; i < m; ++i) out[i] = nd < 0 ? fn.get(x + (size_t)i * f->dim) : fn.deriv(nd, x + (size_t)i * f->dim);
+  return 0;
+}
+
 // the last step's molar changes before the locks (nc * n)
 int orc_sim_last_dn(void* h, double* dN) {
   Simulator* s = (Simulator*)h;

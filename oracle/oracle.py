@@ -67,6 +67,7 @@ def _declare(L):
     L.orc_sim_time.restype = d
     L.orc_sim_time.argtypes = [vp]
     L.orc_sim_last_dn.argtypes = [vp, P(d)]
+    L.orc_function_eval.argtypes = [P(abi.rsg_function), i, i, P(d), P(d)]
     L.orc_sim_calculate_dt.argtypes = [vp, d, P(abi.rsg_dt_control), P(d), P(abi.rsg_dt_factors)]
     L.orc_sim_throughput_factor.restype = d
     L.orc_sim_throughput_factor.argtypes = [vp, P(abi.rsg_dt_control)]
@@ -247,6 +248,14 @@ class Mesh:
         col = np.zeros(nnz.value, dtype=np.int32)
         lib().orc_mesh_pattern(self.h, which, abi.iptr(rp), abi.iptr(col), C.byref(nnz))
         return rp, col
+
+
+def function_eval(fn, x, nd=-1):
+    """util/Function.get (nd < 0) or deriv(nd, ...) at the rows of x (m x dim)."""
+    x = np.ascontiguousarray(np.atleast_2d(x), dtype=np.float64)
+    out = np.zeros(len(x))
+    lib().orc_function_eval(C.byref(fn), nd, len(x), abi.dptr(x), abi.dptr(out))
+    return out
 
 
 def potential_matrix(mesh, rowptr, col):
