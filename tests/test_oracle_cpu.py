@@ -4,7 +4,8 @@ invariants (no GPU needed):
 * ILU(0) exactness on tri-/penta-diagonal matrices
   (mtj sparse/test/ILUTest.java, IncompleteFactorizationTest.java:40-76);
 * IterativeSolverTest: CG/BiCGstab/GMRES x {none, diagonal, ILU, SSOR}
-  recover x to 1e-4 (sparse/test/IterativeSolverTest.java:37-177);
+  recover x to 1e-4 (sparse/test/IterativeSolverTest.java:37-177), and
+  CGAMGTest's CG + AMG;
 * mesh self-tests (geometry/Mesh.java:393-416, 620-660) and Connection.check
   (geometry/Connection.java:80-107);
 * MPFA uniform-flow reproduction (geometry/flux/MPFA.java:246-283, 1e-6);
@@ -75,6 +76,26 @@ def test_iterative_solver_kat(method, pc):
             assert np.max(np.abs(x - xt)) < 1e-4
 
 
+def test_cg_amg_kat():
+    """CGAMGTest (sparse/test/CGAMGTest.java, SPDIterativeSolverTest.java:37-52):
+    CG preconditioned by AMG on SPD band matrices of the test's sizes
+    (n <= 50, bandwidth <= 10, diagonal shift 100) recovers x to 1e-4 on every
+    repeated solve."""
+    for seed in range(8):
+        g = np.random.Generator(np.random.PCG64(100 + seed))
+        n = int(g.integers(1, 51))
+        band = int(g.integers(0, min(10, n)))
+        A = rand_banded(n, band, 200 + seed, spd=True)
+        assert np.linalg.eigvalsh(A)[0] > 0
+        rp, col, val = csr_of(A)
+        xt = g.random(n)
+        b = A @ xt
+        for _ in range(5):
+            x, it, res, hist, st = O.solve(abi.CG, abi.PC_AMG, rp, col, val, b, g.random(n))
+            assert st == 0
+            assert np.max(np.abs(x - xt)) < 1e-4
+
+
 def test_monitor_failure_reasons():
     A = rand_banded(30, 3, 1, False)
     rp, col, val = csr_of(A)
@@ -84,6 +105,51 @@ def test_monitor_failure_reasons():
     _, _, _, _, st = O.solve(abi.CG, abi.PC_NONE, rp, col, val, np.full(30, np.nan), np.zeros(30),
                              raise_on_fail=False)
     assert st == 2  # NaN residual -> Reason.Divergence
+
+
+def test_comprow_vector_products():
+    """MatrixTest's vector products (matrix/test/MatrixTest.java:562-640) on
+    CompRowMatrix: mult, multAdd and transMult against the test's dense loops,
+    x and y left as given otherwise.  Per row the oracle adds the stored
+    entries in column order, the dense loop adds the same terms plus exact
+    zeros, so the two agree far inside the test's 1e-5."""
+    for seed in range(6):
+        g = np.random.Generator(np.random.PCG64(300 + seed))
+        n = int(g.integers(1, 51))
+        A = np.where(g.random((n, n)) < 0.3, g.standard_normal((n, n)), 0.0)
+        rp, col, val = csr_of(A)
+        x, y, alpha = g.standard_normal(n), g.standard_normal(n), g.random()
+        x0 = x.copy()
+        assert np.allclose(O.csr_op(0, rp, col, val, x), A @ x, rtol=1e-13, atol=1e-13)
+        assert np.allclose(O.csr_op(1, rp, col, val, x, y, alpha), y + alpha * (A @ x), rtol=1e-13, atol=1e-13)
+        assert np.allclose(O.csr_op(2, rp, col, val, x), A.T @ x, rtol=1e-13, atol=1e-13)
+        assert np.array_equal(x, x0)
+
+
+def test_zero_rows_semantics():
+    """Matrices.zeroRows (matrix/Matrices.java:631-652): the listed rows are
+    zeroed, their diagonal set to the given value, other rows untouched; a
+    listed row without a stored diagonal cannot take the value in a
+    CompRowMatrix and is reported."""
+    g = np.random.Generator(np.random.PCG64(7))
+    n = 12
+    A = np.where(g.random((n, n)) < 0.4, g.standard_normal((n, n)), 0.0)
+    A[np.arange(n), np.arange(n)] = 5.0
+    rp, col, val = csr_of(A)
+    rows = np.array([7, 0, 3, 3], np.int32)  # unsorted, with a repeat
+    out = O.zero_rows(rp, col, val, 2.5, rows)
+    B = A.copy()
+    B[[0, 3, 7]] = 0.0
+    B[[0, 3, 7], [0, 3, 7]] = 2.5
+    dense = np.zeros((n, n))
+    for i in range(n):
+        dense[i, col[rp[i]:rp[i + 1]]] = out[rp[i]:rp[i + 1]]
+    assert np.array_equal(dense, B)
+    assert len(out) == len(val)
+    A[4, 4] = 0.0
+    rp, col, val = csr_of(A)
+    with pytest.raises(O.OracleError):
+        O.zero_rows(rp, col, val, 1.0, [4])
 
 
 def test_dgesv_matches_numpy():
