@@ -292,3 +292,21 @@ def table(keep, coords, data):
     flat = keep.f64(data.reshape(-1, order="F"))
     f.data = dptr(flat)
     return f
+
+
+def even_table(keep, ranges, data):
+    """util/EvenLookupTable as its configuration gives it: per axis (xMin,
+    xMax) and data of shape (n0, n1, n2); the knots are xMin + j (xMax - xMin)
+    / (n - 1), summed one spacing at a time (EvenLookupTable.java:86-162)."""
+    f = rsg_function()
+    f.kind = FN_EVEN_TABLE
+    f.dim = len(ranges)
+    data = np.asarray(data, dtype=np.float64)
+    assert data.ndim == len(ranges)
+    for d, (lo, hi) in enumerate(ranges):
+        arr = keep.f64([lo, hi])
+        f.n[d] = data.shape[d]
+        f.coord[d] = dptr(arr)
+    flat = keep.f64(data.reshape(-1, order="F"))
+    f.data = dptr(flat)
+    return f

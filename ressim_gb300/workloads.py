@@ -113,10 +113,11 @@ def perturbed_nodes(ni, nj, nk, dx, dy, dz, frac, seed):
     return np.ascontiguousarray(pts)
 
 
-def two_phase_fluid(keep, p_range=(20 * BAR, 600 * BAR), n_p=64):
+def two_phase_fluid(keep, p_range=(20 * BAR, 600 * BAR), n_p=64, even=False):
     """Oil/water black-oil fluid: exponential compressibility tables for the
     molar densities (4e-5 /bar water, 1e-4 /bar oil), constant viscosities
-    (1 cP water, 5 cP oil), no gas component, no mass transfer."""
+    (1 cP water, 5 cP oil), no gas component, no mass transfer.  even=True
+    gives the density tables as EvenLookupTables over the same ranges."""
     p0 = 200 * BAR
     ps = np.linspace(p_range[0], p_range[1], n_p)
     Ts = np.array([250.0, 450.0])
@@ -131,12 +132,18 @@ def two_phase_fluid(keep, p_range=(20 * BAR, 600 * BAR), n_p=64):
     f.molecular_weight[1] = 0.2
     f.group[0] = 0
     f.group[1] = 1
-    f.water_density = abi.table(keep, [ps, Ts], xiw)
+    if even:
+        f.water_density = abi.even_table(keep, [p_range, (Ts[0], Ts[-1])], xiw)
+    else:
+        f.water_density = abi.table(keep, [ps, Ts], xiw)
     f.water_viscosity = abi.constant(1.0 * CENTIPOISE, 2)
     f.water_enthalpy = abi.constant(0.0, 2)
     f.bubble_point = abi.constant(0.0, 2)
     f.dew_point = abi.constant(0.0, 2)
-    f.oil_density = abi.table(keep, [ps, Cs, Ts], xio)
+    if even:
+        f.oil_density = abi.even_table(keep, [p_range, (Cs[0], Cs[-1]), (Ts[0], Ts[-1])], xio)
+    else:
+        f.oil_density = abi.table(keep, [ps, Cs, Ts], xio)
     f.gas_density = abi.constant(100.0, 3)
     f.oil_viscosity = abi.constant(5.0 * CENTIPOISE, 3)
     f.gas_viscosity = abi.constant(1.0e-5, 3)
