@@ -113,3 +113,40 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(name, "size")] == C.sizeof(t), name
         for f in t._fields_:
             assert got[(name, f[0])] == getattr(t, f[0]).offset, (name, f[0])
+
+
+# entry points that take no handle, or whose null-argument behaviour is not
+# RSG_BAD_ARG (checked separately below)
+_NO_HANDLE = {"rsg_abi_version", "rsg_sweep_mode", "rsg_status_string", "rsg_context_create", "rsg_host_free",
+              "rsg_context_last_error", "rsg_context_kernel_launches"}
+
+
+def test_null_arguments_are_rejected(lib):
+    """Every entry point that takes a handle or output pointer returns
+    RSG_BAD_ARG for null arguments (zero counts, zero tolerances) before it
+    touches the GPU, so a binding's mistakes surface as statuses, never as
+    crashes."""
+    from ressim_gb300 import abi, api
+
+    L = api.lib()
+    checked = []
+    for name in declared():
+        if name in _NO_HANDLE:
+            continue
+        f = getattr(L, name)
+        args = []
+        for t in f.argtypes:
+            if t in (C.c_int32, C.c_int64, C.c_size_t):
+                args.append(0)
+            elif t is C.c_double:
+                args.append(0.0)
+            else:
+                args.append(None)
+        if name == "rsg_ensemble_step":
+            args[0] = 1  # one member, given as a null array
+        assert f(*args) == abi.BAD_ARG, name
+        checked.append(name)
+    assert len(checked) >= 55
+    assert L.rsg_context_last_error(None) == b""
+    assert L.rsg_context_kernel_launches(None) == 0
+    assert L.rsg_host_free(None) == abi.OK
