@@ -96,6 +96,53 @@ def test_cg_amg_kat():
             assert np.max(np.abs(x - xt)) < 1e-4
 
 
+def poisson2d(m):
+    n = m * m
+    A = np.zeros((n, n))
+    for i in range(m):
+        for j in range(m):
+            k = i * m + j
+            A[k, k] = 4.0
+            for di, dj in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+                if 0 <= i + di < m and 0 <= j + dj < m:
+                    A[k, (i + di) * m + j + dj] = -1.0
+    return A
+
+
+def test_amg_single_level_is_dense_lu():
+    """A matrix too small to coarsen is solved by the coarsest level alone,
+    MTJ DenseLU.factor / solve / transSolve (AMG.java:269-271,333-342,
+    DenseLU.java:83-98,180-196): apply is A^-1 b and transApply A^-T b."""
+    for n in (1, 5, 17, 30):
+        A = rand_banded(n, 5, 400 + n, spd=False)
+        rp, col, val = csr_of(A)
+        m = O.AMG(rp, col, val)
+        assert m.levels() == 1
+        b = np.random.Generator(np.random.PCG64(n)).standard_normal(n)
+        assert np.allclose(m.apply(b, np.zeros(n)), np.linalg.solve(A, b), rtol=1e-12, atol=1e-14)
+        assert np.allclose(m.apply(b, np.zeros(n), trans=True), np.linalg.solve(A.T, b), rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("which", ["poisson", "banded"])
+def test_amg_vcycle_is_linear_and_trans_apply_is_its_adjoint(which):
+    """From a zero start the V-cycle (pre-smoothing, restriction, coarse LU,
+    prolongation, post-smoothing) is a linear map M, and transApply applies
+    its transpose: M(2 b1 - 3 b2) = 2 M b1 - 3 M b2 and <M b1, b2> =
+    <b1, M^T b2>, to rounding, on multi-level hierarchies."""
+    A = poisson2d(40) if which == "poisson" else rand_banded(400, 6, 7, spd=True)
+    n = len(A)
+    rp, col, val = csr_of(A)
+    m = O.AMG(rp, col, val)
+    assert m.levels() >= 2
+    g = np.random.Generator(np.random.PCG64(11))
+    b1, b2, z = g.standard_normal(n), g.standard_normal(n), np.zeros(n)
+    M1, M2 = m.apply(b1, z), m.apply(b2, z)
+    M12 = m.apply(2 * b1 - 3 * b2, z)
+    assert np.max(np.abs(M12 - (2 * M1 - 3 * M2))) <= 1e-13 * np.max(np.abs(M12))
+    T2 = m.apply(b2, z, trans=True)
+    assert abs(M1 @ b2 - b1 @ T2) <= 1e-12 * abs(M1 @ b2)
+
+
 def test_monitor_failure_reasons():
     A = rand_banded(30, 3, 1, False)
     rp, col, val = csr_of(A)
