@@ -47,6 +47,34 @@ def test_ilu_exact_band(penta):
         assert np.linalg.norm(b - A @ y) <= 1e-5
 
 
+def test_ilu0_matches_a_on_its_pattern():
+    """ILU(0) (sparse/ILU.java:64-140) on random patterns: the unit-lower L
+    and upper U it stores reproduce A on A's pattern ((LU)_ij = a_ij there),
+    apply is (LU)^-1 b and transApply (LU)^-T b."""
+    for seed in range(5):
+        g = np.random.Generator(np.random.PCG64(500 + seed))
+        n = 40
+        A = np.where(g.random((n, n)) < 0.15, g.standard_normal((n, n)), 0.0)
+        A[np.arange(n), np.arange(n)] = 6.0 + g.random(n)
+        rp, col, val = csr_of(A)
+        b = g.standard_normal(n)
+        LU, y = O.ilu(rp, col, val, b)
+        _, yt = O.ilu(rp, col, val, b, trans=True)
+        L, U = np.eye(n), np.zeros((n, n))
+        for i in range(n):
+            for q in range(rp[i], rp[i + 1]):
+                j = col[q]
+                if j < i:
+                    L[i, j] = LU[q]
+                else:
+                    U[i, j] = LU[q]
+        P = L @ U
+        mask = A != 0
+        assert np.allclose(P[mask], A[mask], rtol=1e-12, atol=1e-12)
+        assert np.allclose(y, np.linalg.solve(P, b), rtol=1e-11, atol=1e-12)
+        assert np.allclose(yt, np.linalg.solve(P.T, b), rtol=1e-11, atol=1e-12)
+
+
 def rand_banded(n, band, seed, spd):
     g = np.random.Generator(np.random.PCG64(seed))
     A = np.zeros((n, n))
