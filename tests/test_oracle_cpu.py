@@ -11,7 +11,12 @@ invariants (no GPU needed):
 * MPFA uniform-flow reproduction (geometry/flux/MPFA.java:246-283, 1e-6);
 * PotentialCalculator with a linear analytic potential (numerics/analytical/LinearX);
 * the netlib dense LU against numpy;
-* volume-balance initialisation and per-step mass balance of the two-phase step.
+* volume-balance initialisation and per-step mass balance of the two-phase step;
+* mathematical identities: ILU(0) reproduces A on its pattern, AMG's V-cycle
+  is linear with transApply its adjoint, Krylov methods terminate on a
+  degree-3 minimal polynomial, transmissibilities are homogeneous in K;
+* CompRowMatrix products and zeroRows (matrix/test/MatrixTest.java,
+  Matrices.java:631-652).
 """
 import numpy as np
 import pytest
@@ -505,3 +510,24 @@ def test_two_point_values_on_an_orthogonal_grid(dim):
             assert abs(entries[t] + expect) <= 1e-12 * expect
             others = [v for e, v in entries.items() if e not in (h, t)]
             assert all(abs(v) <= 1e-12 * expect for v in others)
+
+
+@pytest.mark.parametrize("scheme", ["mpfa", "tpfa"])
+def test_transmissibilities_are_homogeneous_in_k(scheme):
+    """Every term of the interaction-region system T = C A^-1 B - D
+    (geometry/flux/O_MPFA.java:131-239) and of the two-point value
+    (TPFA.java:50-72) carries K once, so scaling all permeabilities by c
+    scales every transmissibility by c and leaves the MD lists alone: exactly
+    for c = 4 (a power of two changes no rounding), to rounding for c = 3.
+    Perturbed 3D grid, full tensors."""
+    case = W.two_phase_case(ni=6, nj=5, nk=4, seed=3)
+    out = []
+    for c in (1.0, 4.0, 3.0):
+        m = O.Mesh(3, 6, 5, 4, coords=case["nodes"], perm=case["perm"] * c)
+        m.mpfa(tpfa=(scheme == "tpfa"))
+        out.append(m.transmissibilities())
+    for ptr_el in zip(out[0][:2], out[1][:2], out[2][:2]):
+        assert all(np.array_equal(ptr_el[0], a) for a in ptr_el[1:])
+    k1, k4, k3 = out[0][2], out[1][2], out[2][2]
+    assert np.array_equal(k4, 4.0 * k1)
+    assert np.max(np.abs(k3 - 3.0 * k1)) <= 4e-15 * np.max(np.abs(k1))
