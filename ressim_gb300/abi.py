@@ -240,14 +240,16 @@ def dptr(a):
     """Pointer to a contiguous float64 numpy array (or NULL for None)."""
     if a is None:
         return _dptr()
-    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError(f"expected a C-contiguous float64 array, got {a.dtype}")
     return a.ctypes.data_as(_dptr)
 
 
 def iptr(a):
     if a is None:
         return _iptr()
-    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    if a.dtype != np.int32 or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError(f"expected a C-contiguous int32 array, got {a.dtype}")
     return a.ctypes.data_as(_iptr)
 
 
@@ -284,7 +286,8 @@ def table(keep, coords, data):
     f.kind = FN_TABLE
     f.dim = len(coords)
     data = np.asarray(data, dtype=np.float64)
-    assert data.shape == tuple(len(c) for c in coords)
+    if data.shape != tuple(len(c) for c in coords):
+        raise ValueError(f"table data of shape {data.shape} does not match axes of {[len(c) for c in coords]} points")
     for d, c in enumerate(coords):
         arr = keep.f64(c)
         f.n[d] = len(arr)
@@ -302,7 +305,8 @@ def even_table(keep, ranges, data):
     f.kind = FN_EVEN_TABLE
     f.dim = len(ranges)
     data = np.asarray(data, dtype=np.float64)
-    assert data.ndim == len(ranges)
+    if data.ndim != len(ranges):
+        raise ValueError(f"table data has {data.ndim} axes, ranges give {len(ranges)}")
     for d, (lo, hi) in enumerate(ranges):
         arr = keep.f64([lo, hi])
         f.n[d] = data.shape[d]

@@ -239,7 +239,8 @@ class CompRowMatrix:
 
     def set_values(self, values):
         v = _f64(values)
-        assert len(v) == self.nnz
+        if len(v) != self.nnz:
+            raise ValueError(f"{len(v)} values for a pattern of {self.nnz} entries")
         self.ctx.check(lib().rsg_csr_set_values(self.h, abi.dptr(v)), "set_values")
 
     def get_values(self):

@@ -150,3 +150,23 @@ def test_null_arguments_are_rejected(lib):
     assert L.rsg_context_last_error(None) == b""
     assert L.rsg_context_kernel_launches(None) == 0
     assert L.rsg_host_free(None) == abi.OK
+
+
+def test_pointer_helpers_reject_wrong_arrays():
+    """Arrays handed to the C ABI are checked for type and layout even under
+    python -O."""
+    import numpy as np
+
+    from ressim_gb300 import abi
+
+    with pytest.raises(TypeError):
+        abi.dptr(np.zeros(3, np.float32))
+    with pytest.raises(TypeError):
+        abi.iptr(np.zeros(3, np.int64))
+    with pytest.raises(TypeError):
+        abi.dptr(np.zeros((4, 4))[:, 0])
+    keep = abi.Keep()
+    with pytest.raises(ValueError):
+        abi.table(keep, [np.arange(3.0)], np.zeros(4))
+    with pytest.raises(ValueError):
+        abi.even_table(keep, [(0.0, 1.0), (0.0, 1.0)], np.zeros(4))
