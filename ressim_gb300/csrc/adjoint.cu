@@ -61,6 +61,7 @@ rsg_status rsg_potential_adjoint(rsg_mesh* mh, rsg_solver* solver, rsg_csr* A, i
   return guarded(m.ctx, [&] {
     rsg::Context& c = *m.ctx;
     const int n = m.g.nel;
+    if (!m.have_md) throw rsg::Error(RSG_BAD_ARG, "transmissibilities have not been computed");
     if (A->m.n != n) throw rsg::Error(RSG_BAD_ARG, "matrix size differs from the mesh's element count");
     std::vector<int> mask(n, 0);
     for (int q = 0; q < nfixed; ++q) {
