@@ -213,34 +213,109 @@ def two_phase_case(ni=128, nj=128, nk=32, seed=1, perturb=0.1, corr_len=8.0, kz_
     )
 
 
+GAS_CONSTANT = 8.3145  # J/(mol K), util/Constants.java:23
+
+
+def three_phase_fluid(keep, p_range=(20 * BAR, 600 * BAR), n_p=64):
+    """Water, oil and gas black-oil fluid (one component per group): the
+    bubble point (gas fraction of a saturated oil) rises linearly from 0.05 at
+    20 bar to 0.40 at 600 bar, the dew point (oil fraction of a saturated gas)
+    is 0.02; oil molar density has 1e-4 /bar compressibility and rises with
+    dissolved gas (x(1 + C)), gas molar density is p / (0.9 R T) (x(1 + C / 2)
+    with vaporised oil); viscosities 1 cP water, 2 cP oil, 0.02 cP gas."""
+    p0 = 200 * BAR
+    ps = np.linspace(p_range[0], p_range[1], n_p)
+    Ts = np.array([250.0, 450.0])
+    Cs = np.array([0.0, 1.0])
+    xiw0, cw = 1000.0 / 0.01801528, 4.0e-5 / BAR
+    xio0, co = 800.0 / 0.2, 1.0e-4 / BAR
+    f = abi.rsg_blackoil()
+    f.nc = 3
+    for nu, (mw, grp) in enumerate(((0.01801528, 0), (0.2, 1), (0.02, 2))):
+        f.molecular_weight[nu] = mw
+        f.group[nu] = grp
+    f.water_density = abi.table(keep, [ps, Ts], np.repeat((xiw0 * np.exp(cw * (ps - p0)))[:, None], 2, axis=1))
+    f.water_viscosity = abi.constant(1.0 * CENTIPOISE, 2)
+    f.water_enthalpy = abi.constant(0.0, 2)
+    cb = 0.05 + 0.35 * (ps - p_range[0]) / (p_range[1] - p_range[0])
+    f.bubble_point = abi.table(keep, [ps, Ts], np.repeat(cb[:, None], 2, axis=1))
+    f.dew_point = abi.constant(0.02, 2)
+    P, C, T = np.meshgrid(ps, Cs, Ts, indexing="ij")
+    f.oil_density = abi.table(keep, [ps, Cs, Ts], xio0 * np.exp(co * (P - p0)) * (1.0 + C))
+    f.gas_density = abi.table(keep, [ps, Cs, Ts], P / (0.9 * GAS_CONSTANT * T) * (1.0 + 0.5 * C))
+    f.oil_viscosity = abi.constant(2.0 * CENTIPOISE, 3)
+    f.gas_viscosity = abi.constant(0.02 * CENTIPOISE, 3)
+    f.oil_enthalpy = abi.constant(0.0, 3)
+    f.gas_enthalpy = abi.constant(0.0, 3)
+    return f
+
+
+def three_phase_case(ni=12, nj=12, nk=4, seed=5, rate_m3_per_day=0.05, dt=8640.0):
+    """Water, oil and gas on the two-phase case's grid: a gas cap in the top
+    layer (hydrocarbons 99% gas: single-phase gas), undersaturated oil below
+    (12% gas against a 16% bubble point at 200 bar: single-phase oil), gas
+    injected in the four corner columns (two-phase oil/gas where it mixes
+    with the oil) and the Fixed producer column holding the oil zone's
+    composition."""
+    case = two_phase_case(ni=ni, nj=nj, nk=nk, seed=seed, dt=dt)
+    keep = abi.Keep()
+    T = case["temperature"]
+    xiw0, xio0 = 1000.0 / 0.01801528, 800.0 / 0.2
+    xig0 = 200 * BAR / (0.9 * GAS_CONSTANT * T)
+
+    def fractions(sw, zg, xi_hc):
+        nw, nhc = sw * xiw0, (1 - sw) * xi_hc
+        tot = nw + nhc
+        return nw / tot, (1 - zg) * nhc / tot, zg * nhc / tot
+
+    oil_zone = fractions(0.25, 0.12, xio0 * 1.12)
+    gas_cap = fractions(0.20, 0.99, xig0 * 1.005)
+    zs = [-(nk + 1.0), -1.0, -0.99, 1.0]
+    case["fraction_fns"] = [abi.table(keep, [zs], [o, o, g, g]) for o, g in zip(oil_zone, gas_cap)]
+    case["fractions"] = oil_zone
+    case["q"] = {2: rate_m3_per_day * xig0 / 86400.0}
+    case["keep"] = keep
+    return case
+
+
 def build_sources(keep, case):
+    """Regular sources at the injector columns (case["q"]: component -> mol/s
+    per cell, water by default) and a Fixed source at the producer column
+    holding case["fractions"]."""
     srcs = (abi.rsg_source * (len(case["injectors"]) + 1))()
+    rates = case.get("q", {0: case.get("q_water", 0.0)})
     for a, cells in enumerate(case["injectors"]):
         arr = keep.i32(cells)
         srcs[a].type = abi.SOURCE_REGULAR
         srcs[a].num_elements = len(arr)
         srcs[a].elements = abi.iptr(arr)
-        srcs[a].q[0] = case["q_water"]
+        for nu, q in rates.items():
+            srcs[a].q[nu] = q
     arr = keep.i32(case["producer"])
     last = len(case["injectors"])
     srcs[last].type = abi.SOURCE_FIXED
     srcs[last].num_elements = len(arr)
     srcs[last].elements = abi.iptr(arr)
     srcs[last].temperature = case["temperature"]
-    srcs[last].fraction[0] = case["fractions"][0]
-    srcs[last].fraction[1] = case["fractions"][1]
+    for nu, c in enumerate(case["fractions"]):
+        srcs[last].fraction[nu] = c
     return srcs
 
 
 def build_initial(case):
+    """Initial values: datum, constant temperature and per-component mole
+    fractions, constant or given as functions of depth (case["fraction_fns"])."""
     init = abi.rsg_initial()
     init.datum_depth = case["datum_depth"]
     init.datum_pressure = case["datum_pressure"]
     init.temperature = abi.constant(case["temperature"], 1)
-    init.fraction[0] = abi.constant(case["fractions"][0], 1)
-    init.fraction[1] = abi.constant(case["fractions"][1], 1)
-    for nu in range(2, abi.MAX_COMPONENTS):
-        init.fraction[nu] = abi.constant(0.0, 1)
+    fns = case.get("fraction_fns")
+    for nu in range(abi.MAX_COMPONENTS):
+        if fns is not None and nu < len(fns):
+            init.fraction[nu] = fns[nu]
+        else:
+            c = case["fractions"][nu] if nu < len(case["fractions"]) else 0.0
+            init.fraction[nu] = abi.constant(c, 1)
     return init
 
 

@@ -305,6 +305,37 @@ def test_even_lookup_tables_match_oracle(ctx):
     assert np.max(np.abs(gN - oN) / np.maximum(np.abs(oN), 1e-30)) <= 1e-10
 
 
+def _three_phase(ctx, spec_kw):
+    case = W.three_phase_case()
+    keep = abi.Keep()
+    fluid = W.three_phase_fluid(keep)
+    srcs = W.build_sources(keep, case)
+    init = W.build_initial(case)
+    spec = W.runspec(**spec_kw)
+    gm, om = _mpfa_pair(ctx, 3, 12, 12, 4, case["perm"], case["nodes"])
+    gs = api.Discretisation(ctx, gm, fluid, W.corey(), case["porosity"], case["compaction"], srcs, init, spec)
+    os_ = O.Simulator(om, fluid, W.corey(), case["porosity"], case["compaction"], srcs, init, spec)
+    return case, gm, gs, os_, keep
+
+
+def test_three_phase_black_oil_matches_oracle(ctx):
+    """Water, oil and gas (a single-phase gas cap over undersaturated oil, gas
+    injected at the corners): the volume-balanced initial state is bit-exact,
+    and a step of one unconverged Newton iteration (pressure tolerance 1e300)
+    overshoots the explicit molar update into negative moles in the same
+    element as the oracle (RS's MolarMassExplicit failure)."""
+    case, gm, gs, os_, keep = _three_phase(ctx, dict(ptol=1e300, rtol=1e-12))
+    for a, b in zip(gs.state(), os_.state()):
+        assert np.array_equal(a, b)
+    gs.enable_jacobian_capture()
+    with pytest.raises(api.RSGError) as ge:
+        gs.step(case["dt"])
+    with pytest.raises(O.OracleError) as oe:
+        os_.step(case["dt"])
+    assert ge.value.status == oe.value.status == abi.NEGATIVE_MOLES
+    assert "element 67" in str(ge.value) and "element 67" in str(oe.value)
+
+
 def test_two_phase_retract_restores_state(ctx):
     case, gm, om, gs, os_, keep = _two_phase(ctx, 6, 6, 3)
     p0, N0, S0 = gs.state()

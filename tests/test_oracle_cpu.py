@@ -531,3 +531,30 @@ def test_transmissibilities_are_homogeneous_in_k(scheme):
     k1, k4, k3 = out[0][2], out[1][2], out[2][2]
     assert np.array_equal(k4, 4.0 * k1)
     assert np.max(np.abs(k3 - 3.0 * k1)) <= 4e-15 * np.max(np.abs(k1))
+
+
+def test_three_phase_black_oil_regimes_and_balance():
+    """BlackOilEquationOfState's three branches (fluid/
+    BlackOilEquationOfState.java:227-489) on a water-oil-gas case: a
+    single-phase gas cap, single-phase undersaturated oil, and two-phase
+    oil/gas cells that appear where injected gas exceeds the bubble point.
+    The initial state is volume-balanced, saturations sum to one and every
+    step closes the component balance to 1e-12."""
+    case = W.three_phase_case()
+    keep = abi.Keep()
+    m = O.Mesh(3, 12, 12, 4, coords=case["nodes"], perm=case["perm"])
+    m.mpfa()
+    sim = O.Simulator(m, W.three_phase_fluid(keep), W.corey(), case["porosity"], case["compaction"],
+                      W.build_sources(keep, case), W.build_initial(case), W.runspec(rtol=1e-12))
+    R, _ = sim.residual_volume()
+    assert np.max(np.abs(R)) <= 1e-9
+    p, N, S = sim.state()
+    gas_only = (S[2] > 0) & (S[1] == 0)
+    oil_only = (S[1] > 0) & (S[2] == 0)
+    assert gas_only.sum() == 12 * 12 - 1 and oil_only.sum() == 12 * 12 * 3 + 1
+    for _ in range(4):
+        info = sim.step(case["dt"])
+        assert info.mass_balance_error <= 1e-12
+    p, N, S = sim.state()
+    assert np.allclose(S.sum(axis=0), 1.0, atol=1e-12)
+    assert ((S[1] > 0) & (S[2] > 0)).sum() >= 5  # two-phase oil/gas at the injection front
