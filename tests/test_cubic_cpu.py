@@ -88,3 +88,48 @@ def test_single_component_volumes_follow_the_cubic():
                               -(A * B + s * e * B ** 2 * (B + 1))])
             Z = roots[np.abs(roots.imag) < 1e-10].real.max()
             assert abs(V[i] - Z * RGAS * T[i] * N[1, i] / p[i]) <= 1e-12 * V[i]
+
+
+def test_two_phase_cells_are_at_equilibrium():
+    """At every two-phase cell of the flash, recomputed here with numpy from
+    the returned phase compositions (Peng-Robinson mixture a and b with the
+    binary interaction coefficients, fugacity coefficients of the generic
+    two-parameter cubic): the oil volume is the smallest real root, the gas
+    volume the largest (to 1e-12 in Z), and oil and gas fugacities agree to
+    the flash tolerance (CubicEquationOfState.java:871-970, |f_oil - f_gas| <
+    FlashTolerance = 0.1 Pa)."""
+    keep = abi.Keep()
+    f = W.compositional_fluid(keep)
+    nc = f.nc
+    p, T, N = W.compositional_cells(400, nc)
+    ph, _ = O.cubic_phase_state(f, p, T, N)
+    both = np.nonzero((ph[1, 0] > 0) & (ph[2, 0] > 0))[0]
+    assert len(both) >= 10
+    s, e, OA, OB, _ = _eos_constants(abi.EOS_PR, 0.0)
+    hc = range(1, nc)
+    for c in both:
+        a_i, b_i = {}, {}
+        for i in hc:
+            w = f.omega[i]
+            m = (0.379642 + 1.48503 * w - 0.164423 * w * w + 0.016666 * w ** 3 if w > 0.49
+                 else _eos_constants(abi.EOS_PR, w)[4])
+            a_i[i] = OA * RGAS ** 2 * f.Tc[i] ** 2 / f.pc[i] * (1 + m * (1 - np.sqrt(T[c] / f.Tc[i]))) ** 2
+            b_i[i] = OB * RGAS * f.Tc[i] / f.pc[i]
+        aij = {(i, j): (1 - f.bic[i * abi.MAX_COMPONENTS + j]) * np.sqrt(a_i[i] * a_i[j]) for i in hc for j in hc}
+        fug = []
+        for a_ph in (1, 2):
+            Nph = ph[a_ph, 6:6 + nc, c]
+            x = {i: Nph[i] / Nph[1:].sum() for i in hc}
+            a = sum(x[i] * x[j] * aij[i, j] for i in hc for j in hc)
+            b = sum(x[i] * b_i[i] for i in hc)
+            A, B = a * p[c] / (RGAS * T[c]) ** 2, b * p[c] / (RGAS * T[c])
+            roots = np.roots([1, (s + e - 1) * B - 1, A + s * e * B ** 2 - (s + e) * B * (B + 1),
+                              -(A * B + s * e * B ** 2 * (B + 1))])
+            real = roots[np.abs(roots.imag) < 1e-8].real
+            Z = p[c] * ph[a_ph, 1, c] / (RGAS * T[c] * Nph[1:].sum())
+            assert abs(Z - (real.min() if a_ph == 1 else real.max())) <= 1e-12
+            lnphi = {i: b_i[i] / b * (Z - 1) - np.log(Z - B)
+                     - A / (B * (s - e)) * (2 * sum(x[j] * aij[i, j] for j in hc) / a - b_i[i] / b)
+                     * np.log((Z + s * B) / (Z + e * B)) for i in hc}
+            fug.append({i: x[i] * p[c] * np.exp(lnphi[i]) for i in hc})
+        assert max(abs(fug[0][i] - fug[1][i]) for i in hc) <= f.flash_tolerance * 1.01
