@@ -505,6 +505,28 @@ int orc_amg_apply(void* h, const double* b, double* x, int trans, char* err, int
   }
 }
 
+// Test hook: every cell's pressure and moles (N component major) replaced,
+// its CV secondaries re-evaluated (CV.calculateSecondaries), and R, dR/dp
+// and dR/dN returned, so that the analytic volume derivatives can be checked
+// against differences.  The simulator is left at the given state.
+int orc_sim_eval_cells(void* h, const double* p, const double* N, double* R, double* dRdp, double* dRdN) {
+  Simulator* s = (Simulator*)h;
+  const int n = s->mesh->numElements();
+  try {
+    for (int i = 0; i < n; ++i) {
+      s->cv[i].p = p[i];
+      for (int nu = 0; nu < s->nc; ++nu) s->cv[i].N[nu] = N[(size_t)nu * n + i];
+      s->cvSecondaries(i);
+      R[i] = s->cv[i].R;
+      dRdp[i] = s->cv[i].dRdp;
+      for (int nu = 0; nu < s->nc; ++nu) dRdN[(size_t)nu * n + i] = s->cv[i].dRdN[nu];
+    }
+  } catch (Failure& f) {
+    return f.status;
+  }
+  return 0;
+}
+
 int orc_sim_residual_volume(void* h, double* R, double* dRdp) {
   Simulator* s = (Simulator*)h;
   for (int i = 0; i < s->mesh->numElements(); ++i) {

@@ -64,6 +64,8 @@ def _declare(L):
     L.orc_sim_state.argtypes = [vp, P(d), P(d), P(d)]
     L.orc_sim_jacobian.argtypes = [vp, P(d), P(d)]
     L.orc_sim_residual_volume.argtypes = [vp, P(d), P(d)]
+    L.orc_sim_eval_cells.argtypes = [vp, P(d), P(d), P(d), P(d), P(d)]
+    L.orc_sim_eval_cells.restype = i
     L.orc_sim_time.restype = d
     L.orc_sim_time.argtypes = [vp]
     L.orc_sim_last_dn.argtypes = [vp, P(d)]
@@ -351,6 +353,16 @@ class Simulator:
         d = np.zeros(self.n)
         lib().orc_sim_residual_volume(self.h, abi.dptr(R), abi.dptr(d))
         return R, d
+
+    def eval_cells(self, p, N):
+        """Re-evaluate every cell at pressures p (n) and moles N (nc x n):
+        returns R, dR/dp and dR/dN (nc x n); the simulator keeps that state."""
+        p, N = _f64(p), _f64(N)
+        R, dRdp, dRdN = np.zeros(self.n), np.zeros(self.n), np.zeros_like(N)
+        st = lib().orc_sim_eval_cells(self.h, abi.dptr(p), abi.dptr(N), abi.dptr(R), abi.dptr(dRdp), abi.dptr(dRdN))
+        if st != 0:
+            raise OracleError(st, "CV secondaries")
+        return R, dRdp, dRdN
 
 
 class AMG:

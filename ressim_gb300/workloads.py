@@ -216,13 +216,14 @@ def two_phase_case(ni=128, nj=128, nk=32, seed=1, perturb=0.1, corr_len=8.0, kz_
 GAS_CONSTANT = 8.3145  # J/(mol K), util/Constants.java:23
 
 
-def three_phase_fluid(keep, p_range=(20 * BAR, 600 * BAR), n_p=64):
+def three_phase_fluid(keep, p_range=(20 * BAR, 600 * BAR), n_p=64, gas_swelling=0.5):
     """Water, oil and gas black-oil fluid (one component per group): the
     bubble point (gas fraction of a saturated oil) rises linearly from 0.05 at
     20 bar to 0.40 at 600 bar, the dew point (oil fraction of a saturated gas)
     is 0.02; oil molar density has 1e-4 /bar compressibility and rises with
-    dissolved gas (x(1 + C)), gas molar density is p / (0.9 R T) (x(1 + C / 2)
-    with vaporised oil); viscosities 1 cP water, 2 cP oil, 0.02 cP gas."""
+    dissolved gas (x(1 + C)), gas molar density is p / (0.9 R T), x(1 +
+    gas_swelling C) with vaporised oil fraction C; viscosities 1 cP water,
+    2 cP oil, 0.02 cP gas."""
     p0 = 200 * BAR
     ps = np.linspace(p_range[0], p_range[1], n_p)
     Ts = np.array([250.0, 450.0])
@@ -242,7 +243,7 @@ def three_phase_fluid(keep, p_range=(20 * BAR, 600 * BAR), n_p=64):
     f.dew_point = abi.constant(0.02, 2)
     P, C, T = np.meshgrid(ps, Cs, Ts, indexing="ij")
     f.oil_density = abi.table(keep, [ps, Cs, Ts], xio0 * np.exp(co * (P - p0)) * (1.0 + C))
-    f.gas_density = abi.table(keep, [ps, Cs, Ts], P / (0.9 * GAS_CONSTANT * T) * (1.0 + 0.5 * C))
+    f.gas_density = abi.table(keep, [ps, Cs, Ts], P / (0.9 * GAS_CONSTANT * T) * (1.0 + gas_swelling * C))
     f.oil_viscosity = abi.constant(2.0 * CENTIPOISE, 3)
     f.gas_viscosity = abi.constant(0.02 * CENTIPOISE, 3)
     f.oil_enthalpy = abi.constant(0.0, 3)
