@@ -133,3 +133,45 @@ def test_two_phase_cells_are_at_equilibrium():
                      * np.log((Z + s * B) / (Z + e * B)) for i in hc}
             fug.append({i: x[i] * p[c] * np.exp(lnphi[i]) for i in hc})
         assert max(abs(fug[0][i] - fug[1][i]) for i in hc) <= f.flash_tolerance * 1.01
+
+
+def test_phase_state_volume_derivatives():
+    """CubicEquationOfState's total-volume derivatives dV/dp, dV/dT and dV/dN
+    (the volume derivatives :621-660 and the flash sensitivities they carry
+    in two-phase cells) against central differences of the phase state.  The
+    step is 1e-4 relative: small enough for the truncation error, large
+    enough that the warm-started flash re-equilibrates beyond its 0.1 Pa
+    fugacity tolerance.  At 1e-6 a two-phase cell often takes one iteration
+    and keeps its old split, and the difference then measures that frozen
+    split.  Components with fewer moles than twice the step are skipped."""
+    keep = abi.Keep()
+    f = W.compositional_fluid(keep)
+    nc = f.nc
+    p, T, N = W.compositional_cells(400, nc)
+    ph, _ = O.cubic_phase_state(f, p, T, N)
+
+    def total(q, fld):
+        return q[1, fld] * (q[1, 0] > 0) + q[2, fld] * (q[2, 0] > 0)
+
+    def check(pp, TT, Np, Nm, pm, Tm, h, fld, ok):
+        qp, _ = O.cubic_phase_state(f, pp, TT, Np, ph.copy())
+        qm, _ = O.cubic_phase_state(f, pm, Tm, Nm, ph.copy())
+        keep_regime = ok & ((qp[1, 0] > 0) == (qm[1, 0] > 0)) & ((qp[2, 0] > 0) == (qm[2, 0] > 0))
+        fd = (total(qp, 1) - total(qm, 1)) / (2 * np.where(ok, h, 1.0))
+        an = total(ph, fld)
+        assert keep_regime.sum() >= 0.9 * ok.sum()
+        err = np.abs(fd - an)[keep_regime] / np.abs(an)[keep_regime]
+        assert np.max(err) <= 2e-6, (fld, np.max(err))
+
+    everywhere = np.ones(len(p), bool)
+    hp, hT = 1e-4 * p, 1e-4 * T
+    check(p + hp, T, N, N, p - hp, T, hp, 3, everywhere)
+    check(p, T + hT, N, N, p, T - hT, hT, 4, everywhere)
+    for nu in range(1, nc):
+        h = 1e-4 * N[1:].sum(axis=0)
+        ok = N[nu] > 2 * h
+        h = np.where(ok, h, 0.0)
+        Np, Nm = N.copy(), N.copy()
+        Np[nu] += h
+        Nm[nu] -= h
+        check(p, T, Np, Nm, p, T, h, 6 + nc + nu, ok)
