@@ -42,3 +42,15 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = _run({"RANK": "1", "WORLD_SIZE": "2"})
     assert r.returncode == 0, r.stderr
     assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+
+
+def test_sweep_bytes():
+    """Algorithmic bytes of the ILU(0) level walks that the roofline divides
+    by: 12 B per strictly lower (upper) entry, 16 (24) B per row."""
+    import numpy as np
+
+    import bench
+
+    rp = np.array([0, 2, 5, 7], np.int32)  # 3 x 3 tridiagonal
+    col = np.array([0, 1, 0, 1, 2, 1, 2], np.int32)
+    assert bench.sweep_bytes(rp, col) == (12 * 2 + 16 * 3, 12 * 2 + 24 * 3)
