@@ -9,7 +9,11 @@ oracle consume identical bytes:
 * ``potential_case``: 2D single-phase incompressible potential problem
   (MPFA-O, full anisotropic tensor, Dirichlet columns, injector/producer);
 * ``two_phase_case``: 3D oil/water black-oil problem on a perturbed hexahedral
-  grid with a lognormal permeability field and a five-spot well pattern.
+  grid with a lognormal permeability field and a five-spot well pattern;
+* ``three_phase_case``: the same grid with water, oil and gas (a gas cap over
+  undersaturated oil, gas injected at the corners);
+* ``compositional_case`` / ``compositional_cells``: Peng-Robinson fluids with
+  water and three hydrocarbon pseudo-components, on a grid or per cell.
 
 Units are SI as in RS (Pa, m^2, Pa*s, K, mol).
 """
