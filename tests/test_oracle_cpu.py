@@ -563,7 +563,8 @@ def test_three_phase_black_oil_regimes_and_balance():
 @pytest.mark.parametrize("gas_swelling", [0.0, 0.5])
 def test_black_oil_volume_derivatives(gas_swelling):
     """CV.calculateResidualVolume's dR/dp and dR/dN (field/CV.java:475-501)
-    from the black-oil EOS's analytic volume derivatives, against central
+    from the black-oil EOS's analytic volume derivatives and the rock's
+    compaction (CV.java:446-459), against central
     differences of R, in all three regimes of a water-oil-gas state (gas cap,
     undersaturated oil, two-phase front after four steps).  With a gas
     density independent of the vaporised-oil fraction every derivative
@@ -575,8 +576,9 @@ def test_black_oil_volume_derivatives(gas_swelling):
     keep = abi.Keep()
     m = O.Mesh(3, 12, 12, 4, coords=case["nodes"], perm=case["perm"])
     m.mpfa()
+    compaction = np.full(len(case["porosity"]), 5e-10)  # rock compressibility [1/Pa], so dphi/dp enters dR/dp
     sim = O.Simulator(m, W.three_phase_fluid(keep, gas_swelling=gas_swelling), W.corey(), case["porosity"],
-                      case["compaction"], W.build_sources(keep, case), W.build_initial(case), W.runspec(rtol=1e-12))
+                      compaction, W.build_sources(keep, case), W.build_initial(case), W.runspec(rtol=1e-12))
     for _ in range(4):
         sim.step(case["dt"])
     p, N, S = sim.state()
