@@ -605,3 +605,29 @@ def test_black_oil_volume_derivatives(gas_swelling):
             assert np.min(err[gas_only]) > 1e-3  # the reference's sign in the gas cap
         else:
             assert np.max(err) <= 1e-6
+
+
+def test_hydrostatic_equilibrium_is_stationary():
+    """Water of constant density initialised by Field.volumeBalance
+    (p = p_datum - rho g dz) on a perturbed grid with full-tensor MPFA-O and
+    gravity (CS.java:94-170): every connection's potential sum
+    sum_k t_k (p_k + rho g z_k) vanishes because sum_k t_k = 0, so with no
+    wells three steps leave pressures and moles unchanged to rounding."""
+    case = W.two_phase_case(ni=8, nj=7, nk=5, seed=2)
+    case["fractions"] = (1.0, 0.0)
+    case["injectors"] = []
+    keep = abi.Keep()
+    fluid = W.two_phase_fluid(keep)
+    fluid.water_density = abi.constant(1000.0 / 0.01801528, 2)
+    m = O.Mesh(3, 8, 7, 5, coords=case["nodes"], perm=case["perm"])
+    m.mpfa()
+    n = 8 * 7 * 5
+    sim = O.Simulator(m, fluid, W.corey(), case["porosity"], np.full(n, 1e-9), W.build_sources(keep, case),
+                      W.build_initial(case), W.runspec(rtol=1e-12))
+    p0, N0, _ = sim.state()
+    assert p0.max() - p0.min() > 1e4  # a real hydrostatic gradient over five layers
+    for _ in range(3):
+        sim.step(case["dt"])
+    p1, N1, _ = sim.state()
+    assert np.max(np.abs(p1 - p0) / p0) <= 1e-13
+    assert np.max(np.abs(N1[0] - N0[0]) / N0[0]) <= 1e-10
