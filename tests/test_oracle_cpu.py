@@ -631,3 +631,20 @@ def test_hydrostatic_equilibrium_is_stationary():
     p1, N1, _ = sim.state()
     assert np.max(np.abs(p1 - p0) / p0) <= 1e-13
     assert np.max(np.abs(N1[0] - N0[0]) / N0[0]) <= 1e-10
+
+
+@pytest.mark.parametrize("scheme", ["mpfa", "tpfa"])
+def test_transmissibilities_are_translation_invariant(scheme):
+    """The interaction-region geometry (O_MPFA.java:271-457, MPFA.java:314-354)
+    and the two-point distances (TPFA.java:50-72) use coordinate differences
+    only: moving the whole perturbed grid by (1000, -500, -250) m keeps the MD
+    lists and changes the transmissibilities only by the rounding of the
+    larger coordinates."""
+    case = W.two_phase_case(ni=6, nj=5, nk=4, seed=3)
+    out = []
+    for offset in ((0.0, 0.0, 0.0), (1000.0, -500.0, -250.0)):
+        m = O.Mesh(3, 6, 5, 4, coords=np.ascontiguousarray(case["nodes"] + np.array(offset)), perm=case["perm"])
+        m.mpfa(tpfa=(scheme == "tpfa"))
+        out.append(m.transmissibilities())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert np.max(np.abs(out[0][2] - out[1][2])) <= 1e-12 * np.max(np.abs(out[0][2]))
