@@ -648,3 +648,18 @@ def test_transmissibilities_are_translation_invariant(scheme):
         out.append(m.transmissibilities())
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
     assert np.max(np.abs(out[0][2] - out[1][2])) <= 1e-12 * np.max(np.abs(out[0][2]))
+
+
+@pytest.mark.parametrize("omega", [1.0, 1.3, 0.7])
+def test_ssor_from_zero_is_the_closed_form(omega):
+    """SSOR.apply (sparse/SSOR.java:126-194), forward then reverse sweep with
+    omegaF = omegaR = omega from a zero start, equals the textbook SSOR
+    preconditioner omega (2 - omega) (D + omega U)^-1 D (D + omega L)^-1 b on a
+    non-symmetric matrix."""
+    A = rand_banded(30, 4, 9, spd=False)
+    rp, col, val = csr_of(A)
+    b = np.random.Generator(np.random.PCG64(2)).standard_normal(30)
+    x = O.ssor(rp, col, val, b, np.zeros(30), omega_f=omega, omega_r=omega)
+    D, L, U = np.diag(np.diag(A)), np.tril(A, -1), np.triu(A, 1)
+    ref = (2 - omega) * omega * np.linalg.solve(D + omega * U, D @ np.linalg.solve(D + omega * L, b))
+    assert np.max(np.abs(x - ref)) <= 1e-14 * np.max(np.abs(ref))
