@@ -5,21 +5,25 @@ Workload: 3D oil/water black-oil case on a perturbed 128 x 128 x 32 hex grid
 Swc = Sor = 0.2, five-spot wells; MPFA-O transmissibilities; every step is
 one Discretisation.solve(dt): the pressure Newton loop (properties, Darcy
 fluxes, Jacobian assembly, BiCGstab + ILU(0) to 1e-8 relative residual,
-pressure update) and the explicit molar-mass update.
+pressure update) and the explicit molar-mass update.  The timed steps are
+the first K steps from the initial state (the GPU takes its W warm-up steps
+first and returns to the initial state).
 
 Metric: cell-Newton-steps/s = cells x pressure Newton iterations / seconds.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl resgpu|reference]
 
 Prints one JSON line on rank 0.  `value` is device time (CUDA events on the
-library's stream, inputs resident); `e2e` runs the same steps through the
-public API with the state staged through page-locked host memory every step.
-`--impl reference` times the CPU oracle (the C++ restatement of RS + MTJ,
-single-threaded like RS) on a bounded sample of the workload.
+library's stream, inputs resident); `e2e` replays the same K steps from the
+initial state through the public API with the state staged through
+page-locked host memory every step.  `--impl reference` times the CPU oracle
+(the C++ restatement of RS + MTJ, single-threaded like RS) on the same K
+steps with the same converged Newton loop.
 """
 import argparse
 import json
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -109,10 +113,20 @@ def build_case(args):
     return case, keep, fluid, co, srcs, init, spec
 
 
-# DRAM bytes (read + write) per launch of the ILU(0) level walks, from one ncu
-# capture of this workload (profiles/ilu_sweep_ring_two_phase_128x128x32.md);
-# keyed by grid size and kernel family.
+# DRAM bytes (read + write) per launch of the ILU(0) level walks, measured by
+# one ncu capture of this workload (dram__bytes_read.sum +
+# dram__bytes_write.sum); keyed by grid size and kernel family.  ncu cannot
+# run inside the timed benchmark, so the line labels these as a capture's.
 NCU_TRAFFIC = {(128, 128, 32): {"ilu_lower": 91_788_288, "ilu_upper": 95_744_256}}
+NCU_TRAFFIC_SOURCE = "ncu capture of the same kernel on the same workload (not measured in this run)"
+
+
+def config_of(args, nnz, dt):
+    """Workload description shared by both arms (same keys, same values)."""
+    return {"workload": f"two-phase oil/water black-oil, {args.ni}x{args.nj}x{args.nk} perturbed hex grid, MPFA-O, "
+                        f"BiCGstab+ILU(0) FP64 to {args.rtol:g} relative residual, Newton converged per step, "
+                        f"first K steps from the initial state",
+            "cells": args.ni * args.nj * args.nk, "pattern_nnz": int(nnz), "dt_s": dt, "seed": args.seed}
 
 
 def sweep_bytes(rp, col):
@@ -138,8 +152,10 @@ def run_resgpu(args, rank, world, local_rank):
     n = counts["elements"]
     sim = api.Discretisation(ctx, mesh, fluid, co, case["porosity"], case["compaction"], srcs, init, spec)
     dt = case["dt"]
+    sim.save_state()  # the initial state: the timed and end-to-end passes both start here
     for _ in range(args.warmup):
         sim.step(dt)
+    sim.restore_state()
     barrier(world)
     clocks = ClockSampler(local_rank)
     clocks.start()
@@ -163,10 +179,11 @@ def run_resgpu(args, rank, world, local_rank):
     dev_s = max_over_ranks(dev_s, world)
     units = float(n) * newton
     units = sum_over_ranks(units, world)
+    p_end = sim.state()[0]
 
     # end to end through the public API with page-locked host staging
     nc = sim.nc
-    e2e = None if args.no_e2e else e2e_pass(args, ctx, sim, n, nc, dt, world)
+    e2e = None if args.no_e2e else e2e_pass(args, ctx, sim, n, nc, dt, world, newton, p_end)
     res = finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, e2e, rank)
     # the secondary legs report their failure instead of ending the run
     def leg(name, fn):
@@ -175,9 +192,10 @@ def run_resgpu(args, rank, world, local_rank):
         except Exception as e:  # noqa: BLE001
             res[name] = {"error": f"{type(e).__name__}: {e}"}
 
-    if args.mixed_steps > 0:
-        leg("mixed", lambda: mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, sim, n, dt, res["ms_per_step"],
-                                       world))
+    if args.mixed_steps >= 0:
+        leg("mixed", lambda: mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, sim, n, dt, dev_s, p_end, world))
+    if args.amg and rank == 0:
+        leg("amg", lambda: amg_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world))
     if args.ensemble > 0 and rank == 0:
         leg("ensemble", lambda: ensemble_leg(args))
     if args.flash_cells > 0 and rank == 0:
@@ -189,19 +207,22 @@ def run_resgpu(args, rank, world, local_rank):
     return res
 
 
-def e2e_pass(args, ctx, sim, n, nc, dt, world):
-    """The timed steps again through the public API with the state staged
-    through page-locked host memory every step (host -> device before the
-    step, device -> host after it)."""
+def e2e_pass(args, ctx, sim, n, nc, dt, world, newton_timed, p_timed):
+    """The timed steps again, from the same initial state, through the
+    public API with the state staged through page-locked host memory every
+    step (host -> device before the step, device -> host after it).  The
+    steps and Newton iterations are those of the timed pass."""
     from ressim_gb300 import api
 
     hp = api.PinnedArray(n)
     hN = api.PinnedArray(nc * n)
     hS = api.PinnedArray(3 * n)
+    sim.restore_state()
     p, N, S = sim.state()
     hp.array[:] = p
     hN.array[:] = N.reshape(-1)
     e2e_newton = 0
+    lib = api.lib()
     barrier(world)
     ctx.synchronize()
     t0 = time.perf_counter()
@@ -209,7 +230,6 @@ def e2e_pass(args, ctx, sim, n, nc, dt, world):
         sim.set_state(hp.array, hN.array)
         info = sim.step(dt)
         e2e_newton += info.newton_iterations
-        lib = api.lib()
         ctx.check(lib.rsg_sim_get_state(sim.h, abi.dptr(hp.array), abi.dptr(hN.array), abi.dptr(hS.array)),
                   "get_state")
     ctx.synchronize()
@@ -217,7 +237,9 @@ def e2e_pass(args, ctx, sim, n, nc, dt, world):
     e2e_units = sum_over_ranks(float(n) * e2e_newton, world)
     h2d = (1 + nc) * n * 8
     d2h = (1 + nc + 3) * n * 8
-    return {"value": e2e_units / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    return {"value": e2e_units / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "newton_iterations": e2e_newton, "same_steps_as_timed": e2e_newton == newton_timed,
+            "max_rel_pressure_diff_vs_timed": float(np.max(np.abs(hp.array - p_timed) / np.abs(p_timed)))}
 
 
 def adjoint_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world):
@@ -252,25 +274,105 @@ def adjoint_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world):
             "grad_abs_max": float(np.max(np.abs(grad))), "grad_finite": bool(np.all(np.isfinite(grad)))}
 
 
-def mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, fp64_sim, n, dt, fp64_ms, world):
+def amg_leg(args, ctx, mesh, case, fluid, co, srcs, init, n, world):
+    """MTJ's smoothed-aggregation AMG on the benchmark's first pressure
+    system (the Jacobian and residual of the first Newton iteration): FP64
+    GMRES(30) + AMG, and the mixed-precision solver (FP64 flexible GMRES
+    around FP32 BiCGstab) with the FP32 AMG hierarchy, both to the
+    benchmark's relative tolerance from x = 0.  Reported: setup wall time
+    (aggregation, smoothed interpolation, Galerkin products and SSOR plans
+    on the GPU, with their host-side planning), solve device time and
+    iterations, the V-cycle's device time from the event-bracketed kernel
+    families, its algorithmic bytes (level operators and interpolation read
+    by the four SSOR sweeps, the residual, restriction and prolongation) and
+    their fraction of the HBM peak, and the two solutions' difference.
+    BiCGstab + AMG, the configuration's FP64 pairing, diverges on this
+    system as it does in MTJ (the oracle's and the GPU's tests show it), so
+    GMRES is the Krylov method here."""
+    from ressim_gb300 import api
+
+    spec = W.runspec(ptol=1e300, rtol=1e-2)
+    sim = api.Discretisation(ctx, mesh, fluid, co, case["porosity"], case["compaction"], srcs, init, spec)
+    sim.enable_jacobian_capture()
+    sim.step(case["dt"])
+    rp, col = mesh.pattern(0)
+    val, rhs = sim.jacobian(len(col))
+    sim.release()
+    A = api.CompRowMatrix(ctx, n, rp, col, val)
+    hbm, peak_kind = peaks()
+    out = {"system": f"first pressure Jacobian of the {args.ni}x{args.nj}x{args.nk} case", "rtol": args.rtol}
+    vfam = ("amg_copy", "amg_zero", "amg_resid", "amg_restrict", "amg_prolong", "amg_direct", "amg_coarse_cvt",
+            "ssor_fwd", "ssor_bwd", "ssor_copy", "ssor_fwd_f32", "ssor_bwd_f32")
+    xs = {}
+    for name, cls in (("fp64_gmres", api.GMRES), ("mixed", api.MixedFGMRES)):
+        s = cls(ctx, abi.PC_AMG, rtol=args.rtol, atol=1e-50, max_iter=20000)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        s.set_matrix(A)
+        ctx.synchronize()
+        setup_ms = (time.perf_counter() - t0) * 1e3
+        levels = s.amg_levels()
+        sizes = [s.amg_level_sizes(k) for k in range(levels)]
+        ctx.set_profiling(True)
+        ctx.profile_reset()
+        ctx.timer_record(10)
+        x = s.solve(A, rhs, np.zeros(n), raise_on_fail=False)
+        ctx.timer_record(11)
+        ctx.synchronize()
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        solve_ms = ctx.timer_elapsed_ms(10, 11)
+        cycles = prof.get("amg_direct", (0.0, 0))[1]
+        vms = sum(prof[f][0] for f in vfam if f in prof)
+        f32 = name == "mixed"
+        eb, vb = (8, 4) if f32 else (12, 8)  # bytes per stored entry (value + index), per vector element
+        vbytes = 0
+        for k, (ln, lnnz, lc, pnnz) in enumerate(sizes):
+            if k == levels - 1:
+                break
+            vbytes += 4 * (eb * lnnz + 4 * vb * ln)  # four SSOR sweeps: row entries, b, x, half iterate
+            vbytes += eb * lnnz + 3 * vb * ln        # residual
+            vbytes += 2 * (eb * pnnz + vb * (ln + lc))  # restriction and prolongation
+        per_cycle = vms / cycles if cycles else None
+        info = s.last_info
+        out[name] = {"levels": levels, "level_rows": [int(z[0]) for z in sizes], "setup_ms": setup_ms,
+                     "solve_ms": solve_ms, "iterations": info.iterations, "status": abi.STATUS.get(info.reason),
+                     "inner_iterations": info.inner_iterations if f32 else None, "v_cycles": cycles,
+                     "v_cycle_ms": per_cycle, "v_cycle_bytes": vbytes,
+                     "v_cycle_gbs": vbytes / (per_cycle / 1e3) / 1e9 if per_cycle else None,
+                     "v_cycle_hbm_frac": (vbytes / (per_cycle / 1e3) / 1e9 / hbm) if per_cycle else None,
+                     "peak_source": peak_kind}
+        xs[name] = x
+        s.release()
+    out["max_rel_diff_mixed_vs_fp64"] = float(np.max(np.abs(xs["mixed"] - xs["fp64_gmres"])) /
+                                              np.max(np.abs(xs["fp64_gmres"])))
+    A.release()
+    return out
+
+
+def mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, fp64_sim, n, dt, fp64_s, p_fp64, world):
     """The same steps with the mixed-precision pressure solver (FP64 flexible
     GMRES around FP32 BiCGstab + FP32 ILU(0)) to the same relative residual:
-    device time per step against the FP64 BiCGstab + ILU(0) steps above
-    (both simulations start from the initial state and take the same warm-up
-    steps), and the largest relative pressure difference after one step
-    taken by both from the same state."""
+    the first K steps from the initial state after W warm-up steps, exactly
+    as the FP64 line times them, so the speed-up compares the same steps;
+    the pressures after those steps against the FP64 line's; and the largest
+    relative pressure difference after one more step taken by both from the
+    same state."""
     from ressim_gb300 import api
 
     spec = W.runspec(method=abi.FGMRES_MIXED, rtol=args.rtol, atol=1e-50, inner_iterations=int(args.inner[0]),
                      inner_tolerance=args.inner[1])
     sim = api.Discretisation(ctx, mesh, fluid, co, case["porosity"], case["compaction"], srcs, init, spec)
+    sim.save_state()
     for _ in range(args.warmup):
         sim.step(dt)
+    sim.restore_state()
+    steps = args.mixed_steps if args.mixed_steps > 0 else args.steps
     barrier(world)
     ctx.synchronize()
     newton = linear = 0
     ctx.timer_record(2)
-    for _ in range(args.mixed_steps):
+    for _ in range(steps):
         info = sim.step(dt)
         newton += info.newton_iterations
         linear += info.linear_iterations
@@ -279,6 +381,7 @@ def mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, fp64_sim, n, dt, fp6
     dev_s = max_over_ranks(ctx.timer_elapsed_ms(2, 3) / 1e3, world)
     units = sum_over_ranks(float(n) * newton, world)
     p, N, _ = sim.state()
+    diff_k = float(np.max(np.abs(p - p_fp64) / np.abs(p_fp64))) if steps == args.steps else None
     sim.set_state(p, N)
     fp64_sim.set_state(p, N)
     # the comparison step is also the event-profiled one (per-kernel times)
@@ -290,7 +393,7 @@ def mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, fp64_sim, n, dt, fp6
     fp64_sim.step(dt)
     pm = sim.state()[0]
     pd = fp64_sim.state()[0]
-    ms = dev_s * 1e3 / args.mixed_steps
+    ms = dev_s * 1e3 / steps
     # FP32 SpMV of the inner solver: 4 B value + 4 B column per entry, row
     # length, x, y and the dot operand per row
     rp, col = mesh.pattern(0)
@@ -303,11 +406,15 @@ def mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, fp64_sim, n, dt, fp6
         inner = {"kernel": "k_f32_spmv_dot", "launches": cnt, "avg_launch_us": round(t_ms / cnt * 1e3, 2),
                  "bytes_per_launch": f32_bytes, "achieved_gbs": round(gbs, 1), "peak": hbm,
                  "frac": round(gbs / hbm, 4), "peak_source": peak_kind}
-    return {"value": units / dev_s, "unit": METRIC, "ms_per_step": ms, "steps": args.mixed_steps,
-            "speedup_vs_fp64_per_step": fp64_ms / ms, "newton_iterations": newton, "outer_iterations": linear,
-            "inner": {"iterations": int(args.inner[0]), "rtol": args.inner[1]},
-            "max_rel_pressure_diff_vs_fp64": float(np.max(np.abs(pm - pd) / np.abs(pd))),
-            "inner_spmv": inner}
+    out = {"value": units / dev_s, "unit": METRIC, "ms_per_step": ms, "steps": steps,
+           "newton_iterations": newton, "outer_iterations": linear,
+           "inner": {"iterations": int(args.inner[0]), "rtol": args.inner[1]},
+           "max_rel_pressure_diff_vs_fp64_after_steps": diff_k,
+           "max_rel_pressure_diff_vs_fp64_one_step": float(np.max(np.abs(pm - pd) / np.abs(pd))),
+           "inner_spmv": inner}
+    if steps == args.steps:
+        out["speedup_vs_fp64_same_steps"] = fp64_s / dev_s
+    return out
 
 
 def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, newton, linear, dt, e2e, rank=0):
@@ -335,7 +442,8 @@ def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, ne
         achieved = fam_bytes[k] / per_launch / 1e9
         traffic = NCU_TRAFFIC.get((args.ni, args.nj, args.nk), {}).get(k)
         roof = {"bound": "hbm", "kernel": k, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 5), "traffic": traffic, "peak_source": peak_kind,
+                "frac": round(achieved / hbm, 5), "traffic": traffic,
+                "traffic_source": NCU_TRAFFIC_SOURCE if traffic else None, "peak_source": peak_kind,
                 "bytes_per_launch": fam_bytes[k], "avg_launch_us": round(per_launch * 1e6, 2)}
     spmv_ms = prof.get("spmv_dot", (0, 1))
     spmv_bytes = 12 * len(col) + 4 * (n + 1) + 16 * n + 8 * n
@@ -357,12 +465,11 @@ def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, ne
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded lognormal permeability, perturbed grid, five-spot)",
-        "config": {
-            "workload": f"two-phase oil/water black-oil, {args.ni}x{args.nj}x{args.nk} perturbed hex grid, MPFA-O, "
-                        f"BiCGstab+ILU(0) FP64 to {args.rtol:g} relative residual",
-            "cells": n, "pattern_nnz": len(col), "newton_iterations": newton, "linear_iterations": linear,
-            "dt_s": dt, "l2": "matrix and factors (>300 MB) exceed the 129 MB L2", "parallelism": f"replicas x{world}",
-        },
+        "config": config_of(args, len(col), dt),
+        "newton_iterations": newton,
+        "linear_iterations": linear,
+        "l2": "matrix and factors (>300 MB) exceed the 129 MB L2",
+        "parallelism": f"replicas x{world}",
         "e2e": e2e,
         "gpu_launches": launches,
         "sweep_mode": {-1: "undecided", 0: "one launch per level", 1: "one cluster walks all levels",
@@ -551,16 +658,17 @@ def compositional_leg(args):
     return out
 
 
-def oracle_full(args):
+def oracle_full(args, one_newton=False):
     """The oracle (single-threaded C++ restatement of RS + MTJ) on the full
-    workload, set to take one Newton iteration per time step (pressure
-    tolerance 1e300), so that one step is one bounded sample of the work the
-    GPU path measures: assembly, BiCGstab + ILU(0) to the same relative
-    residual, and the explicit molar-mass update over every cell."""
+    workload from its initial state.  With one_newton the pressure tolerance
+    is 1e300, so that a step is one Newton iteration: assembly, BiCGstab +
+    ILU(0) to the same relative residual and the explicit molar-mass update
+    over every cell (the bounded CPU-baseline sample)."""
     from oracle import oracle as O
 
     case, keep, fluid, co, srcs, init, spec = build_case(args)
-    spec.pressure_tolerance = 1e300
+    if one_newton:
+        spec.pressure_tolerance = 1e300
     m = O.Mesh(3, args.ni, args.nj, args.nk, coords=case["nodes"], perm=case["perm"])
     m.mpfa()
     sim = O.Simulator(m, fluid, co, case["porosity"], case["compaction"], srcs, init, spec)
@@ -578,18 +686,34 @@ def oracle_steps(sim, case, steps):
 
 
 def cpu_baseline(args):
-    sim, case, keep, m = oracle_full(args)
+    sim, case, keep, m = oracle_full(args, one_newton=True)
     newton, linear, secs = oracle_steps(sim, case, args.cpu_steps)
     n = args.ni * args.nj * args.nk
     return {"value": n * newton / secs, "unit": METRIC, "cores": 1, "kind": "port",
             "sample": f"oracle (C++ restatement of RS+MTJ, single thread, as the reference's solvers are) on the "
-                      f"full {args.ni}x{args.nj}x{args.nk} case: {args.cpu_steps} time step(s) of one Newton "
-                      f"iteration each, {linear} BiCGstab iterations, {secs:.1f} s"}
+                      f"full {args.ni}x{args.nj}x{args.nk} case: the first {args.cpu_steps} time step(s) from the "
+                      f"initial state, one Newton iteration each, {linear} BiCGstab iterations, {secs:.1f} s"}
+
+
+def java_probe():
+    """RS and MTJ are Java; the reference itself runs only where a JVM is."""
+    java = shutil.which("java")
+    return {"java": java, "reference_jvm": "unavailable on this box (no JVM)" if java is None else
+            "present, but the timed reference is the C++ port of the same Java code"}
 
 
 def run_reference(args):
+    """The same K steps from the initial state on the oracle, with the same
+    converged Newton loop as the GPU line.  Warm-up: W steps of a 16x16x4
+    case of the same physics (the CPU code has no device state or first-launch
+    cost to warm; running W full steps would only add W x ~45 s)."""
+    small = argparse.Namespace(**vars(args))
+    small.ni, small.nj, small.nk = 16, 16, 4
+    wsim, wcase, _, _ = oracle_full(small)
+    oracle_steps(wsim, wcase, args.warmup)
+    del wsim
     sim, case, keep, m = oracle_full(args)
-    oracle_steps(sim, case, args.warmup)
+    rp, col = m.pattern(0)
     newton, linear, secs = oracle_steps(sim, case, args.steps)
     n = args.ni * args.nj * args.nk
     value = n * newton / secs
@@ -607,13 +731,14 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded lognormal permeability, perturbed grid, five-spot)",
-        "config": {"workload": f"two-phase oil/water black-oil, {args.ni}x{args.nj}x{args.nk} perturbed hex grid, "
-                               f"MPFA-O, BiCGstab+ILU(0) FP64 to {args.rtol:g} relative residual; one Newton "
-                               f"iteration per timed step",
-                   "cells": n, "newton_iterations": newton, "linear_iterations": linear},
+        "config": config_of(args, len(col), case["dt"]),
+        "newton_iterations": newton,
+        "linear_iterations": linear,
+        "jvm": java_probe(),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
-                         "sample": f"{args.steps} time steps of one Newton iteration each on the full case "
-                                   f"({linear} BiCGstab iterations, {secs:.1f} s)"},
+                         "sample": f"the first {args.steps} time steps from the initial state on the full case, "
+                                   f"Newton converged as on the GPU ({newton} Newton and {linear} BiCGstab "
+                                   f"iterations, {secs:.1f} s); warm-up: {args.warmup} steps of a 16x16x4 case"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -670,8 +795,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     ap.add_argument("--no-kernel-profile", action="store_true", help="skip the event-bracketed per-kernel pass")
-    ap.add_argument("--mixed-steps", type=int, default=2,
-                    help="steps timed with the mixed-precision pressure solver (0: skip)")
+    ap.add_argument("--mixed-steps", type=int, default=0,
+                    help="steps timed with the mixed-precision pressure solver (0: the same K steps as the FP64 "
+                         "line, -1: skip)")
+    ap.add_argument("--amg", type=int, default=1, help="AMG leg on the first pressure system (0: skip)")
     ap.add_argument("--ensemble", type=int, default=16, help="ensemble members stepped concurrently (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=1)
     ap.add_argument("--flash-cells", type=int, default=1048576,

@@ -81,9 +81,26 @@ const char* rsg_context_last_error(rsg_ctx* ctx);
 /* How the level-scheduled triangular sweeps run in this process:
  * -1 not decided yet, 0 one launch per level, 1 one thread-block cluster
  * walking all levels with hardware cluster barriers, 2 ILU sweeps on one
- * cluster exchanging values through distributed shared memory (st.async +
+ * cluster whose CTAs own contiguous row blocks and push each computed value
+ * through distributed shared memory to the CTAs that read it (st.async +
  * mbarrier transaction counts, no cluster barrier per level). */
 int32_t rsg_sweep_mode(void);
+/* Builds on the host the distributed-shared-memory schedule of one ILU(0)
+ * triangular sweep of a CSR pattern (sweep 0: the unit lower solve, 1: the
+ * upper solve; ctas: 8 or 16 CTAs in the cluster) and checks it against the
+ * pattern: every row placed once, every index inside its array, every
+ * operand either computed in the reading CTA or pushed to it within the
+ * ring's depth, and the per-level receive counts equal to the values pushed.
+ * stats (4 values, may be NULL): plan levels, ring depth, values pushed in
+ * one sweep, most neighbours of one CTA.  Needs no GPU.  Returns RSG_OK for a
+ * sound schedule, RSG_UNSUPPORTED when the pattern has none (the sweep then
+ * runs without the ring), RSG_OUT_OF_PATTERN when the check fails (msg, of
+ * msg_len bytes, may be NULL, says what failed).  Inspection only: no
+ * counterpart in the reference (UnitLowerCompRowMatrix.solve and
+ * UpperCompRowMatrix.solve, mtj/src/no/uib/cipr/matrix/sparse/ILU.java:54-140,
+ * are sequential loops). */
+rsg_status rsg_sweep_plan_check(int32_t n, const int32_t* row_ptr, const int32_t* col, int32_t sweep, int32_t ctas,
+                                int64_t* stats, char* msg, int32_t msg_len);
 /* Number of kernels this context has launched so far. */
 int64_t rsg_context_kernel_launches(rsg_ctx* ctx);
 /* Waits for all work queued on the context's stream. */
@@ -140,7 +157,10 @@ rsg_status rsg_solver_set_monitor(rsg_solver* s, double rtol, double atol, doubl
 rsg_status rsg_solver_set_restart(rsg_solver* s, int32_t restart);
 /* Mixed precision (RSG_FGMRES_MIXED): FP64 flexible GMRES(restart) whose
  * preconditioner is `inner_iterations` FP32 BiCGstab steps (stopping early at
- * inner_rtol) with the FP32 copy of the preconditioner.  Default 10, 1e-3.
+ * inner_rtol) with the FP32 copy of the preconditioner: ILU(0) factors, or
+ * the AMG hierarchy (operators, interpolation and SSOR smoother coefficients
+ * in FP32, one V-cycle from a zero start per application, coarsest LU in
+ * FP64), or the inverted diagonal.  SSOR is not offered.  Default 10, 1e-3.
  * No counterpart in the reference (a new capability beside MTJ's solvers). */
 rsg_status rsg_solver_set_inner(rsg_solver* s, int32_t inner_iterations, double inner_rtol);
 /* SSOR omegas (SSOR(F, reverse, omegaF, omegaR)) */
@@ -177,13 +197,21 @@ rsg_status rsg_solver_amg_level(rsg_solver* s, int32_t k, int32_t* sizes, int32_
  * reduction order.
  *
  * All workspace (five vectors of n doubles plus reduction partials, about
- * 40 MiB) is one static device array that every GPU loading the library
- * holds until the process exits.  n may not exceed RSG_NOALLOC_MAX_ROWS
+ * 40 MiB) is one static device array.  The driver reserves it on a device
+ * when it loads the library's module there (with CUDA's default lazy module
+ * loading: during the first call on that device) and the device holds it
+ * until the process exits; a caller whose device memory is spoken for after
+ * start-up makes one call with a 1-row system at start-up, or runs with
+ * CUDA_MODULE_LOADING=EAGER.  n may not exceed RSG_NOALLOC_MAX_ROWS
  * (RSG_BAD_ARG otherwise).  The entry point calls no cudaMalloc or cudaFree.
  * Its first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * (cudaGetSymbolAddress); make that first call before any stream capture
+ * begins.  After cudaDeviceReset on a device the looked-up address is
+ * stale: do not call the entry point on that device again in the process.
  * Every call shares the array: calls that overlap on the GPU (different
- * streams or threads) race and must be serialised by the caller.
+ * streams or threads) race and must be serialised by the caller.  A zero
+ * diagonal returns RSG_ZERO_PIVOT whatever the residual, as
+ * DiagonalPreconditioner.setMatrix fails before any iteration.
  * stream: a cudaStream_t, or NULL for the default stream.  The call returns
  * when the solve has finished; d_x holds the result (also on failure). */
 #define RSG_NOALLOC_MAX_ROWS 1048576
@@ -343,6 +371,16 @@ rsg_status rsg_sim_destroy(rsg_sim* s);
  * (Field.retract). */
 rsg_status rsg_sim_step(rsg_sim* s, double dt, rsg_step_info* info);
 rsg_status rsg_sim_retract(rsg_sim* s);
+/* A device-side copy of the whole simulator state: time, pressures,
+ * temperatures, moles, and the per-phase records and presence flags the next
+ * step reads.  rsg_sim_save_state keeps one copy per simulator (replacing the
+ * previous one); rsg_sim_restore_state returns to it, after which the same
+ * steps repeat bit for bit (RSG_BAD_ARG if nothing was saved).  Like
+ * Field.retract (field/Field.java:535-545), which returns one step, but to
+ * any saved point; RS keeps such points as serialised Field objects
+ * (numerics/Main.java:86-105). */
+rsg_status rsg_sim_save_state(rsg_sim* s);
+rsg_status rsg_sim_restore_state(rsg_sim* s);
 /* Discrete adjoint of a simulator run (Discretisation's sequential pressure
  * Newton step and explicit molar update, numerics/Discretisation.java:280-919;
  * black-oil fluids with at most 3 components).  rsg_sim_forward runs nsteps

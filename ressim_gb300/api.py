@@ -57,6 +57,7 @@ def _declare(L):
     sigs = {
         "rsg_abi_version": (i32, []),
         "rsg_sweep_mode": (i32, []),
+        "rsg_sweep_plan_check": (i32, [i32, P(i32), P(i32), i32, i32, P(i64), C.c_char_p, i32]),
         "rsg_status_string": (C.c_char_p, [i32]),
         "rsg_context_create": (i32, [i32, PP()]),
         "rsg_context_destroy": (i32, [vp]),
@@ -114,6 +115,8 @@ def _declare(L):
                                        P(abi.rsg_source), P(abi.rsg_initial), P(abi.rsg_runspec), PP()]),
         "rsg_sim_step": (i32, [vp, d, P(abi.rsg_step_info)]),
         "rsg_sim_retract": (i32, [vp]),
+        "rsg_sim_save_state": (i32, [vp]),
+        "rsg_sim_restore_state": (i32, [vp]),
         "rsg_sim_get_state": (i32, [vp, P(d), P(d), P(d)]),
         "rsg_sim_set_state": (i32, [vp, P(d), P(d)]),
         "rsg_sim_get_jacobian": (i32, [vp, P(d), P(d)]),
@@ -346,6 +349,12 @@ class IterativeSolver:
         self.ctx.check(lib().rsg_solver_amg_levels(self.h, C.byref(n)), "amg_levels")
         return n.value
 
+    def amg_level_sizes(self, k):
+        """(rows, operator entries, coarse rows, interpolation entries) of AMG level k."""
+        sz = np.zeros(4, np.int32)
+        self.ctx.check(lib().rsg_solver_amg_level(self.h, k, abi.iptr(sz), *([None] * 7)), "amg_level")
+        return tuple(int(v) for v in sz)
+
     def amg_level(self, k):
         """Level k of the AMG hierarchy: operator (CSR), aggregates and the
         interpolation operator by columns."""
@@ -528,6 +537,14 @@ class Discretisation:
         if st != 0 and raise_on_fail:
             self.ctx.check(st, "Discretisation.solve")
         return info
+
+    def save_state(self):
+        """Keeps a device-side copy of the whole state (rsg_sim_save_state)."""
+        self.ctx.check(lib().rsg_sim_save_state(self.h), "save_state")
+
+    def restore_state(self):
+        """Returns to the state kept by save_state; the same steps then repeat bit for bit."""
+        self.ctx.check(lib().rsg_sim_restore_state(self.h), "restore_state")
 
     def retract(self):
         self.ctx.check(lib().rsg_sim_retract(self.h), "retract")

@@ -576,53 +576,65 @@ __global__ void k_dense_solve(int n, const double* __restrict__ A, const int* __
 }
 
 // ------------------------------------------------------------- V-cycle ----
+// Templated on the value type: double is the MTJ V-cycle, float the
+// mixed-precision solver's FP32 copy of it (same order of operations).
 // r = f; A.multAdd(-1, u, r) (CompRowMatrix.java:335-353)
+template <typename T>
 __global__ void k_amg_resid(int n, const int* __restrict__ rp, const int* __restrict__ col,
-                            const double* __restrict__ val, const double* __restrict__ u,
-                            const double* __restrict__ f, double* __restrict__ r, const int* active) {
+                            const T* __restrict__ val, const T* __restrict__ u, const T* __restrict__ f,
+                            T* __restrict__ r, const int* active) {
   if (active && *active != 0) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double d = 0;
+  T d = 0;
   for (int q = rp[i]; q < rp[i + 1]; ++q) d += val[q] * u[col[q]];
-  r[i] = f[i] + -1.0 * d;
+  r[i] = f[i] + (T)-1 * d;
 }
 
 // I.transMult(r, f_next) (CompColMatrix.java:299-316)
+template <typename T>
 __global__ void k_amg_restrict(int c, const int* __restrict__ qptr, const int* __restrict__ qrow,
-                               const double* __restrict__ qval, const double* __restrict__ r,
-                               double* __restrict__ f, const int* active) {
+                               const T* __restrict__ qval, const T* __restrict__ r, T* __restrict__ f,
+                               const int* active) {
   if (active && *active != 0) return;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= c) return;
-  double dot = 0;
+  T dot = 0;
   for (int q = qptr[j]; q < qptr[j + 1]; ++q) dot += qval[q] * r[qrow[q]];
   f[j] = dot;
 }
 
 // I.multAdd(u_next, u) (CompColMatrix.java:277-296, alpha 1): each row
 // receives its terms in ascending column order
+template <typename T>
 __global__ void k_amg_prolong(int n, const int* __restrict__ prp, const int* __restrict__ pcol,
-                              const double* __restrict__ pval, const double* __restrict__ un,
-                              double* __restrict__ u, const int* active) {
+                              const T* __restrict__ pval, const T* __restrict__ un, T* __restrict__ u,
+                              const int* active) {
   if (active && *active != 0) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double y = u[i];
+  T y = u[i];
   for (int e = prp[i]; e < prp[i + 1]; ++e) y += pval[e] * un[pcol[e]];
   u[i] = y;
 }
 
-__global__ void k_amg_copy(int n, const double* __restrict__ a, double* __restrict__ b, const int* active) {
+template <typename A, typename B>
+__global__ void k_amg_copy(int n, const A* __restrict__ a, B* __restrict__ b, const int* active) {
   if (active && *active != 0) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = a[i];
+  if (i < n) b[i] = (B)a[i];
 }
 
-__global__ void k_amg_zero(int n, double* __restrict__ b, const int* active) {
+template <typename T>
+__global__ void k_amg_zero(int n, T* __restrict__ b, const int* active) {
   if (active && *active != 0) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = 0.0;
+  if (i < n) b[i] = 0;
+}
+
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
 }
 
 int read_int(Context& ctx, const int* d) {
@@ -643,6 +655,8 @@ struct AmgLevel {
   DeviceBuffer<double> pval, qval;
   std::unique_ptr<Precond> smoother;  // SSOR, omegas switched between pre and post
   DeviceBuffer<double> u, f, r;
+  // FP32 copies for the mixed-precision solver: operator, interpolation both ways, work vectors
+  DeviceBuffer<float> valf, pvalf, qvalf, uf, ff, rf;
 };
 
 }  // namespace
@@ -775,6 +789,7 @@ struct AMGPrecond : Precond {
   void setup(Csr& M) override {
     // AMG.setMatrix (AMG.java:224-286)
     Context& c = *ctx;
+    f32_ready = false;
     for (int k = 0; k < M.n; ++k)
       if (M.h_diag[k] < 0)
         throw Error(RSG_MISSING_DIAGONAL, "Matrix is missing a diagonal entry on row " + std::to_string(k + 1));
@@ -834,14 +849,14 @@ struct AMGPrecond : Precond {
     const int eb = blocks_for(n, 256);
     set_ssor_params(l.smoother.get(), 1.0, 1.85, 1);  // preRelax: SSOR(omegaPreF, omegaPreR)
     l.smoother->apply(l.f.get(), l.u.get(), active);
-    RSG_LAUNCH(c, "amg_zero", k_amg_zero, blocks_for(nx.A->n, 256), 256, 0, nx.A->n, nx.u.get(), active);
-    RSG_LAUNCH(c, "amg_resid", k_amg_resid, eb, 256, 0, n, l.A->rowptr.get(), l.A->col.get(), l.val, l.u.get(),
-               l.f.get(), l.r.get(), active);
-    RSG_LAUNCH(c, "amg_restrict", k_amg_restrict, blocks_for(l.c, 256), 256, 0, l.c, l.qptr.get(), l.qrow.get(),
-               l.qval.get(), l.r.get(), nx.f.get(), active);
+    RSG_LAUNCH(c, "amg_zero", k_amg_zero<double>, blocks_for(nx.A->n, 256), 256, 0, nx.A->n, nx.u.get(), active);
+    RSG_LAUNCH(c, "amg_resid", k_amg_resid<double>, eb, 256, 0, n, l.A->rowptr.get(), l.A->col.get(), l.val,
+               l.u.get(), l.f.get(), l.r.get(), active);
+    RSG_LAUNCH(c, "amg_restrict", k_amg_restrict<double>, blocks_for(l.c, 256), 256, 0, l.c, l.qptr.get(),
+               l.qrow.get(), l.qval.get(), l.r.get(), nx.f.get(), active);
     cycle(k + 1, active);
-    RSG_LAUNCH(c, "amg_prolong", k_amg_prolong, eb, 256, 0, n, l.prp.get(), l.pcol.get(), l.pval.get(), nx.u.get(),
-               l.u.get(), active);
+    RSG_LAUNCH(c, "amg_prolong", k_amg_prolong<double>, eb, 256, 0, n, l.prp.get(), l.pcol.get(), l.pval.get(),
+               nx.u.get(), l.u.get(), active);
     set_ssor_params(l.smoother.get(), 1.85, 1.0, 1);  // postRelax: SSOR(omegaPostF, omegaPostR)
     l.smoother->apply(l.f.get(), l.u.get(), active);
   }
@@ -851,11 +866,79 @@ struct AMGPrecond : Precond {
     Context& c = *ctx;
     const int n = L[0].A->n;
     const int eb = blocks_for(n, 256);
-    RSG_LAUNCH(c, "amg_copy", k_amg_copy, eb, 256, 0, n, x, L[0].u.get(), active);
-    RSG_LAUNCH(c, "amg_copy", k_amg_copy, eb, 256, 0, n, b, L[0].f.get(), active);
+    RSG_LAUNCH(c, "amg_copy", (k_amg_copy<double, double>), eb, 256, 0, n, x, L[0].u.get(), active);
+    RSG_LAUNCH(c, "amg_copy", (k_amg_copy<double, double>), eb, 256, 0, n, b, L[0].f.get(), active);
     trans = t;
     cycle(0, active);
-    RSG_LAUNCH(c, "amg_copy", k_amg_copy, eb, 256, 0, n, L[0].u.get(), x, active);
+    RSG_LAUNCH(c, "amg_copy", (k_amg_copy<double, double>), eb, 256, 0, n, L[0].u.get(), x, active);
+  }
+
+  // FP32 copy of the hierarchy, made on the first FP32 apply after a setup:
+  // operators, interpolation and the smoothers' coefficients in FP32 (half
+  // the bytes per V-cycle); the coarsest LU stays FP64.
+  bool f32_ready = false;
+  void build_f32() {
+    Context& c = *ctx;
+    const int m = (int)L.size();
+    for (int k = 0; k < m; ++k) {
+      AmgLevel& l = L[k];
+      const int64_t nnz = std::max(l.A->nnz, 1), n = l.A->n;
+      l.valf.resize(nnz);
+      RSG_LAUNCH(c, "amg_f32", k_to_f32, blocks_for(nnz, 256), 256, 0, nnz, l.val, l.valf.get());
+      if (k < m - 1) {
+        const int64_t pn = (int64_t)l.pval.size();
+        l.pvalf.resize(pn);
+        l.qvalf.resize(pn);
+        RSG_LAUNCH(c, "amg_f32", k_to_f32, blocks_for(pn, 256), 256, 0, pn, l.pval.get(), l.pvalf.get());
+        RSG_LAUNCH(c, "amg_f32", k_to_f32, blocks_for(pn, 256), 256, 0, pn, l.qval.get(), l.qvalf.get());
+      }
+      l.uf.resize(n);
+      l.ff.resize(n);
+      l.rf.resize(n);
+    }
+    f32_ready = true;
+  }
+
+  void cycle_f32(int k, const int* active) {
+    Context& c = *ctx;
+    const int m = (int)L.size();
+    AmgLevel& l = L[k];
+    const int n = l.A->n;
+    const int eb = blocks_for(n, 256);
+    if (k == m - 1) {
+      if (info > 0) throw Error(RSG_SINGULAR, "MatrixSingularException: the coarsest AMG operator is singular");
+      RSG_LAUNCH(c, "amg_coarse_cvt", (k_amg_copy<float, double>), eb, 256, 0, n, l.ff.get(), l.f.get(), active);
+      RSG_LAUNCH(c, "amg_direct", k_dense_solve, 1, 32, 0, nc, lu.get(), piv.get(), l.f.get(), l.u.get(), 0, active);
+      RSG_LAUNCH(c, "amg_coarse_cvt", (k_amg_copy<double, float>), eb, 256, 0, n, l.u.get(), l.uf.get(), active);
+      return;
+    }
+    AmgLevel& nx = L[k + 1];
+    set_ssor_params(l.smoother.get(), 1.0, 1.85, 1);
+    l.smoother->apply_f32(l.ff.get(), l.uf.get(), active);
+    RSG_LAUNCH(c, "amg_zero", k_amg_zero<float>, blocks_for(nx.A->n, 256), 256, 0, nx.A->n, nx.uf.get(), active);
+    RSG_LAUNCH(c, "amg_resid", k_amg_resid<float>, eb, 256, 0, n, l.A->rowptr.get(), l.A->col.get(), l.valf.get(),
+               l.uf.get(), l.ff.get(), l.rf.get(), active);
+    RSG_LAUNCH(c, "amg_restrict", k_amg_restrict<float>, blocks_for(l.c, 256), 256, 0, l.c, l.qptr.get(),
+               l.qrow.get(), l.qvalf.get(), l.rf.get(), nx.ff.get(), active);
+    cycle_f32(k + 1, active);
+    RSG_LAUNCH(c, "amg_prolong", k_amg_prolong<float>, eb, 256, 0, n, l.prp.get(), l.pcol.get(), l.pvalf.get(),
+               nx.uf.get(), l.uf.get(), active);
+    set_ssor_params(l.smoother.get(), 1.85, 1.0, 1);
+    l.smoother->apply_f32(l.ff.get(), l.uf.get(), active);
+  }
+
+  // One FP32 V-cycle from a zero start (the inner stage of the mixed-precision
+  // solver wants a fixed linear preconditioner, unlike MTJ's apply, which
+  // starts from the caller's vector).
+  void apply_f32(const float* b, float* x, const int* active) override {
+    Context& c = *ctx;
+    if (!f32_ready) build_f32();
+    const int n = L[0].A->n;
+    const int eb = blocks_for(n, 256);
+    RSG_LAUNCH(c, "amg_zero", k_amg_zero<float>, eb, 256, 0, n, L[0].uf.get(), active);
+    RSG_LAUNCH(c, "amg_copy", (k_amg_copy<float, float>), eb, 256, 0, n, b, L[0].ff.get(), active);
+    cycle_f32(0, active);
+    RSG_LAUNCH(c, "amg_copy", (k_amg_copy<float, float>), eb, 256, 0, n, L[0].uf.get(), x, active);
   }
 
   void apply(const double* b, double* x, const int* active) override { run(b, x, active, false); }

@@ -884,8 +884,8 @@ SolverPtr make_solver(Context* ctx, int method, int precond, double rtol, double
                       int restart) {
   if (method != RSG_CG && method != RSG_BICGSTAB && method != RSG_GMRES && method != RSG_FGMRES_MIXED)
     throw Error(RSG_UNSUPPORTED, "linear solver not available");
-  if (method == RSG_FGMRES_MIXED && precond != RSG_PC_ILU && precond != RSG_PC_DIAGONAL && precond != RSG_PC_NONE)
-    throw Error(RSG_UNSUPPORTED, "the mixed-precision solver takes ILU, diagonal or no preconditioning");
+  if (method == RSG_FGMRES_MIXED && precond == RSG_PC_SSOR)
+    throw Error(RSG_UNSUPPORTED, "the mixed-precision solver takes ILU, AMG, diagonal or no preconditioning");
   SolverPtr s(new Solver(ctx, method, precond));
   s->rtol = rtol;
   s->atol = atol;
@@ -921,8 +921,8 @@ rsg_status rsg_solver_create(rsg_ctx* ctx, int32_t method, int32_t precond, rsg_
   if (method < RSG_CG || method > RSG_FGMRES_MIXED) return RSG_BAD_ARG;
   rsg_solver* h = new rsg_solver();
   rsg_status st = guarded(&ctx->c, [&] {
-    if (method == RSG_FGMRES_MIXED && precond != RSG_PC_ILU && precond != RSG_PC_DIAGONAL && precond != RSG_PC_NONE)
-      throw rsg::Error(RSG_UNSUPPORTED, "the mixed-precision solver takes ILU, diagonal or no preconditioning");
+    if (method == RSG_FGMRES_MIXED && precond == RSG_PC_SSOR)
+      throw rsg::Error(RSG_UNSUPPORTED, "the mixed-precision solver takes ILU, AMG, diagonal or no preconditioning");
     h->s.reset(new rsg::Solver(&ctx->c, method, precond));
   });
   if (st != RSG_OK) {

@@ -10,6 +10,18 @@ namespace rsg {
 
 constexpr int SELL_C = 32;
 
+// Ring schedule of an ILU(0) sweep for one cluster of C CTAs (precond.cu,
+// k_sweep_ring): CTAs own contiguous row blocks, every level has
+// RING_SLICES slices (W = RING_SLICES / C per CTA), each value is pushed only
+// to the CTAs that read it.  R == 0: no ring schedule for this pattern.
+struct RingPlan {
+  int C = 0, nlev = 0, R = 0, slack = 0;
+  DeviceBuffer<int> slice_base, row, len, ridx, src, diag_src, expect;
+  DeviceBuffer<unsigned short> pmask, nbr;
+  DeviceBuffer<double> val, diag;
+  DeviceBuffer<float> valf, diagf;
+};
+
 // Level schedule of a triangular sweep, laid out as SELL-32 slices that never
 // straddle a level: slot (slice s, lane l, k) lives at base[s] + 32*k + l.
 struct SweepPlan {
@@ -22,12 +34,7 @@ struct SweepPlan {
   DeviceBuffer<double> diag;  // diagonal per slot row (upper sweeps)
   DeviceBuffer<float> diagf;
   int max_rows_per_level = 0;
-  // Push-ring schedule for one cluster whose warps take one slice each
-  // (RING_SLICES warps in all): every level fits and every entry refers to a
-  // row of the last ring_R - 2 levels.  ring_R == 0: unavailable.
-  int ring_R = 0, ring_slot = 0;
-  DeviceBuffer<int> ridx;            // per entry slot: ring index of the column's value
-  DeviceBuffer<int> ring_expect[2];  // clusters of 8 / 16 CTAs: per level and rank, rows the others push
+  RingPlan ring;              // ILU sweeps only
 };
 
 constexpr int RING_SLICES = 64;

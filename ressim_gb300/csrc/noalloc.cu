@@ -4,11 +4,15 @@
 // a real-time loop that forbids allocation.
 //
 // All workspace lives in one file-scope static device array.  The CUDA
-// driver reserves it when the library's module is loaded, and every GPU
-// that loads the library holds it until the process exits.  Host code must
-// not use the array's name as a device address (on the host it names a
-// shadow, not device memory), so the first call on each device looks up
-// the device address with cudaGetSymbolAddress and caches it.
+// driver reserves it when it loads the library's module on a device (with
+// the default lazy module loading: at the first call on that device), and
+// that device holds it until the process exits.  Host code must not use the
+// array's name as a device address (on the host it names a shadow, not
+// device memory), so the first call on each device looks up the device
+// address with cudaGetSymbolAddress and caches it.  A cudaDeviceReset
+// unloads the module and makes the cached address stale: after a reset of
+// a device, this entry point must not be called on it again in the same
+// process.
 //
 // The kernels compute exactly what rsg_solver_solve computes for CG with the
 // diagonal preconditioner (mtj/src/no/uib/cipr/matrix/sparse/CG.java:58-87,
@@ -62,8 +66,10 @@ enum { E_TOP = 1, E_RHO, E_ALPHA, E_NEXT };
 __device__ void n_epilogue(int epi, NState* s, double t, double* hist) {
   switch (epi) {
     case E_TOP: {
+      // a zero diagonal found by k_n_init stays the call's status even when
+      // the initial residual already meets the tolerance
       int m = n_monitor(s, sqrt(t), hist);
-      if (m != 0) s->status = m;
+      if (m != 0) atomicCAS(&s->status, 0, m);
       break;
     }
     case E_RHO:
@@ -76,7 +82,7 @@ __device__ void n_epilogue(int epi, NState* s, double t, double* hist) {
       s->iter++;
       s->first = 0;
       int m = n_monitor(s, sqrt(t), hist);
-      if (m != 0) s->status = m;
+      if (m != 0) atomicCAS(&s->status, 0, m);
       break;
     }
   }
@@ -196,6 +202,17 @@ __global__ void __launch_bounds__(RT) k_n_update(int n, double* x, Scr w) {
   n_reduce(acc, w, E_NEXT);
 }
 
+// Launches one kernel and returns that launch's own error, leaving any
+// error the caller's thread recorded before this call untouched.
+template <typename... KArgs, typename... Args>
+cudaError_t launch(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = st;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 }  // namespace
 
 extern "C" rsg_status rsg_cg_diagonal_noalloc(int32_t device, void* stream, int32_t n, int32_t nnz,
@@ -252,7 +269,10 @@ extern "C" rsg_status rsg_cg_diagonal_noalloc(int32_t device, void* stream, int3
     }
     const int nblk = std::max(1, std::min((n + RT - 1) / RT, MAX_BLOCKS));
     const int eb = (n + 255) / 256;
-    k_n_init<<<nblk, RT, 0, st>>>(n, d_row_ptr, d_col, d_val, d_x, d_b, w);
+    if (launch(k_n_init, nblk, RT, st, n, d_row_ptr, d_col, d_val, (const double*)d_x, d_b, w) != cudaSuccess) {
+      status = RSG_CUDA_ERROR;
+      break;
+    }
     for (int guard = 0; guard <= max_iter + 1; ++guard) {
       if (cudaMemcpyAsync(&hs, w.s, sizeof(hs), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess) {
@@ -260,16 +280,14 @@ extern "C" rsg_status rsg_cg_diagonal_noalloc(int32_t device, void* stream, int3
         break;
       }
       if (hs.status != 0) break;
-      k_n_precond_dot<<<nblk, RT, 0, st>>>(n, w);
-      k_n_p<<<eb, 256, 0, st>>>(n, w);
-      k_n_spmv_dot<<<nblk, RT, 0, st>>>(n, d_row_ptr, d_col, d_val, w);
-      k_n_update<<<nblk, RT, 0, st>>>(n, d_x, w);
+      if (launch(k_n_precond_dot, nblk, RT, st, n, w) != cudaSuccess || launch(k_n_p, eb, 256, st, n, w) != cudaSuccess ||
+          launch(k_n_spmv_dot, nblk, RT, st, n, d_row_ptr, d_col, d_val, w) != cudaSuccess ||
+          launch(k_n_update, nblk, RT, st, n, d_x, w) != cudaSuccess) {
+        status = RSG_CUDA_ERROR;
+        break;
+      }
     }
     if (status != RSG_OK) break;
-    if (cudaGetLastError() != cudaSuccess) {
-      status = RSG_CUDA_ERROR;
-      break;
-    }
     if (info) {
       info->iterations = hs.iter;
       info->residual = hs.residual;

@@ -211,32 +211,69 @@ __global__ void __launch_bounds__(256) k_sweep_pipelined(SweepArgs<T> a) {
   }
 }
 
-// ILU sweeps with the computed values exchanged through distributed shared
-// memory instead of L2.  Every CTA of the cluster keeps a replica of the
-// values of the last R levels (a ring of R level slots in its shared
-// memory).  The lane that computes a row writes the value into its own
-// replica and pushes it into the other CTAs' replicas with st.async, whose
-// completion is counted in bytes on the receiving CTA's mbarrier of that
-// level slot.  Besides its rows, each CTA pushes one 8-byte token per level
-// to every other CTA once it has finished the previous level, so a level's
-// phase completes only when every CTA is done with the level before it: no
-// CTA runs more than one level ahead of another.  A CTA starts level l once
-// its mbarrier of level l-1 has seen every byte owed to it (armed with
-// expect_tx from a host-built table) and a CTA barrier has published its
-// own rows; all operand gathers are then local shared-memory loads and there
-// is no cluster-wide barrier per level.
+// ILU sweeps on one thread-block cluster whose CTAs own contiguous blocks
+// of rows, with the computed values exchanged through distributed shared
+// memory.  A row-block partition keeps most of a row's operands inside its
+// CTA: on a stencil pattern in natural order a block of grid planes reads
+// only the edge plane of the block before it (lower sweep) or after it
+// (upper sweep), so each value is pushed to the few CTAs that read it
+// instead of to every CTA.
 //
-// Slot reuse: a CTA pushing level l into slot l mod R has seen the token of
-// every CTA for level l-1, so each of them has finished level l-2 and is at
-// most computing level l-1, whose operands lie in levels >= l-1-(R-2) when
-// R >= lookback + 2; slot l mod R held level l-R, which nobody reads any
-// more, and its mbarrier phase for level l-R has completed.
+// Layout (RingPlan): every plan level has RING_SLICES slices; CTA c owns
+// slices [c W, c W + W) of each level (W = RING_SLICES / C warps, one slice
+// per warp), holding its rows of that level packed from the first slot.  A
+// level of the dependency schedule whose rows of one CTA exceed W * 32 is
+// split into consecutive plan levels (rows of one level are independent, so
+// any order among them is valid).
+//
+// Every CTA keeps a replica of the last R levels (a ring of R level slots of
+// RING_SLICES * 32 values in its shared memory; each value at its slot
+// position in the level).  The lane that computes a row writes the value into
+// its own replica; the even lane of each lane pair pushes the pair's two
+// values with st.async into the replicas of the CTAs that read either of
+// them (a per-pair CTA mask from the plan).  Completion is counted in bytes on
+// the receiving CTA's mbarrier of that level slot, armed with expect_tx from
+// the plan's table of values each CTA receives per level.  Besides data, each
+// CTA pushes one 8-byte token per level to each CTA it exchanges values with
+// (its neighbours: the mask is symmetric) when it starts level l, meaning
+// "finished level l-1"; the token counts towards the neighbour's slot of
+// level l + S (S = the plan's slack), so a CTA starts level l only after
+// every neighbour has finished level l-2-S.  Data flows one way between two
+// CTAs (a lower sweep's blocks read earlier blocks), so with S > 0 each CTA
+// can run up to S + 1 levels ahead of the CTA it feeds: the pushes of level
+// l-1 have landed long before the reader starts level l, and the transfer
+// latency leaves the chain of levels.
+//
+// Slot reuse (R >= lookback + 2 + S and R >= 2 S + 2): a CTA pushing level l
+// into a neighbour's slot l mod R has seen that neighbour's token for level
+// l-2-S (in its own wait for level l-1), so the neighbour computes level
+// l-1-S or later, whose operands lie in levels >= l-1-S-lookback > l-R; slot
+// l mod R held level l-R, which it no longer reads, and that slot's mbarrier
+// phase for level l-R has completed (the neighbour waited on it at level
+// l-R+1 <= l-1-S).  A token for level l+S lands in slot (l+S) mod R, whose
+// phase for level l+S-R completed at level l+S-R+1 <= l-1-S.  Bytes of a
+// level can reach a slot before its owner arms it for that level: the phase
+// cannot complete before the owner's own arrival.
 struct RingArgs {
-  int R;                // ring depth in levels (>= lookback + 2)
-  int slot;             // values per level slot (slices x 32)
-  const int* ridx;      // per entry slot: ring index of the column's value
-  const int* expect;    // per level and CTA rank: rows pushed by the other CTAs
-  int* err;             // set to 1 + level when a wait runs out
+  int nlev, R;
+  int slack;                   // levels a CTA may run ahead of a neighbour beyond one
+  const int* slice_base;       // per slice: offset of its first entry
+  const int* row;              // per slot: row id, -1 if empty
+  const int* len;              // per slot: entries of the row
+  const int* ridx;             // per entry: ring index of the column's value
+  const unsigned short* pmask; // per slot (even lanes): CTAs that read either value of the pair
+  const int* expect;           // per level and CTA: values pushed to it
+  const unsigned short* nbr;   // per CTA: CTAs it exchanges values or tokens with
+  int* err;                    // set to 1 + level when a wait runs out
+};
+
+template <typename T>
+struct RingVals {
+  const T* val;
+  const T* diag;
+  const T* b;
+  T* x;
+  const int* active;
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -295,19 +332,70 @@ __device__ __forceinline__ void push_pair(unsigned remote, float v0, float v1, u
                : "memory");
 }
 
+constexpr int RING_TOKEN_BYTES = 8;
+constexpr int RING_MAX_CTAS = 16;
+constexpr int RING_SLOT = RING_SLICES * 32;  // values per level slot
+constexpr size_t RING_SMEM_MAX = 200 * 1024;
+
+// RSG_SWEEP=pipelined switches the ring walks off; RSG_RING_CTAS=8 plans
+// them for clusters of 8 CTAs with 8 warps each instead of 16 with 4.
+static bool ring_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("RSG_SWEEP");
+    return !(e && std::string(e) == "pipelined");
+  }();
+  return on;
+}
+
+static int ring_ctas() {
+  static const int c = [] {
+    const char* e = getenv("RSG_RING_CTAS");
+    return (e && atoi(e) == 8) ? 8 : 16;
+  }();
+  return c;
+}
+
+// Dynamic shared memory of k_sweep_ring: ring, mbarriers, tokens.
+template <typename T>
+__host__ __device__ inline size_t ring_smem_bytes(int R) {
+  return sizeof(T) * (size_t)R * RING_SLOT + 8 * (size_t)R + RING_TOKEN_BYTES * (size_t)RING_MAX_CTAS;
+}
+
+struct RingMeta {
+  int row, len, base, slot;
+  unsigned pm;
+};
+
+template <typename T, int MAXW>
+struct RingRow {
+  int row, len, base;
+  unsigned pm;
+  T b, d;
+  T v[MAXW];
+  int c[MAXW];
+};
+
+__device__ __forceinline__ RingMeta ring_meta(const RingArgs& g, int l, int gwarp, int lane) {
+  RingMeta m{-1, 0, 0, 0, 0u};
+  if (l >= g.nlev) return m;
+  const int s = l * RING_SLICES + gwarp;
+  m.slot = s * 32 + lane;
+  m.row = g.row[m.slot];
+  m.len = g.len[m.slot];
+  m.base = g.slice_base[s] + lane;
+  m.pm = g.pmask[m.slot];
+  return m;
+}
+
 template <int KIND, typename T, int MAXW>
-__device__ __forceinline__ void load_ring_coeffs(const SweepArgs<T>& a, const RingArgs& g, const int* ls,
-                                                 const SlotMeta& m, int l, int gwarp, int lane,
-                                                 RowPrefetch<T, MAXW>& p) {
+__device__ __forceinline__ void ring_coeffs(const RingArgs& g, const RingVals<T>& a, const RingMeta& m,
+                                            RingRow<T, MAXW>& p) {
   p.row = m.row;
   p.len = m.row >= 0 ? m.len : 0;
   p.base = m.base;
-  const int r = m.row >= 0 ? m.row : 0;
-  p.b = a.b[r];
-  if (KIND == SW_ILU_UPPER) {
-    const int s = (m.row >= 0) ? ls[l] + gwarp : 0;
-    p.d = a.diag[s * 32 + lane];
-  }
+  p.pm = m.row >= 0 ? m.pm : 0u;
+  p.b = a.b[m.row >= 0 ? m.row : 0];
+  if (KIND == SW_ILU_UPPER) p.d = a.diag[m.row >= 0 ? m.slot : 0];
 #pragma unroll
   for (int k = 0; k < MAXW; ++k)
     if (k < p.len) {
@@ -316,71 +404,56 @@ __device__ __forceinline__ void load_ring_coeffs(const SweepArgs<T>& a, const Ri
     }
 }
 
-constexpr int RING_TOKEN_BYTES = 8;
-constexpr int RING_MAX_CTAS = 16;
-
-// Dynamic shared memory of k_sweep_ring: ring, mbarriers, tokens, level offsets.
-template <typename T>
-__host__ __device__ inline size_t ring_smem_bytes(int R, int slot, int nlev) {
-  return sizeof(T) * (size_t)R * slot + 8 * (size_t)R + RING_TOKEN_BYTES * (size_t)RING_MAX_CTAS +
-         4 * (size_t)(nlev + 1);
-}
-
 template <int KIND, typename T, int MAXW, int RING_CTAS>
-__global__ void __launch_bounds__(RING_SLICES / RING_CTAS * 32) k_sweep_ring(SweepArgs<T> a, RingArgs g) {
+__global__ void __launch_bounds__(RING_SLICES / RING_CTAS * 32) k_sweep_ring(RingArgs g, RingVals<T> a) {
   constexpr int RING_WARPS = RING_SLICES / RING_CTAS;
   if (a.active && *a.active != 0) return;  // uniform over the cluster
   extern __shared__ __align__(16) unsigned char smem[];
   T* ring = reinterpret_cast<T*>(smem);
-  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + sizeof(T) * (size_t)g.R * g.slot);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + sizeof(T) * (size_t)g.R * RING_SLOT);
   unsigned long long* tok = bar + g.R;
-  int* ls = reinterpret_cast<int*>(tok + RING_MAX_CTAS);
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
   const int lane = threadIdx.x & 31;
   const int gwarp = (int)rank * RING_WARPS + (threadIdx.x >> 5);
   const unsigned ring0 = smem_addr(ring), bar0 = smem_addr(bar), tok0 = smem_addr(tok);
   if (threadIdx.x < g.R) mbar_init(bar0 + 8 * threadIdx.x, 1);
-  for (int q = threadIdx.x; q <= a.nlev; q += blockDim.x) ls[q] = a.level_slices[q];
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   cluster.sync();  // every replica's barriers exist before the first push
-  unsigned rring[RING_CTAS], rbar[RING_CTAS];
-#pragma unroll
-  for (int c = 0; c < RING_CTAS; ++c) {
-    rring[c] = cluster_addr(ring0, c);
-    rbar[c] = cluster_addr(bar0, c);
-  }
-  RowPrefetch<T, MAXW> cur, nxt;
-  SlotMeta m1 = load_meta(a, ls, 1, gwarp, lane);
+  const unsigned nbr = g.nbr[rank];
+  const unsigned token_tx = RING_TOKEN_BYTES * __popc(nbr);
+  RingRow<T, MAXW> cur, nxt;
+  RingMeta m1 = ring_meta(g, 1, gwarp, lane);
   {
-    SlotMeta m0 = load_meta(a, ls, 0, gwarp, lane);
-    load_ring_coeffs<KIND, T, MAXW>(a, g, ls, m0, 0, gwarp, lane, cur);
+    const RingMeta m0 = ring_meta(g, 0, gwarp, lane);
+    ring_coeffs<KIND, T, MAXW>(g, a, m0, cur);
   }
-  const unsigned token_tx = RING_TOKEN_BYTES * (RING_CTAS - 1);
-  int exp_cur = (threadIdx.x == 0 && a.nlev > 0) ? g.expect[rank] : 0;
+  int exp_cur = (threadIdx.x == 0 && g.nlev > 0) ? g.expect[rank] : 0;
   int slot_l = 0, par_l = 0, slot_p = 0, par_p = 0;  // level l and level l-1
   bool ok = true;
-  for (int l = 0; l < a.nlev; ++l) {
-    if (threadIdx.x == 0) mbar_arm(bar0 + 8 * slot_l, (unsigned)(exp_cur * sizeof(T)) + token_tx);
-    const int exp_nxt = (threadIdx.x == 0 && l + 1 < a.nlev) ? g.expect[(l + 1) * RING_CTAS + rank] : 0;
-    const SlotMeta m2 = load_meta(a, ls, l + 2, gwarp, lane);
-    load_ring_coeffs<KIND, T, MAXW>(a, g, ls, m1, l + 1, gwarp, lane, nxt);
+  for (int l = 0; l < g.nlev; ++l) {
+    if (threadIdx.x == 0) mbar_arm(bar0 + 8 * slot_l, (unsigned)(exp_cur * sizeof(T)) + (l >= g.slack ? token_tx : 0u));
+    const int exp_nxt = (threadIdx.x == 0 && l + 1 < g.nlev) ? g.expect[(l + 1) * RING_CTAS + rank] : 0;
+    const RingMeta m2 = ring_meta(g, l + 2, gwarp, lane);
+    ring_coeffs<KIND, T, MAXW>(g, a, m1, nxt);
     const int late = (l > 0) ? !mbar_wait(bar0 + 8 * slot_p, par_p) : 0;
     if (__syncthreads_or(late)) {
       if (threadIdx.x == 0) atomicCAS(g.err, 0, 1 + l);
       ok = false;
       break;
     }
-    if (threadIdx.x == 0) {
-      // this CTA has finished level l-1
-#pragma unroll
-      for (int c = 0; c < RING_CTAS; ++c)
-        if (c != (int)rank)
-          push_b64(cluster_addr(tok0, c) + RING_TOKEN_BYTES * rank, (unsigned long long)l, rbar[c] + 8 * slot_l);
+    if (threadIdx.x == 0 && l + g.slack < g.nlev) {
+      // this CTA has finished level l-1: a token for the neighbours' slot of level l + slack
+      const int ts = slot_l + g.slack < g.R ? slot_l + g.slack : slot_l + g.slack - g.R;
+      for (unsigned m = nbr; m; m &= m - 1) {
+        const unsigned c = __ffs(m) - 1;
+        push_b64(cluster_addr(tok0, c) + RING_TOKEN_BYTES * rank, (unsigned long long)l,
+                 cluster_addr(bar0, c) + 8 * ts);
+      }
     }
     const bool act = cur.row >= 0;
     T v = 0;
-    const int own = slot_l * g.slot + gwarp * 32 + lane;
+    const int own = slot_l * RING_SLOT + gwarp * 32 + lane;
     if (act) {
       T sum = 0;
 #pragma unroll
@@ -394,15 +467,17 @@ __global__ void __launch_bounds__(RING_SLICES / RING_CTAS * 32) k_sweep_ring(Swe
       ring[own] = v;
       a.x[cur.row] = v;
     }
-    // the even lane of each pair pushes both values (rows of a level are
-    // packed from its first slot, so a pair with an active odd lane has an
-    // active even lane; an unused odd slot is never read)
+    // the even lane of each pair pushes both values to the CTAs that read
+    // them (rows of a level are packed from the CTA's first slot, so a pair
+    // with an active odd lane has an active even lane; an unused odd slot is
+    // never read)
     const T v_odd = __shfl_down_sync(0xffffffffu, v, 1);
     if (act && !(lane & 1)) {
       const unsigned off = (unsigned)(own * sizeof(T)), boff = (unsigned)(8 * slot_l);
-#pragma unroll
-      for (int c = 0; c < RING_CTAS; ++c)
-        if (c != (int)rank) push_pair(rring[c] + off, v, v_odd, rbar[c] + boff);
+      for (unsigned m = cur.pm; m; m &= m - 1) {
+        const unsigned c = __ffs(m) - 1;
+        push_pair(cluster_addr(ring0, c) + off, v, v_odd, cluster_addr(bar0, c) + boff);
+      }
     }
     cur = nxt;
     m1 = m2;
@@ -414,10 +489,10 @@ __global__ void __launch_bounds__(RING_SLICES / RING_CTAS * 32) k_sweep_ring(Swe
       par_l ^= 1;
     }
   }
-  if (ok && a.nlev > 0) {
+  if (ok && g.nlev > 0) {
     // everything owed to this CTA lands before any CTA may exit
     if (!mbar_wait(bar0 + 8 * slot_p, par_p)) {
-      atomicCAS(g.err, 0, 1 + a.nlev);
+      atomicCAS(g.err, 0, 1 + g.nlev);
       ok = false;
     }
   }
@@ -565,6 +640,217 @@ __global__ void k_diag_apply(int n, const T* __restrict__ inv, const T* __restri
   if (i < n) x[i] = b[i] * inv[i];
 }
 
+// ------------------------------------------------------- ring planning ----
+// Host form of a RingPlan (see k_sweep_ring).  Rows belong to CTAs in
+// contiguous blocks (owner = row * C / n); each dependency level is split
+// into plan levels of at most W * 32 rows per CTA.
+struct HostRing {
+  int C = 0, nlev = 0, R = 0, slack = 0;
+  std::vector<int> slice_base, row, len, ridx, src, diag_src, expect;
+  std::vector<unsigned short> pmask, nbr;
+};
+
+// Largest padded slot count accepted for a ring plan: levels hold
+// RING_SLOT slots whether or not they are full, so a pattern with very many
+// narrow levels (a tridiagonal matrix) walks with the plain cluster kernels.
+static int64_t ring_slot_budget(int n) { return 8 * (int64_t)n + (int64_t)8 * 1024 * 1024; }
+
+// Builds the ring schedule of one sweep.  entries: 0 strictly lower part, 1
+// strictly upper part; upper_levels: dependencies on higher rows.  Returns
+// false when no schedule exists within the shared-memory and slot limits.
+static bool plan_ring(int n, const std::vector<int>& rp, const std::vector<int>& cl, const std::vector<int>& dg,
+                      bool upper_levels, int entries, int C, size_t max_smem, HostRing& H) {
+  if (n <= 0 || C < 1 || C > RING_MAX_CTAS || RING_SLICES % C) return false;
+  const int W = RING_SLICES / C, cap = W * 32;
+  auto ent = [&](int r, int& q0, int& q1) {
+    if (entries == 0) {
+      q0 = rp[r];
+      q1 = dg[r];
+    } else {
+      q0 = dg[r] + 1;
+      q1 = rp[r + 1];
+    }
+  };
+  std::vector<int> lev(n, 0);
+  if (!upper_levels) {
+    for (int i = 0; i < n; ++i) {
+      int L = 0, q0, q1;
+      ent(i, q0, q1);
+      for (int q = q0; q < q1; ++q) L = std::max(L, lev[cl[q]] + 1);
+      lev[i] = L;
+    }
+  } else {
+    for (int i = n - 1; i >= 0; --i) {
+      int L = 0, q0, q1;
+      ent(i, q0, q1);
+      for (int q = q0; q < q1; ++q) L = std::max(L, lev[cl[q]] + 1);
+      lev[i] = L;
+    }
+  }
+  int ndep = 0;
+  for (int i = 0; i < n; ++i) ndep = std::max(ndep, lev[i] + 1);
+  auto owner = [&](int r) { return (int)((int64_t)r * C / n); };
+  // rows per (dependency level, CTA) and the plan levels of each dependency level
+  std::vector<int> cnt((size_t)ndep * C, 0);
+  for (int i = 0; i < n; ++i) cnt[(size_t)lev[i] * C + owner(i)]++;
+  std::vector<int> pl0(ndep + 1, 0);
+  for (int L = 0; L < ndep; ++L) {
+    int sub = 1;
+    for (int c = 0; c < C; ++c) sub = std::max(sub, (cnt[(size_t)L * C + c] + cap - 1) / cap);
+    pl0[L + 1] = pl0[L] + sub;
+  }
+  const int nlev = pl0[ndep];
+  if ((int64_t)nlev * RING_SLOT > ring_slot_budget(n)) return false;
+  std::vector<int> plev(n), ppos(n);
+  std::fill(cnt.begin(), cnt.end(), 0);
+  for (int i = 0; i < n; ++i) {  // ascending rows within a CTA's level
+    const int c = owner(i);
+    const int k = cnt[(size_t)lev[i] * C + c]++;
+    plev[i] = pl0[lev[i]] + k / cap;
+    ppos[i] = c * cap + k % cap;
+  }
+  int look = 0;
+  for (int i = 0; i < n; ++i) {
+    int q0, q1;
+    ent(i, q0, q1);
+    for (int q = q0; q < q1; ++q) look = std::max(look, plev[i] - plev[cl[q]]);
+  }
+  // the deepest ring that fits gives the most slack (at most the lookback: R >= 2 S + 2)
+  if (ring_smem_bytes<double>(look + 2) > max_smem) return false;
+  int S = 0;
+  while (S < look && ring_smem_bytes<double>(look + 3 + S) <= max_smem) ++S;
+  const int R = look + 2 + S;
+  const size_t nslot = (size_t)nlev * RING_SLOT, nslice = (size_t)nlev * RING_SLICES;
+  H.C = C;
+  H.nlev = nlev;
+  H.R = R;
+  H.slack = S;
+  H.row.assign(nslot, -1);
+  H.len.assign(nslot, 0);
+  H.diag_src.assign(nslot, -1);
+  std::vector<int> width(nslice, 0);
+  for (int i = 0; i < n; ++i) {
+    int q0, q1;
+    ent(i, q0, q1);
+    const size_t slot = (size_t)plev[i] * RING_SLOT + ppos[i];
+    H.row[slot] = i;
+    H.len[slot] = q1 - q0;
+    H.diag_src[slot] = dg[i];
+    width[slot / 32] = std::max(width[slot / 32], q1 - q0);
+  }
+  H.slice_base.assign(nslice + 1, 0);
+  int64_t pos = 0;
+  for (size_t s = 0; s < nslice; ++s) {
+    H.slice_base[s] = (int)pos;
+    pos += (int64_t)width[s] * 32;
+    if (pos > INT32_MAX) return false;
+  }
+  H.slice_base[nslice] = (int)pos;
+  H.ridx.assign(std::max<int64_t>(pos, 1), 0);
+  H.src.assign(std::max<int64_t>(pos, 1), -1);
+  // which CTAs read each row's value
+  std::vector<unsigned short> mask(n, 0);
+  for (int i = 0; i < n; ++i) {
+    int q0, q1;
+    ent(i, q0, q1);
+    const size_t slot = (size_t)plev[i] * RING_SLOT + ppos[i];
+    const int64_t b = H.slice_base[slot / 32] + (int64_t)(slot % 32);
+    for (int q = q0, k = 0; q < q1; ++q, ++k) {
+      const int j = cl[q];
+      H.src[b + 32 * k] = q;
+      H.ridx[b + 32 * k] = (plev[j] % R) * RING_SLOT + ppos[j];
+      if (owner(j) != owner(i)) mask[j] |= (unsigned short)(1u << owner(i));
+    }
+  }
+  H.pmask.assign(nslot, 0);
+  H.expect.assign((size_t)nlev * C, 0);
+  H.nbr.assign(C, 0);
+  for (size_t s0 = 0; s0 < nslot; s0 += 2) {
+    const int r0 = H.row[s0], r1 = H.row[s0 + 1];
+    if (r0 < 0) continue;
+    const unsigned short m = (unsigned short)(mask[r0] | (r1 >= 0 ? mask[r1] : 0));
+    H.pmask[s0] = m;
+    const int l = (int)(s0 / RING_SLOT), c = owner(r0);
+    H.nbr[c] |= m;
+    for (int t = 0; t < C; ++t)
+      if (m >> t & 1) H.expect[(size_t)l * C + t] += 2;
+  }
+  for (int c = 0; c < C; ++c)
+    for (int t = 0; t < C; ++t)
+      if (H.nbr[c] >> t & 1) H.nbr[t] |= (unsigned short)(1u << c);
+  return true;
+}
+
+// Independent check of a ring schedule against the matrix: every row is
+// placed once, every slot and entry index stays inside its arrays, every
+// operand of a row lies in an earlier level within the ring's reach and is
+// either the CTA's own value or pushed to it, and the expected counts equal
+// the values pushed.  Returns an empty string when the schedule is sound.
+static std::string check_ring(int n, const std::vector<int>& rp, const std::vector<int>& cl,
+                              const std::vector<int>& dg, int entries, const HostRing& H) {
+  const int C = H.C, R = H.R, W = RING_SLICES / C;
+  const size_t nslot = (size_t)H.nlev * RING_SLOT;
+  if (H.row.size() != nslot || H.len.size() != nslot || H.pmask.size() != nslot) return "slot arrays";
+  if (H.slice_base.size() != (size_t)H.nlev * RING_SLICES + 1) return "slice offsets";
+  if (R < 2 || ring_smem_bytes<double>(R) > RING_SMEM_MAX) return "ring depth";
+  if (H.slack < 0 || R < 2 * H.slack + 2) return "slack";
+  const int64_t nent = H.slice_base.back();
+  std::vector<int> plev(n, -1), ppos(n, -1);
+  auto owner = [&](int r) { return (int)((int64_t)r * C / n); };
+  for (size_t s = 0; s < nslot; ++s) {
+    const int r = H.row[s];
+    if (r < -1 || r >= n) return "row id out of range";
+    if (r < 0) {
+      if (H.pmask[s]) return "mask on an empty slot";
+      continue;
+    }
+    if (plev[r] >= 0) return "row placed twice";
+    plev[r] = (int)(s / RING_SLOT);
+    ppos[r] = (int)(s % RING_SLOT);
+    if (ppos[r] / (W * 32) != owner(r)) return "row outside its CTA's slots";
+    if ((s & 1) && H.row[s - 1] < 0) return "odd lane active without its even lane";
+  }
+  for (int i = 0; i < n; ++i)
+    if (plev[i] < 0) return "row missing";
+  std::vector<int> got((size_t)H.nlev * C, 0);
+  for (size_t s = 0; s < nslot; ++s) {
+    const int r = H.row[s];
+    if (r < 0) continue;
+    const int q0 = entries == 0 ? rp[r] : dg[r] + 1, q1 = entries == 0 ? dg[r] : rp[r + 1];
+    if (H.len[s] != q1 - q0) return "row length";
+    const size_t sl = s / 32;
+    const int64_t w = (int64_t)(H.slice_base[sl + 1] - H.slice_base[sl]) / 32;
+    if (H.len[s] > w) return "row longer than its slice";
+    for (int k = 0; k < H.len[s]; ++k) {
+      const int64_t e = H.slice_base[sl] + (int64_t)(s % 32) + 32 * (int64_t)k;
+      if (e < 0 || e >= nent) return "entry index out of range";
+      const int j = cl[q0 + k];
+      if (H.src[e] != q0 + k) return "entry source";
+      if (H.ridx[e] < 0 || H.ridx[e] >= R * RING_SLOT) return "ring index out of range";
+      if (H.ridx[e] != (plev[j] % R) * RING_SLOT + ppos[j]) return "ring index";
+      if (plev[j] >= plev[r] || plev[r] - plev[j] > R - 2 - H.slack) return "operand outside the ring's reach";
+      if (owner(j) != owner(r)) {
+        const size_t sj = (size_t)plev[j] * RING_SLOT + ppos[j];
+        if (!(H.pmask[sj & ~(size_t)1] >> owner(r) & 1)) return "operand not pushed to its reader";
+      }
+    }
+    if (!(s & 1)) {
+      const unsigned m = H.pmask[s];
+      if (m >> owner(r) & 1) return "value pushed to its own CTA";
+      if (m & ~H.nbr[owner(r)]) return "push target is not a neighbour";
+      for (int t = 0; t < C; ++t)
+        if (m >> t & 1) got[(size_t)(s / RING_SLOT) * C + t] += 2;
+    }
+  }
+  if (got != H.expect) return "expected counts";
+  for (int c = 0; c < C; ++c) {
+    if (H.nbr[c] >> c & 1) return "neighbour of itself";
+    for (int t = 0; t < C; ++t)
+      if ((H.nbr[c] >> t & 1) != (H.nbr[t] >> c & 1)) return "neighbour masks not symmetric";
+  }
+  return "";
+}
+
 // ------------------------------------------------------------ planning ----
 // entries: 0 lower part, 1 upper part, 2 full row without the diagonal.
 // upper_levels: schedule by dependencies on higher rows (backward sweeps).
@@ -659,52 +945,8 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
       }
     }
   // push-ring schedule (lower or upper ILU parts only)
-  std::vector<int> ridx, expect[2];
-  P.ring_R = 0;
-  if (entries != 2) {
-    int max_sl = 0, look = 0;
-    for (int l = 0; l < nlev; ++l) max_sl = std::max(max_sl, level_slices[l + 1] - level_slices[l]);
-    std::vector<int> ring_pos(n);  // slice offset within the level * 32 + lane
-    for (int l = 0; l < nlev; ++l)
-      for (int t = 0; t < cnt[l + 1] - cnt[l]; ++t) ring_pos[order[cnt[l] + t]] = t;
-    for (int i = 0; i < n; ++i) {
-      int b0, b1, c0, c1;
-      row_entries(i, b0, b1, c0, c1);
-      for (int q = b0; q < b1; ++q) look = std::max(look, lev[i] - lev[cl[q]]);
-    }
-    const int R = look + 2;
-    if (max_sl <= RING_SLICES && R <= 32) {
-      P.ring_R = R;
-      P.ring_slot = max_sl * 32;
-      ridx.assign(col.size(), 0);
-      for (int s = 0; s < ns; ++s)
-        for (int lane = 0; lane < 32; ++lane) {
-          int r = row[(size_t)s * 32 + lane];
-          if (r < 0) continue;
-          for (int k = 0; k < len[(size_t)s * 32 + lane]; ++k) {
-            int c = col[base[s] + 32 * k + lane];
-            ridx[base[s] + 32 * k + lane] = (lev[c] % R) * P.ring_slot + ring_pos[c];
-          }
-        }
-      for (int e = 0; e < 2; ++e) {
-        const int C = 8 << e, W = RING_SLICES / C;
-        auto& ex = expect[e];
-        ex.assign((size_t)nlev * C, 0);
-        for (int l = 0; l < nlev; ++l) {
-          const int rows = cnt[l + 1] - cnt[l];
-          // values pushed by each CTA: its rows, rounded up to whole lane pairs
-          int total = 0;
-          std::vector<int> sent(C);
-          for (int c = 0; c < C; ++c) {
-            const int own = std::min(std::max(rows - c * W * 32, 0), W * 32);
-            sent[c] = 2 * ((own + 1) / 2);
-            total += sent[c];
-          }
-          for (int c = 0; c < C; ++c) ex[(size_t)l * C + c] = total - sent[c];
-        }
-      }
-    }
-  }
+  HostRing H;
+  const bool ring = entries != 2 && plan_ring(n, rp, cl, dg, upper_levels, entries, ring_ctas(), RING_SMEM_MAX, H);
   Context& ctx = *A.ctx;
   P.nlev = nlev;
   P.nslices = ns;
@@ -726,12 +968,36 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
   up(P.len, len);
   up(P.col, col);
   up(P.src, src);
-  if (P.ring_R) {
-    P.ridx.resize(ridx.size());
-    up(P.ridx, ridx);
-    for (int e = 0; e < 2; ++e) {
-      P.ring_expect[e].resize(expect[e].size());
-      up(P.ring_expect[e], expect[e]);
+  RingPlan& G = P.ring;
+  G.R = 0;
+  if (ring) {
+    G.C = H.C;
+    G.nlev = H.nlev;
+    G.R = H.R;
+    G.slack = H.slack;
+    G.slice_base.resize(H.slice_base.size());
+    G.row.resize(H.row.size());
+    G.len.resize(H.len.size());
+    G.ridx.resize(H.ridx.size());
+    G.src.resize(H.src.size());
+    G.pmask.resize(H.pmask.size());
+    G.expect.resize(H.expect.size());
+    G.nbr.resize(H.nbr.size());
+    G.val.resize(H.src.size());
+    G.valf.resize(H.src.size());
+    up(G.slice_base, H.slice_base);
+    up(G.row, H.row);
+    up(G.len, H.len);
+    up(G.ridx, H.ridx);
+    up(G.src, H.src);
+    up(G.pmask, H.pmask);
+    up(G.expect, H.expect);
+    up(G.nbr, H.nbr);
+    if (with_diag) {
+      G.diag_src.resize(H.diag_src.size());
+      G.diag.resize(H.diag_src.size());
+      G.diagf.resize(H.diag_src.size());
+      up(G.diag_src, H.diag_src);
     }
   }
   if (with_diag) {
@@ -757,6 +1023,22 @@ static void plan_values(Context& ctx, SweepPlan& P, const double* csr_vals, bool
     if (f32)
       RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<float>, blocks_for(ds, 256), 256, 0, ds, P.diag_src.get(),
                  csr_vals, P.diagf.get());
+  }
+  RingPlan& G = P.ring;
+  if (!G.R) return;
+  const int64_t gs = (int64_t)G.src.size();
+  RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<double>, blocks_for(gs, 256), 256, 0, gs, G.src.get(), csr_vals,
+             G.val.get());
+  if (f32)
+    RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<float>, blocks_for(gs, 256), 256, 0, gs, G.src.get(), csr_vals,
+               G.valf.get());
+  if (with_diag) {
+    const int64_t ds = (int64_t)G.diag_src.size();
+    RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<double>, blocks_for(ds, 256), 256, 0, ds, G.diag_src.get(),
+               csr_vals, G.diag.get());
+    if (f32)
+      RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<float>, blocks_for(ds, 256), 256, 0, ds, G.diag_src.get(),
+                 csr_vals, G.diagf.get());
   }
 }
 
@@ -806,15 +1088,11 @@ static bool launch_cluster(Context& ctx, const char* name, Kernel kern, const Ar
   return true;
 }
 
-// Push-ring launch: one cluster with the ring, its mbarriers and the level
-// offsets in dynamic shared memory.  FP64 walks use a cluster of 16 CTAs
-// (4 warps each) when the device schedules one, since their time per level
-// is bound by the SMs' FP64 rate; FP32 walks use 8 CTAs of 8 warps.
-// RSG_SWEEP=pipelined switches the ring off, RSG_RING_CTAS=8|16 forces the
-// cluster size.  Returns false when the ring does not fit or no cluster can
-// be scheduled.
-static std::atomic<int> g_ring_mode{-1};  // -1: not read; 0 off; 1 on
-static int g_ring_ctas = 0;               // forced cluster size, 0: automatic
+// Push-ring launch: one cluster of the plan's CTA count with the ring and its
+// mbarriers in dynamic shared memory.  The plan is built for 16 CTAs of 4
+// warps (RSG_RING_CTAS=8 selects 8 CTAs of 8 warps); RSG_SWEEP=pipelined
+// switches the ring off.  Returns false when the plan has no ring schedule
+// or no such cluster can be scheduled.
 static std::atomic<bool> g_ring_used{false};
 
 template <typename Kernel>
@@ -844,10 +1122,8 @@ static bool ring_schedulable(Kernel kern, int ctas, size_t smem) {
   return e == cudaSuccess && nclusters >= 1;
 }
 
-constexpr size_t RING_SMEM_MAX = 200 * 1024;
-
 template <int KIND, typename T, int CTAS>
-static bool launch_ring_n(Context& ctx, const char* name, const SweepPlan& P, const SweepArgs<T>& a, size_t smem) {
+static bool launch_ring_n(Context& ctx, const char* name, const RingPlan& G, const RingVals<T>& a, size_t smem) {
   auto kern = k_sweep_ring<KIND, T, 16, CTAS>;
   static std::atomic<int> ok{0};  // per instantiation: 0 not probed, 1 schedulable, -1 not
   if (!ok) {
@@ -855,7 +1131,8 @@ static bool launch_ring_n(Context& ctx, const char* name, const SweepPlan& P, co
     if (!ok) ok = ring_schedulable(kern, CTAS, RING_SMEM_MAX) ? 1 : -1;
   }
   if (ok < 0) return false;
-  RingArgs g{P.ring_R, P.ring_slot, P.ridx.get(), P.ring_expect[CTAS == 16].get(), ctx.dev_err.get()};
+  RingArgs g{G.nlev,        G.R,           G.slack,       G.slice_base.get(), G.row.get(), G.len.get(),
+             G.ridx.get(), G.pmask.get(), G.expect.get(), G.nbr.get(),       ctx.dev_err.get()};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CTAS);
   cfg.blockDim = dim3(RING_SLICES / CTAS * 32);
@@ -869,28 +1146,34 @@ static bool launch_ring_n(Context& ctx, const char* name, const SweepPlan& P, co
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   LaunchScope scope(ctx, name);
-  RSG_CUDA(cudaLaunchKernelEx(&cfg, kern, a, g));
+  RSG_CUDA(cudaLaunchKernelEx(&cfg, kern, g, a));
   g_ring_used = true;
   return true;
 }
 
+template <typename T>
+struct RingPick;
+template <>
+struct RingPick<double> {
+  static const double* val(const RingPlan& G) { return G.val.get(); }
+  static const double* diag(const RingPlan& G) { return G.diag.get(); }
+};
+template <>
+struct RingPick<float> {
+  static const float* val(const RingPlan& G) { return G.valf.get(); }
+  static const float* diag(const RingPlan& G) { return G.diagf.get(); }
+};
+
 template <int KIND, typename T>
-static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, const SweepArgs<T>& a) {
-  if (g_ring_mode < 0) {
-    std::lock_guard<std::mutex> lk(g_probe_mu);
-    if (g_ring_mode < 0) {
-      const char* c = getenv("RSG_RING_CTAS");
-      g_ring_ctas = c ? atoi(c) : 0;
-      const char* e = getenv("RSG_SWEEP");
-      g_ring_mode = (e && std::string(e) == "pipelined") ? 0 : 1;
-    }
-  }
-  if (!g_ring_mode || !P.ring_R) return false;
-  const size_t smem = ring_smem_bytes<T>(P.ring_R, P.ring_slot, P.nlev);
+static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, const T* val, const T* diag, const T* b,
+                        T* x, const int* active) {
+  if (!ring_enabled() || !P.ring.R) return false;
+  const size_t smem = ring_smem_bytes<T>(P.ring.R);
   if (smem > RING_SMEM_MAX) return false;
-  const bool want16 = g_ring_ctas ? g_ring_ctas == 16 : sizeof(T) == 8;
-  if (want16 && launch_ring_n<KIND, T, 16>(ctx, name, P, a, smem)) return true;
-  return launch_ring_n<KIND, T, 8>(ctx, name, P, a, smem);
+  const RingVals<T> a{val, diag, b, x, active};
+  if (P.ring.C == 16) return launch_ring_n<KIND, T, 16>(ctx, name, P.ring, a, smem);
+  if (P.ring.C == 8) return launch_ring_n<KIND, T, 8>(ctx, name, P.ring, a, smem);
+  return false;
 }
 
 template <int KIND, typename T>
@@ -898,8 +1181,11 @@ static void run_sweep(Context& ctx, const char* name, const SweepPlan& P, const 
                       T* x, T* xx, T omega, const int* active) {
   SweepArgs<T> a{P.nlev, P.level_slices.get(), P.slice_base.get(), P.row.get(), P.len.get(), P.col.get(), val, diag,
                  b, x, xx, omega, active};
-  if constexpr (KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER)
-    if (launch_ring<KIND, T>(ctx, name, P, a)) return;
+  if constexpr (KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER) {
+    const bool ring = launch_ring<KIND, T>(ctx, name, P, RingPick<T>::val(P.ring),
+                                           KIND == SW_ILU_UPPER ? RingPick<T>::diag(P.ring) : nullptr, b, x, active);
+    if (ring) return;
+  }
   if ((KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER) && P.nlev <= SWEEP_MAX_LEVELS) {
     if (launch_cluster(ctx, name, k_sweep_pipelined<KIND, T, 16>, a, 256)) return;
   } else if (launch_cluster(ctx, name, k_sweep_cluster<KIND, T>, a))
@@ -1093,6 +1379,7 @@ struct SSORPrecond : Precond {
   const int* pattern_id = nullptr;
   SweepPlan Fp, Bp;
   DeviceBuffer<double> xx;
+  DeviceBuffer<float> xxf;
   double omegaF = 1, omegaR = 1;
   bool reverse = true;
   explicit SSORPrecond(Context* c) : ctx(c) {}
@@ -1103,11 +1390,23 @@ struct SSORPrecond : Precond {
       build_plan(M, Fp, false, 2, true);
       build_plan(M, Bp, true, 2, true);
       xx.resize(M.n);
+      xxf.resize(M.n);
       A = &M;
       pattern_id = M.rowptr.get();
     }
-    plan_values(*ctx, Fp, M.val.get(), true, false);
-    plan_values(*ctx, Bp, M.val.get(), true, false);
+    // FP32 copies too: the mixed-precision solver smooths its FP32 AMG levels with them
+    plan_values(*ctx, Fp, M.val.get(), true, true);
+    plan_values(*ctx, Bp, M.val.get(), true, true);
+  }
+  void apply_f32(const float* b, float* x, const int* active) override {
+    run_sweep<SW_SSOR_FWD, float>(*ctx, "ssor_fwd_f32", Fp, Fp.valf.get(), Fp.diagf.get(), b, x, xxf.get(),
+                                  (float)omegaF, active);
+    if (!reverse) {
+      RSG_CUDA(cudaMemcpyAsync(x, xxf.get(), sizeof(float) * A->n, cudaMemcpyDeviceToDevice, ctx->stream));
+      return;
+    }
+    run_sweep<SW_SSOR_BWD, float>(*ctx, "ssor_bwd_f32", Bp, Bp.valf.get(), Bp.diagf.get(), b, x, xxf.get(),
+                                  (float)omegaR, active);
   }
   void apply(const double* b, double* x, const int* active) override {
     // SSOR.java:143-194; x holds the starting iterate
@@ -1193,3 +1492,50 @@ void release_trans_plan(const Precond* p) {
 }  // namespace rsg
 
 extern "C" int32_t rsg_sweep_mode(void) { return rsg::g_ring_used.load() ? 2 : rsg::g_cluster_ok.load(); }
+
+// Builds the ring schedule of one ILU(0) sweep of a pattern on the host and
+// checks it (rsg::check_ring).  Needs no GPU.
+extern "C" rsg_status rsg_sweep_plan_check(int32_t n, const int32_t* row_ptr, const int32_t* col, int32_t sweep,
+                                           int32_t ctas, int64_t* stats, char* msg, int32_t msg_len) {
+  auto say = [&](const std::string& m) {
+    if (msg && msg_len > 0) {
+      std::strncpy(msg, m.c_str(), (size_t)msg_len - 1);
+      msg[msg_len - 1] = 0;
+    }
+  };
+  if (n <= 0 || !row_ptr || !col || (sweep != 0 && sweep != 1) || (ctas != 8 && ctas != 16)) return RSG_BAD_ARG;
+  try {
+    std::vector<int> rp(row_ptr, row_ptr + n + 1);
+    if (rp[0] != 0) return RSG_BAD_ARG;
+    for (int i = 0; i < n; ++i)
+      if (rp[i + 1] < rp[i]) return RSG_BAD_ARG;
+    std::vector<int> cl(col, col + rp[n]), dg(n, -1);
+    for (int i = 0; i < n; ++i)
+      for (int q = rp[i]; q < rp[i + 1]; ++q) {
+        if (cl[q] < 0 || cl[q] >= n || (q > rp[i] && cl[q] <= cl[q - 1])) return RSG_BAD_ARG;
+        if (cl[q] == i) dg[i] = q;
+      }
+    for (int i = 0; i < n; ++i)
+      if (dg[i] < 0) return RSG_MISSING_DIAGONAL;
+    rsg::HostRing H;
+    if (!rsg::plan_ring(n, rp, cl, dg, sweep == 1, sweep, ctas, rsg::RING_SMEM_MAX, H)) {
+      say("no ring schedule");
+      return RSG_UNSUPPORTED;
+    }
+    const std::string err = rsg::check_ring(n, rp, cl, dg, sweep, H);
+    say(err);
+    if (stats) {
+      int64_t pushed = 0, nb = 0;
+      for (int v : H.expect) pushed += v;
+      for (unsigned short m : H.nbr) nb = std::max<int64_t>(nb, __builtin_popcount(m));
+      stats[0] = H.nlev;
+      stats[1] = H.R;
+      stats[2] = pushed;
+      stats[3] = nb;
+    }
+    return err.empty() ? RSG_OK : RSG_OUT_OF_PATTERN;
+  } catch (const std::exception& e) {
+    say(e.what());
+    return RSG_CUDA_ERROR;
+  }
+}

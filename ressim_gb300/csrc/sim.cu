@@ -1562,6 +1562,8 @@ struct Sim {
   };
   std::vector<Snapshot> ck;        // state at the first step of every block
   Snapshot adj_end;                // state after the forward run
+  Snapshot saved;                  // rsg_sim_save_state
+  bool has_saved = false;
   std::vector<double> adj_dt;
   int adj_every = 0;
   bool adj_ready = false;
@@ -2164,6 +2166,27 @@ rsg_status rsg_sim_backward(rsg_sim* s, double rtol, double* dJ_dlogk, double* d
 rsg_status rsg_sim_retract(rsg_sim* s) {
   if (!s) return RSG_BAD_ARG;
   return guarded(s->s->ctx, [&] { s->s->retract(); });
+}
+
+rsg_status rsg_sim_save_state(rsg_sim* s) {
+  if (!s) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    m.snap(m.saved);
+    m.ctx->sync();
+    m.has_saved = true;
+  });
+}
+
+rsg_status rsg_sim_restore_state(rsg_sim* s) {
+  if (!s) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    if (!m.has_saved) throw rsg::Error(RSG_BAD_ARG, "no saved state: call rsg_sim_save_state first");
+    m.unsnap(m.saved);
+    m.ctx->sync();
+    m.check_flag();
+  });
 }
 
 rsg_status rsg_sim_get_state(rsg_sim* s, double* p, double* N, double* S) {

@@ -167,7 +167,10 @@ def corey(swc=0.2, sor=0.2, n=2.0):
 
 
 def runspec(method=abi.BICGSTAB, precond=abi.PC_ILU, rtol=1e-8, atol=1e-50, max_linear=5000,
-            max_newton=10, ptol=1e-6, stop_rule=0, inner_iterations=0, inner_tolerance=0.0):
+            max_newton=10, ptol=1e-6, stop_rule=0, inner_iterations=0, inner_tolerance=0.0, omega=0.0, ax=0.0,
+            ay=0.0):
+    """RunSpec (rs/src/no/uib/cipr/rs/numerics/RunSpec.java) as rsg_runspec;
+    omega, ax, ay: the rotating frame of Field's BodyForces."""
     s = abi.rsg_runspec()
     s.max_nonlinear_pressure_iterations = max_newton
     s.pressure_tolerance = ptol
@@ -182,6 +185,9 @@ def runspec(method=abi.BICGSTAB, precond=abi.PC_ILU, rtol=1e-8, atol=1e-50, max_
     s.gmres_restart = 30
     s.inner_iterations = inner_iterations
     s.inner_tolerance = inner_tolerance
+    s.omega = omega
+    s.ax = ax
+    s.ay = ay
     return s
 
 

@@ -29,8 +29,11 @@ def test_reference_arm_line():
     assert d["metric"] == d["unit"] == "cell-Newton-steps/s"
     assert d["steps"] == 2 and d["warmup"] == 1 and d["higher_is_better"] is True
     assert d["value"] > 0 and d["config"]["cells"] == 256
-    # one Newton iteration per timed step
-    assert d["config"]["newton_iterations"] == 2
+    # the converged Newton loop of the GPU line: at least one iteration per step
+    assert d["newton_iterations"] >= 2 and d["linear_iterations"] > 0
+    assert set(d["config"]) == {"workload", "cells", "pattern_nnz", "dt_s", "seed"}
+    assert "first K steps from the initial state" in d["config"]["workload"]
+    assert "java" in d["jvm"]
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] == 1
     e = d["e2e"]
@@ -54,3 +57,16 @@ def test_sweep_bytes():
     rp = np.array([0, 2, 5, 7], np.int32)  # 3 x 3 tridiagonal
     col = np.array([0, 1, 0, 1, 2, 1, 2], np.int32)
     assert bench.sweep_bytes(rp, col) == (12 * 2 + 16 * 3, 12 * 2 + 24 * 3)
+
+
+def test_both_arms_describe_the_same_workload():
+    """The GPU line and the reference line build their config from one
+    function, so the driver sees the same workload on both."""
+    import argparse
+
+    import bench
+
+    a = argparse.Namespace(ni=128, nj=128, nk=32, rtol=1e-8, seed=1)
+    assert bench.config_of(a, 13716856, 8640.0) == bench.config_of(a, 13716856, 8640.0)
+    src = open(os.path.join(ROOT, "bench.py")).read()
+    assert src.count('"config": config_of(args, len(col)') == 2

@@ -1,5 +1,6 @@
 """Mixed-precision solver (RSG_FGMRES_MIXED): FP64 flexible GMRES around an
-FP32 BiCGstab with the FP32 preconditioner.  It has no counterpart in MTJ, so
+FP32 BiCGstab with the FP32 preconditioner (ILU(0) factors, the AMG
+hierarchy, or the inverted diagonal, stored in FP32).  It has no counterpart in MTJ, so
 its results are checked against an FP64 direct solve (LAPACK through numpy)
 or the FP64 oracle solution of the same system (IterativeSolver.solve,
 sparse/CG.java) at a tighter tolerance: the solution within 1e-8 relative,
@@ -30,6 +31,42 @@ def test_mixed_matches_fp64_solution(ctx, pc, n, band, seed):
     r = O.csr_op(1, rp, col, val, x, b, -1.0)
     assert np.linalg.norm(r) <= 1e-11 * np.linalg.norm(b)
     assert s.last_info.iterations > 0
+
+
+def test_mixed_fp32_amg_matches_fp64_solution(ctx):
+    """FP32 AMG hierarchy (MTJ's smoothed aggregation, built in FP64 and
+    copied to FP32) inside the mixed solver: the solution of the 64 x 64
+    MPFA-O potential system and of a two-phase pressure Jacobian within 1e-8
+    of the FP64 solution, true FP64 residual at the requested tolerance."""
+    case = W.potential_case(rate=2e-15)
+    gm = api.Mesh(ctx, 2, 64, 64, 0, case["perm"])
+    gm.compute_mpfa()
+    rp, col = gm.pattern(1)
+    A = api.CompRowMatrix(ctx, len(rp) - 1, rp, col)
+    gm.assemble_potential(A)
+    A.zero_rows(1.0, case["dirichlet_cells"])
+    val = A.get_values()
+    b = W.potential_rhs(case)
+    systems = [(rp, col, val, b)]
+    c2, gm2, om2, gs2, os2, keep = _two_phase(ctx, 24, 24, 8, spec_kw=dict(ptol=1e300, rtol=1e-2))
+    gs2.enable_jacobian_capture()
+    gs2.step(c2["dt"])
+    rp2, col2 = gm2.pattern(0)
+    jv, jr = gs2.jacobian(len(col2))
+    systems.append((rp2, col2, jv, jr))
+    for rp_, col_, val_, b_ in systems:
+        n = len(rp_) - 1
+        M = api.CompRowMatrix(ctx, n, rp_, col_, val_)
+        s = api.MixedFGMRES(ctx, abi.PC_AMG, rtol=1e-10, max_iter=3000)
+        s.set_matrix(M)
+        assert s.amg_levels() >= 2
+        x = s.solve(M, b_, np.zeros(n))
+        ref = api.GMRES(ctx, abi.PC_AMG, rtol=1e-13, max_iter=20000)
+        ref.set_matrix(M)
+        xr = ref.solve(M, b_, np.zeros(n))
+        assert np.max(np.abs(x - xr)) <= 1e-8 * np.max(np.abs(xr))
+        r = O.csr_op(1, rp_, col_, val_, x, b_, -1.0)
+        assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(b_)
 
 
 def test_mixed_repeat_solve_and_restart(ctx):

@@ -483,3 +483,54 @@ def test_tpfa_two_phase_steps_match_oracle(ctx):
     op, oN, _ = os_.state()
     assert np.max(np.abs(gp - op) / np.abs(op)) <= 1e-10
     assert np.max(np.abs(gN - oN) / np.maximum(np.abs(oN), 1e-300)) <= 1e-10
+
+
+def test_three_phase_converged_steps_match_oracle(ctx):
+    """Water, oil and gas with converged Newton iterations over six steps:
+    the gas cap and the gas injected at the corners put cells in all three
+    hydrocarbon regimes of BlackOilEquationOfState.calculatePhaseState
+    (single-phase oil, single-phase gas, two-phase oil/gas:
+    rs/src/no/uib/cipr/rs/fluid/BlackOilEquationOfState.java:169-547).  Newton
+    counts equal, pressures, saturations and moles within 1e-10 of the
+    oracle, mass balance within 1e-12."""
+    case, gm, gs, os_, keep = _three_phase(ctx, dict(rtol=1e-12))
+    regimes = set()
+    for _ in range(6):
+        gi = gs.step(case["dt"])
+        oi = os_.step(case["dt"])
+        assert gi.newton_iterations == oi.newton_iterations
+        assert gi.mass_balance_error <= 1e-12
+        gp, gN, gS = gs.state()
+        op, oN, oS = os_.state()
+        assert np.max(np.abs(gp - op) / np.abs(op)) <= 1e-10
+        assert np.max(np.abs(gS - oS)) <= 1e-10
+        assert np.max(np.abs(gN - oN) / np.maximum(np.abs(oN), 1e-30)) <= 1e-10
+        so, sg = oS[1], oS[2]
+        regimes |= {"oil"} if np.any((so > 0) & (sg == 0)) else set()
+        regimes |= {"gas"} if np.any((so == 0) & (sg > 0)) else set()
+        regimes |= {"oil+gas"} if np.any((so > 0) & (sg > 0)) else set()
+    assert regimes == {"oil", "gas", "oil+gas"}, regimes
+
+
+def test_rotation_body_force_step_matches_oracle(ctx):
+    """A rotating frame (RunSpec's omega and rotation axis): the Darcy
+    potential carries rho (g z - omega^2 r^2 / 2) (rs/src/no/uib/cipr/rs/field/
+    CS.java:161-170).  Two converged steps with omega = 0.5 rad/s about the
+    vertical axis through (3, 2): within 1e-10 of the oracle, and different
+    from the same steps without rotation."""
+    kw = dict(rtol=1e-12)
+    case, gm, om, gs, os_, keep = _two_phase(ctx, 10, 8, 4, spec_kw=kw)
+    ref = gs
+    case, gm, om, gs, os_, keep = _two_phase(ctx, 10, 8, 4, spec_kw=dict(kw, omega=0.5, ax=3.0, ay=2.0))
+    for _ in range(2):
+        gi = gs.step(case["dt"])
+        oi = os_.step(case["dt"])
+        ref.step(case["dt"])
+        assert gi.newton_iterations == oi.newton_iterations
+        assert gi.mass_balance_error <= 1e-12
+    gp, gN, gS = gs.state()
+    op, oN, oS = os_.state()
+    assert np.max(np.abs(gp - op) / np.abs(op)) <= 1e-10
+    assert np.max(np.abs(gS - oS)) <= 1e-10
+    assert np.max(np.abs(gN - oN) / np.maximum(np.abs(oN), 1e-30)) <= 1e-10
+    assert np.max(np.abs(gp - ref.state()[0]) / np.abs(gp)) > 1e-6

@@ -1,7 +1,8 @@
-"""The JNI shim printed in INTEGRATION.md compiles against include/rsg.h.
-There is no JDK here, so a minimal stand-in declares the few JNI types and
-JNIEnv functions the shim uses (with the JNI specification's signatures);
-the check is that the shim's calls into the C ABI match the header."""
+"""The JNI shim (ressim_gb300/jni/rsg_jni.c) compiles against include/rsg.h,
+and INTEGRATION.md quotes it verbatim.  There is no JDK here, so a minimal
+stand-in declares the few JNI types and JNIEnv functions the shim uses (with
+the JNI specification's signatures); the check is that the shim's calls into
+the C ABI match the header."""
 import os
 import re
 import shutil
@@ -20,7 +21,9 @@ typedef double jdouble;
 typedef void* jobject;
 typedef jobject jclass;
 typedef jobject jarray;
+typedef jint jsize;
 typedef jarray jintArray;
+typedef jarray jlongArray;
 typedef jarray jdoubleArray;
 struct JNINativeInterface_;
 typedef const struct JNINativeInterface_* JNIEnv;
@@ -29,6 +32,8 @@ struct JNINativeInterface_ {
   void (*ReleasePrimitiveArrayCritical)(JNIEnv*, jarray, void*, jint);
   void (*SetIntArrayRegion)(JNIEnv*, jintArray, jint, jint, const jint*);
   void (*SetDoubleArrayRegion)(JNIEnv*, jdoubleArray, jint, jint, const jdouble*);
+  void (*SetLongArrayRegion)(JNIEnv*, jlongArray, jint, jint, const jlong*);
+  jsize (*GetArrayLength)(JNIEnv*, jarray);
 };
 #define JNIEXPORT
 #define JNICALL
@@ -36,14 +41,22 @@ struct JNINativeInterface_ {
 """
 
 
+SHIM = os.path.join(ROOT, "ressim_gb300", "jni", "rsg_jni.c")
+
+
 @pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
 def test_jni_shim_compiles_against_the_header(tmp_path):
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```c\n(.*?)```", text, re.S)
-    assert len(blocks) == 1 and "rsg_solver_solve" in blocks[0]
     (tmp_path / "jni.h").write_text(JNI_STANDIN)
-    (tmp_path / "shim.c").write_text(blocks[0])
     r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-c", "-I", str(tmp_path), "-I",
-                        os.path.join(ROOT, "include"), str(tmp_path / "shim.c"), "-o", str(tmp_path / "shim.o")],
+                        os.path.join(ROOT, "include"), SHIM, "-o", str(tmp_path / "shim.o")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_integration_doc_quotes_the_shim():
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```c\n(.*?)```", text, re.S)
+    assert blocks and "rsg_solver_solve" in blocks[0]
+    src = open(SHIM).read()
+    for b in blocks:
+        assert b.strip() in src
