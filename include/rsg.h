@@ -497,6 +497,26 @@ rsg_status rsg_sim_create_cubic(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_cubic_fl
  * No counterpart in the reference (RS runs one field per process). */
 rsg_status rsg_ensemble_step(int32_t count, rsg_sim* const* sims, const double* dt, int32_t max_concurrent,
                              rsg_step_info* infos, int32_t* statuses);
+/* Ensembles in lockstep: one time step of dt[i] on every member, with the
+ * pressure solves of all members in ONE persistent launch per Newton
+ * iteration.  Each member's Discretisation.solve(dt)
+ * (numerics/Discretisation.java:208-225) runs as in rsg_sim_step: the
+ * members assemble their Jacobians and factor their ILU(0) preconditioners on
+ * their own streams, then one kernel of thread-block clusters takes the
+ * members from a work queue and solves each pressure system completely
+ * (BiCGstab, mtj/.../sparse/BiCGstab.java:65-116, with ILU(0)) through
+ * per-member offsets, and each member updates its pressure and tests its
+ * Newton convergence; converged members leave the loop.  Members must use
+ * RSG_BICGSTAB with RSG_PC_ILU.  precision 0 walks the FP64 factors; 1 walks
+ * their FP32 copies (mixed precision: vectors, SpMV, dots and the stopping
+ * test stay FP64, so the relative residual is met in FP64).  A member whose
+ * step fails stops there (statuses[i], infos[i]); the others go on.  Returns
+ * the first failing member's status.  Results agree with rsg_sim_step per
+ * member to the Krylov solver's rounding (the dot products are summed in a
+ * different order) and do not depend on the number of members or on their
+ * order.  No counterpart in the reference (RS runs one field per process). */
+rsg_status rsg_ensemble_step_batched(int32_t count, rsg_sim* const* sims, const double* dt, int32_t precision,
+                                     rsg_step_info* infos, int32_t* statuses);
 /* Field.getTime: advanced by every rsg_sim_step, restored by rsg_sim_retract. */
 rsg_status rsg_sim_get_time(rsg_sim* s, double* t);
 /* Discretisation.calculateDt(dt) (numerics/Discretisation.java:928-1002): the

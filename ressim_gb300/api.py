@@ -125,6 +125,7 @@ def _declare(L):
         "rsg_sim_forward": (i32, [vp, i32, P(d), i32, i32, P(i32), P(d), P(d), P(d), P(abi.rsg_adjoint_info)]),
         "rsg_sim_backward": (i32, [vp, d, P(d), P(d), P(d), P(abi.rsg_adjoint_info)]),
         "rsg_ensemble_step": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
+        "rsg_ensemble_step_batched": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
         "rsg_cubic_phase_state": (i32, [vp, P(abi.rsg_cubic_fluid), i32, P(d), P(d), P(d), P(d), P(i32)]),
         "rsg_cubic_phase_state_cells": (i32, [vp, P(abi.rsg_cubic_fluid), i32, P(d), P(d), P(d), P(d), P(i32),
                                               P(i32)]),
@@ -660,6 +661,23 @@ def ensemble_step(sims, dts, max_concurrent=0):
     st = lib().rsg_ensemble_step(n, hs, abi.dptr(d), max_concurrent, infos, abi.iptr(sts))
     if st not in (0, 1, 2, 3, 7, 8, 13):
         raise RSGError(st, "ensemble_step")
+    return list(infos), sts
+
+
+def ensemble_step_batched(sims, dts, precision=0):
+    """One time step of every Discretisation of `sims` in lockstep, with the
+    pressure solves of all members in one persistent launch per Newton
+    iteration (rsg_ensemble_step_batched).  precision 0: FP64 ILU(0) walks;
+    1: the factors' FP32 copies inside the FP64 BiCGstab.  Returns
+    (per-member rsg_step_info list, statuses)."""
+    n = len(sims)
+    hs = (C.c_void_p * n)(*[s.h for s in sims])
+    d = np.ascontiguousarray(np.broadcast_to(np.asarray(dts, np.float64), (n,)))
+    infos = (abi.rsg_step_info * n)()
+    sts = np.zeros(n, np.int32)
+    st = lib().rsg_ensemble_step_batched(n, hs, abi.dptr(d), int(precision), infos, abi.iptr(sts))
+    if st != 0 and not (sts == st).any():  # a failure of the call itself, not of one member's step
+        raise RSGError(st, "ensemble_step_batched")
     return list(infos), sts
 
 

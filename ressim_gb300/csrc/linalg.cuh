@@ -10,6 +10,24 @@ namespace rsg {
 
 constexpr int SELL_C = 32;
 
+// One row of the SELL-32 copy (entry k of the row in lane l of slice s at
+// slice_base[s] + 32 k + l) times x, each product fused into the running
+// sum, in CSR order.  NC: x gathers through the read-only cache, for an x
+// that no thread writes during the kernel; otherwise from L2 (an x written
+// earlier in the same launch by other SMs, as in a persistent solver).
+template <bool NC>
+__device__ __forceinline__ double sell_row_fma(const double* __restrict__ val, const int* __restrict__ col,
+                                               const double* x, int base, int len) {
+  double d = 0;
+#pragma unroll 8
+  for (int k = 0; k < len; ++k) {
+    const int q = base + 32 * k;
+    const double xv = NC ? __ldg(x + col[q]) : __ldcg(x + col[q]);
+    d = __fma_rn(val[q], xv, d);
+  }
+  return d;
+}
+
 // Ring schedule of an ILU(0) sweep for one cluster of C CTAs (precond.cu,
 // k_sweep_ring): CTAs own contiguous row blocks, every level has
 // RING_SLICES slices (W = RING_SLICES / C per CTA), each value is pushed only
@@ -108,6 +126,31 @@ SolverPtr make_solver(Context* ctx, int method, int precond, double rtol, double
 void solver_setup(Solver& s, Csr& A);
 void solver_solve(Solver& s, Csr& A, const double* b, double* x, rsg_solve_info* info);
 void solver_set_inner(Solver& s, int iterations, double rtol);
+// what a solver was created with, and its preconditioner
+struct SolverView {
+  int method, pc_kind;
+  Precond* pc;
+  double rtol, atol, dtol;
+  int maxIter;
+};
+SolverView solver_view(Solver& s);
+// One pressure system of an ensemble member: A x = b with the member's
+// solver (BiCGstab + ILU(0), set up on A), on the member's context.
+struct EnsSystem {
+  Context* ctx;
+  Csr* A;
+  Solver* solver;
+  const double* b;
+  double* x;
+};
+// Solves every system in one persistent launch (ensemble.cu).  precision 0:
+// FP64 ILU(0) walks, 1: the factors' FP32 copies inside the FP64 BiCGstab.
+// status[i]: RSG_OK or the member's failure (MTJ's reasons, RSG_TIMEOUT).
+void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vector<rsg_solve_info>& info,
+                    std::vector<int>& status);
+// the ring schedules and factor values of an ILU(0) preconditioner after its
+// setup (false for other preconditioners or patterns without ring schedules)
+bool ilu_ring_plans(Precond* p, const RingPlan** lower, const RingPlan** upper);
 // the solver no longer refers to the matrix of its last setup (rsg_solver_setup is needed again)
 void solver_forget_matrix(Solver& s);
 

@@ -1361,50 +1361,68 @@ struct Sim {
     copy(N, N_prev, (int64_t)nc * n);
   }
 
-  void step(double dt, rsg_step_info* info) {
+  // Discretisation.solve(dt) in phases, so that ensembles can run the
+  // pressure solves of many members in one launch: step_begin, then per
+  // Newton iteration newton_assemble, a pressure solve of (A, b) into dp,
+  // newton_finish (true once converged), and step_end.
+  int nt_its = 0, nt_lin = 0;
+  double nt_dpMax = 0, nt_dp0 = 0;
+
+  void step_begin(double dt) {
     if (!(dt > 0)) throw Error(RSG_BAD_ARG, "time step must be positive");
     store_state();
     time += dt;  // field.changeTime(dt)
     last_dt = dt;
-    int its = 0, lin = 0;
-    double dpMax = 0, dp0h = 0;
+    nt_its = nt_lin = 0;
+    nt_dpMax = nt_dp0 = 0;
+  }
+
+  // assemblePressureJacobian + LinearSolver's zeroRows/sign, dp = 0, and
+  // the preconditioner's setMatrix
+  void newton_assemble(double dt) {
+    SimDev d = dev();
+    RSG_LAUNCH(*ctx, "flux_conn", k_flux_conn, blocks_for(nconn, 128), 128, 0, d, cdev(), Jh.get(), Jt.get(),
+               rh.get(), rt.get());
+    RSG_LAUNCH(*ctx, "assemble_rows", k_assemble_rows, blocks_for(n, 128), 128, 0, d, adev(), Jh.get(), Jt.get(),
+               rh.get(), rt.get(), dt, A.m.val.get(), b.get(), keep_jacobian ? rawJ.get() : nullptr,
+               keep_jacobian ? rawB.get() : nullptr);
+    A.m.sell_dirty = true;
+    RSG_LAUNCH(*ctx, "zero", k_zero, blocks_for(n, 256), 256, 0, (int64_t)n, dp.get());
+    solver_setup(*solver, A.m);
+  }
+
+  // updatePressure, calculateSecondaries and the stop test; true once the
+  // Newton loop has converged
+  bool newton_finish(const rsg_solve_info& si) {
+    nt_lin += si.iterations;
+    SimDev d = dev();
+    RSG_CUDA(cudaMemsetAsync(dpmax_bits.get(), 0, sizeof(unsigned long long), ctx->stream));
+    int big = INT32_MAX;
+    RSG_CUDA(cudaMemcpyAsync(bad_row.get(), &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    RSG_LAUNCH(*ctx, "update_pressure", k_update_pressure, blocks_for(n, 256), 256, 0, d, dp.get(), locked.get(),
+               p_prev.get(), dpmax_bits.get(), bad_row.get(), dp0.get());
+    secondaries();
+    unsigned long long bits = 0;
+    int bad = 0;
+    RSG_CUDA(cudaMemcpyAsync(&bits, dpmax_bits.get(), sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(&nt_dp0, dp0.get(), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(&bad, bad_row.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    std::memcpy(&nt_dpMax, &bits, sizeof(double));
+    if (bad != INT32_MAX)
+      throw Error(RSG_NONPOSITIVE_PRESSURE, "Non-positive pressure in element " + std::to_string(bad));
+    check_flag();
+    ++nt_its;
     const bool ref_rule = spec.newton_stop_rule == 0;
-    for (;;) {
-      SimDev d = dev();
-      RSG_LAUNCH(*ctx, "flux_conn", k_flux_conn, blocks_for(nconn, 128), 128, 0, d, cdev(), Jh.get(), Jt.get(),
-                 rh.get(), rt.get());
-      RSG_LAUNCH(*ctx, "assemble_rows", k_assemble_rows, blocks_for(n, 128), 128, 0, d, adev(), Jh.get(), Jt.get(),
-                 rh.get(), rt.get(), dt, A.m.val.get(), b.get(), keep_jacobian ? rawJ.get() : nullptr,
-                 keep_jacobian ? rawB.get() : nullptr);
-      A.m.sell_dirty = true;
-      RSG_LAUNCH(*ctx, "zero", k_zero, blocks_for(n, 256), 256, 0, (int64_t)n, dp.get());
-      rsg_solve_info si{};
-      solver_setup(*solver, A.m);
-      solver_solve(*solver, A.m, b.get(), dp.get(), &si);
-      lin += si.iterations;
-      RSG_CUDA(cudaMemsetAsync(dpmax_bits.get(), 0, sizeof(unsigned long long), ctx->stream));
-      int big = INT32_MAX;
-      RSG_CUDA(cudaMemcpyAsync(bad_row.get(), &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-      RSG_LAUNCH(*ctx, "update_pressure", k_update_pressure, blocks_for(n, 256), 256, 0, d, dp.get(), locked.get(),
-                 p_prev.get(), dpmax_bits.get(), bad_row.get(), dp0.get());
-      secondaries();
-      unsigned long long bits = 0;
-      int bad = 0;
-      RSG_CUDA(cudaMemcpyAsync(&bits, dpmax_bits.get(), sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
-      RSG_CUDA(cudaMemcpyAsync(&dp0h, dp0.get(), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-      RSG_CUDA(cudaMemcpyAsync(&bad, bad_row.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-      ctx->sync();
-      std::memcpy(&dpMax, &bits, sizeof(double));
-      if (bad != INT32_MAX)
-        throw Error(RSG_NONPOSITIVE_PRESSURE, "Non-positive pressure in element " + std::to_string(bad));
-      check_flag();
-      ++its;
-      bool conv = ref_rule ? (dp0h < spec.pressure_tolerance) : (dpMax < spec.pressure_tolerance);
-      if (conv) break;
-      if (its >= spec.max_nonlinear_pressure_iterations)
-        throw Error(RSG_NEWTON_NOT_CONVERGED, "Nonlinear pressure solver failed to converge");
-    }
-    // MolarMassExplicit.solve
+    const bool conv = ref_rule ? (nt_dp0 < spec.pressure_tolerance) : (nt_dpMax < spec.pressure_tolerance);
+    if (conv) return true;
+    if (nt_its >= spec.max_nonlinear_pressure_iterations)
+      throw Error(RSG_NEWTON_NOT_CONVERGED, "Nonlinear pressure solver failed to converge");
+    return false;
+  }
+
+  // MolarMassExplicit.solve and the final calculateSecondaries
+  void step_end(double dt, rsg_step_info* info) {
     SimDev d = dev();
     RSG_LAUNCH(*ctx, "molar_conn", k_molar_conn, blocks_for(nconn, 128), 128, 0, d, cdev(), cf.get());
     int big = INT32_MAX;
@@ -1416,16 +1434,27 @@ struct Sim {
     ctx->sync();
     if (bad != INT32_MAX) throw Error(RSG_NEGATIVE_MOLES, "Negative number of moles in element " + std::to_string(bad));
     secondaries();
-    last_newton = its;
+    last_newton = nt_its;
     if (info) {
-      info->newton_iterations = its;
-      info->linear_iterations = lin;
-      info->dp_max = dpMax;
-      info->dp0 = dp0h;
+      info->newton_iterations = nt_its;
+      info->linear_iterations = nt_lin;
+      info->dp_max = nt_dpMax;
+      info->dp0 = nt_dp0;
       info->status = RSG_OK;
       info->mass_balance_error = mass_balance(dt);
     }
     check_flag();
+  }
+
+  void step(double dt, rsg_step_info* info) {
+    step_begin(dt);
+    for (;;) {
+      newton_assemble(dt);
+      rsg_solve_info si{};
+      solver_solve(*solver, A.m, b.get(), dp.get(), &si);
+      if (newton_finish(si)) break;
+    }
+    step_end(dt, info);
   }
 
   double mass_balance(double dt) {
@@ -2107,6 +2136,88 @@ rsg_status rsg_ensemble_step(int32_t count, rsg_sim* const* sims, const double* 
   for (int w = 1; w < workers && w < count; ++w) pool.emplace_back(work);
   work();
   for (auto& t : pool) t.join();
+  for (int i = 0; i < count; ++i)
+    if (st[i] != RSG_OK) return st[i];
+  return RSG_OK;
+}
+
+rsg_status rsg_ensemble_step_batched(int32_t count, rsg_sim* const* sims, const double* dt, int32_t precision,
+                                     rsg_step_info* infos, int32_t* statuses) {
+  if (count < 0 || (count > 0 && (!sims || !dt)) || (precision != 0 && precision != 1)) return RSG_BAD_ARG;
+  std::set<rsg::Sim*> seen;
+  for (int i = 0; i < count; ++i) {
+    if (!sims[i]) return RSG_BAD_ARG;
+    if (!seen.insert(sims[i]->s.get()).second) return RSG_BAD_ARG;  // a member listed twice
+  }
+  std::vector<rsg_status> st(count, RSG_OK);
+  std::vector<char> live(count, 1), done(count, 0);
+  std::vector<rsg_step_info> inf(count);
+  for (int i = 0; i < count; ++i) {
+    rsg::Sim& m = *sims[i]->s;
+    st[i] = guarded(m.ctx, [&] {
+      RSG_CUDA(cudaSetDevice(m.ctx->device));
+      m.step_begin(dt[i]);
+    });
+    if (st[i] != RSG_OK) live[i] = 0;
+  }
+  for (;;) {
+    std::vector<int> act;
+    for (int i = 0; i < count; ++i)
+      if (live[i] && !done[i]) act.push_back(i);
+    if (act.empty()) break;
+    std::vector<int> go;
+    for (int i : act) {
+      rsg::Sim& m = *sims[i]->s;
+      st[i] = guarded(m.ctx, [&] {
+        RSG_CUDA(cudaSetDevice(m.ctx->device));
+        m.newton_assemble(dt[i]);
+      });
+      if (st[i] != RSG_OK) live[i] = 0;
+      else go.push_back(i);
+    }
+    if (go.empty()) continue;
+    std::vector<rsg::EnsSystem> sys;
+    for (int i : go) {
+      rsg::Sim& m = *sims[i]->s;
+      sys.push_back(rsg::EnsSystem{m.ctx, &m.A.m, m.solver.get(), m.b.get(), m.dp.get()});
+    }
+    std::vector<rsg_solve_info> si;
+    std::vector<int> ss;
+    rsg_status e = guarded(sims[go[0]]->s->ctx, [&] { rsg::ensemble_solve(sys, precision, si, ss); });
+    for (size_t k = 0; k < go.size(); ++k) {
+      const int i = go[k];
+      rsg::Sim& m = *sims[i]->s;
+      if (e != RSG_OK) {
+        st[i] = e;
+        live[i] = 0;
+        continue;
+      }
+      if (ss[k] != RSG_OK) {  // LinearSolver.solve maps the solver's failure to a SolverFailure
+        st[i] = (rsg_status)ss[k];
+        live[i] = 0;
+        continue;
+      }
+      bool conv = false;
+      st[i] = guarded(m.ctx, [&] {
+        RSG_CUDA(cudaSetDevice(m.ctx->device));
+        conv = m.newton_finish(si[k]);
+      });
+      if (st[i] != RSG_OK) live[i] = 0;
+      else if (conv) done[i] = 1;
+    }
+  }
+  for (int i = 0; i < count; ++i) {
+    if (done[i]) {
+      rsg::Sim& m = *sims[i]->s;
+      st[i] = guarded(m.ctx, [&] {
+        RSG_CUDA(cudaSetDevice(m.ctx->device));
+        m.step_end(dt[i], &inf[i]);
+      });
+    }
+    inf[i].status = st[i];
+    if (infos) infos[i] = inf[i];
+    if (statuses) statuses[i] = st[i];
+  }
   for (int i = 0; i < count; ++i)
     if (st[i] != RSG_OK) return st[i];
   return RSG_OK;
