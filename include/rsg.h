@@ -517,6 +517,41 @@ rsg_status rsg_ensemble_step(int32_t count, rsg_sim* const* sims, const double* 
  * order.  No counterpart in the reference (RS runs one field per process). */
 rsg_status rsg_ensemble_step_batched(int32_t count, rsg_sim* const* sims, const double* dt, int32_t precision,
                                      rsg_step_info* infos, int32_t* statuses);
+/* IterativeSolver.solve (mtj/.../sparse/IterativeSolver.java:43-74) on many
+ * independent systems in ONE persistent launch: solvers[i] (RSG_BICGSTAB with
+ * RSG_PC_ILU, set up with A[i] by rsg_solver_setup) solves A[i] x[i] = b[i]
+ * from the initial guess x[i], host arrays as in rsg_solver_solve.  The
+ * launch is the ensemble solver of rsg_ensemble_step_batched (precision as
+ * there); statuses[i] and infos[i] report each system (MTJ's reasons;
+ * RSG_UNSUPPORTED for another method or preconditioner; RSG_BAD_ARG for a
+ * solver not set up with its matrix), x[i] is copied back either way, and
+ * the first failing status is returned.  No counterpart in the reference. */
+rsg_status rsg_solver_solve_batched(int32_t count, rsg_solver* const* solvers, rsg_csr* const* A,
+                                    const double* const* b, double* const* x, int32_t precision,
+                                    rsg_solve_info* infos, int32_t* statuses);
+/* Matrix Market exchange files (mtj/src/no/uib/cipr/matrix/io/
+ * MatrixVectorReader.java, MatrixVectorWriter.java).  Host code: paths are
+ * files of the calling process.
+ * rsg_mm_read_matrix_size + rsg_mm_read_csr: CompRowMatrix(MatrixVectorReader)
+ * (sparse/CompRowMatrix.java:68-146): coordinate real/integer files, general,
+ * symmetric (mirrored) or skew-symmetric (negated mirror), optional header,
+ * '%' comments; rows sorted, a repeated entry keeps its last value; *nnz is
+ * the number of stored entries after the mirroring.  Pattern, complex and
+ * array matrices: RSG_UNSUPPORTED; unreadable or ill-formed files and indices
+ * out of range: RSG_BAD_ARG.
+ * rsg_mm_write_csr: MatrixVectorWriter's "%%MatrixMarket matrix coordinate
+ * real general", "%10d %10d %19d" and "%10d %10d % .12e" lines, 1-based, in
+ * CSR order.
+ * rsg_mm_read_vector_size + rsg_mm_read_vector: DenseVector(MatrixVectorReader)
+ * (DenseVector.java:52-96), array or coordinate.  rsg_mm_write_vector:
+ * "%%MatrixMarket vector array real", "%10d", "% .12e" per entry. */
+rsg_status rsg_mm_read_matrix_size(const char* path, int32_t* rows, int32_t* cols, int64_t* nnz);
+rsg_status rsg_mm_read_csr(const char* path, int32_t rows, int64_t nnz, int32_t* row_ptr, int32_t* col, double* val);
+rsg_status rsg_mm_write_csr(const char* path, int32_t rows, int32_t cols, const int32_t* row_ptr, const int32_t* col,
+                            const double* val);
+rsg_status rsg_mm_read_vector_size(const char* path, int32_t* size);
+rsg_status rsg_mm_read_vector(const char* path, int32_t size, double* x);
+rsg_status rsg_mm_write_vector(const char* path, int32_t size, const double* x);
 /* Field.getTime: advanced by every rsg_sim_step, restored by rsg_sim_retract. */
 rsg_status rsg_sim_get_time(rsg_sim* s, double* t);
 /* Discretisation.calculateDt(dt) (numerics/Discretisation.java:928-1002): the

@@ -126,6 +126,13 @@ def _declare(L):
         "rsg_sim_backward": (i32, [vp, d, P(d), P(d), P(d), P(abi.rsg_adjoint_info)]),
         "rsg_ensemble_step": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
         "rsg_ensemble_step_batched": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
+        "rsg_solver_solve_batched": (i32, [i32, P(vp), P(vp), P(vp), P(vp), i32, P(abi.rsg_solve_info), P(i32)]),
+        "rsg_mm_read_matrix_size": (i32, [C.c_char_p, P(i32), P(i32), P(C.c_int64)]),
+        "rsg_mm_read_csr": (i32, [C.c_char_p, i32, C.c_int64, P(i32), P(i32), P(d)]),
+        "rsg_mm_write_csr": (i32, [C.c_char_p, i32, i32, P(i32), P(i32), P(d)]),
+        "rsg_mm_read_vector_size": (i32, [C.c_char_p, P(i32)]),
+        "rsg_mm_read_vector": (i32, [C.c_char_p, i32, P(d)]),
+        "rsg_mm_write_vector": (i32, [C.c_char_p, i32, P(d)]),
         "rsg_cubic_phase_state": (i32, [vp, P(abi.rsg_cubic_fluid), i32, P(d), P(d), P(d), P(d), P(i32)]),
         "rsg_cubic_phase_state_cells": (i32, [vp, P(abi.rsg_cubic_fluid), i32, P(d), P(d), P(d), P(d), P(i32),
                                               P(i32)]),
@@ -662,6 +669,70 @@ def ensemble_step(sims, dts, max_concurrent=0):
     if st not in (0, 1, 2, 3, 7, 8, 13):
         raise RSGError(st, "ensemble_step")
     return list(infos), sts
+
+
+def solve_batched(solvers, matrices, bs, x0s, precision=0):
+    """IterativeSolver.solve for many systems in one persistent launch
+    (rsg_solver_solve_batched): each solver (BiCGstab + ILU(0)) must have
+    been set up with its matrix.  Returns (solutions, infos, statuses)."""
+    n = len(solvers)
+    xs = [np.array(x, dtype=np.float64, copy=True) for x in x0s]
+    bs = [np.ascontiguousarray(b, dtype=np.float64) for b in bs]
+    hs = (C.c_void_p * n)(*[s.h for s in solvers])
+    hm = (C.c_void_p * n)(*[m.h for m in matrices])
+    hb = (C.c_void_p * n)(*[b.ctypes.data for b in bs])
+    hx = (C.c_void_p * n)(*[x.ctypes.data for x in xs])
+    infos = (abi.rsg_solve_info * n)()
+    sts = np.zeros(n, np.int32)
+    st = lib().rsg_solver_solve_batched(n, hs, hm, hb, hx, int(precision), infos, abi.iptr(sts))
+    if st != 0 and not (sts == st).any():
+        raise RSGError(st, "solve_batched")
+    return xs, list(infos), sts
+
+
+def read_matrix_market(path):
+    """CompRowMatrix(MatrixVectorReader): (rows, cols, row_ptr, col, val) of a
+    Matrix Market coordinate file."""
+    rows, cols, nnz = C.c_int32(), C.c_int32(), C.c_int64()
+    st = lib().rsg_mm_read_matrix_size(os.fsencode(path), C.byref(rows), C.byref(cols), C.byref(nnz))
+    if st != 0:
+        raise RSGError(st, f"read_matrix_market({path})")
+    rp = np.zeros(rows.value + 1, np.int32)
+    col = np.zeros(max(nnz.value, 1), np.int32)
+    val = np.zeros(max(nnz.value, 1))
+    st = lib().rsg_mm_read_csr(os.fsencode(path), rows.value, nnz.value, abi.iptr(rp), abi.iptr(col), abi.dptr(val))
+    if st != 0:
+        raise RSGError(st, f"read_matrix_market({path})")
+    return rows.value, cols.value, rp, col[:nnz.value], val[:nnz.value]
+
+
+def write_matrix_market(path, rows, cols, rowptr, col, val):
+    """MatrixVectorWriter output of a CSR matrix (coordinate real general)."""
+    rp, cl, v = _i32(rowptr), _i32(col), np.ascontiguousarray(val, np.float64)
+    st = lib().rsg_mm_write_csr(os.fsencode(path), int(rows), int(cols), abi.iptr(rp), abi.iptr(cl), abi.dptr(v))
+    if st != 0:
+        raise RSGError(st, f"write_matrix_market({path})")
+
+
+def read_matrix_market_vector(path):
+    """DenseVector(MatrixVectorReader)."""
+    n = C.c_int32()
+    st = lib().rsg_mm_read_vector_size(os.fsencode(path), C.byref(n))
+    if st != 0:
+        raise RSGError(st, f"read_matrix_market_vector({path})")
+    x = np.zeros(max(n.value, 1))
+    st = lib().rsg_mm_read_vector(os.fsencode(path), n.value, abi.dptr(x))
+    if st != 0:
+        raise RSGError(st, f"read_matrix_market_vector({path})")
+    return x[:n.value]
+
+
+def write_matrix_market_vector(path, x):
+    """MatrixVectorWriter output of a dense vector (array real)."""
+    v = np.ascontiguousarray(x, np.float64)
+    st = lib().rsg_mm_write_vector(os.fsencode(path), len(v), abi.dptr(v))
+    if st != 0:
+        raise RSGError(st, f"write_matrix_market_vector({path})")
 
 
 def ensemble_step_batched(sims, dts, precision=0):

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIB_DIR, "libresgpu.so")
 SOURCES = ["context.cu", "csr.cu", "precond.cu", "amg.cu", "krylov.cu", "mesh.cu", "sim.cu", "noalloc.cu", "adjoint.cu",
-           "ensemble.cu"]
+           "ensemble.cu", "mmio.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]

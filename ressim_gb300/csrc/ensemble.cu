@@ -110,9 +110,11 @@ __device__ __forceinline__ void cluster_sum(double (&v)[K], double* part, double
 
 // A walk as a called function: its registers are allocated apart from the
 // solver loop's, which keeps both free of spills.
+// (13 entries of a row in registers, as for the 27-point stencil; longer
+// rows read the rest from memory)
 template <int KIND, typename T, int CTAS>
 __device__ __noinline__ bool walk(const RingArgs& g, const RingVals<T>& a, unsigned char* smem) {
-  return ring_walk<KIND, T, 16, CTAS>(g, a, smem);
+  return ring_walk<KIND, T, 13, CTAS>(g, a, smem);
 }
 
 // out = M^-1 in (ILU(0): L y = in, U out = y) on the cluster; ends with a
@@ -396,6 +398,10 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
       status[i] = RSG_BAD_ARG;  // members must share one device
       continue;
     }
+    if (sv.setup_for != q.A) {
+      status[i] = RSG_BAD_ARG;  // the solver must have been set up with this matrix
+      continue;
+    }
     if (sv.method != RSG_BICGSTAB || sv.pc_kind != RSG_PC_ILU || !ilu_ring_plans(sv.pc, &L, &U) ||
         (C != 0 && (L->C != C || U->C != C)) || (L->C != 8 && L->C != 16) || U->C != L->C) {
       status[i] = RSG_UNSUPPORTED;  // BiCGstab + ILU(0) with level-walk schedules for one cluster shape
@@ -488,3 +494,57 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
 }
 
 }  // namespace rsg
+
+using rsg::guarded;
+
+extern "C" {
+
+rsg_status rsg_solver_solve_batched(int32_t count, rsg_solver* const* solvers, rsg_csr* const* A,
+                                    const double* const* b, double* const* x, int32_t precision,
+                                    rsg_solve_info* infos, int32_t* statuses) {
+  if (count < 0 || (count > 0 && (!solvers || !A || !b || !x))) return RSG_BAD_ARG;
+  if (precision != 0 && precision != 1) return RSG_BAD_ARG;
+  for (int i = 0; i < count; ++i)
+    if (!solvers[i] || !A[i] || !b[i] || !x[i]) return RSG_BAD_ARG;
+  if (count == 0) return RSG_OK;
+  std::vector<rsg::DeviceBuffer<double>> db(count), dx(count);
+  std::vector<rsg::EnsSystem> sys(count);
+  rsg::Context* ctx0 = nullptr;
+  std::vector<rsg_status> st(count, RSG_OK);
+  for (int i = 0; i < count; ++i) {
+    rsg::Context* ctx = rsg::solver_view(*solvers[i]->s).ctx;
+    if (!ctx0) ctx0 = ctx;
+    const int n = A[i]->m.n;
+    st[i] = guarded(ctx, [&] {
+      db[i].resize(n);
+      dx[i].resize(n);
+      RSG_CUDA(cudaMemcpyAsync(db[i].get(), b[i], sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+      RSG_CUDA(cudaMemcpyAsync(dx[i].get(), x[i], sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    });
+    sys[i] = rsg::EnsSystem{ctx, &A[i]->m, solvers[i]->s.get(), db[i].get(), dx[i].get()};
+  }
+  std::vector<rsg_solve_info> si;
+  std::vector<int> ss;
+  rsg_status e = guarded(ctx0, [&] { rsg::ensemble_solve(sys, precision, si, ss); });
+  rsg_status first = RSG_OK;
+  for (int i = 0; i < count; ++i) {
+    rsg::Context* ctx = sys[i].ctx;
+    rsg_status r = st[i] != RSG_OK ? st[i] : (e != RSG_OK ? e : (rsg_status)ss[i]);
+    // as rsg_solver_solve: x as it stood at the end, copied back either way
+    rsg_status c = guarded(ctx, [&] {
+      RSG_CUDA(cudaMemcpyAsync(x[i], dx[i].get(), sizeof(double) * A[i]->m.n, cudaMemcpyDeviceToHost, ctx->stream));
+      ctx->sync();
+    });
+    if (r == RSG_OK) r = c;
+    if (infos) {
+      infos[i] = e == RSG_OK ? si[i] : rsg_solve_info{};
+      infos[i].reason = r;
+    }
+    if (statuses) statuses[i] = r;
+    if (first == RSG_OK) first = r;
+  }
+  return first;
+}
+
+}  // extern "C"
+

@@ -34,6 +34,7 @@ __device__ __forceinline__ double sell_row_fma(const double* __restrict__ val, c
 // to the CTAs that read it.  R == 0: no ring schedule for this pattern.
 struct RingPlan {
   int C = 0, nlev = 0, R = 0, slack = 0;
+  int maxlen = 0;  // longest row (entries in the sweep's triangle)
   DeviceBuffer<int> slice_base, row, len, ridx, src, diag_src, expect;
   DeviceBuffer<unsigned short> pmask, nbr;
   DeviceBuffer<double> val, diag;
@@ -132,6 +133,8 @@ struct SolverView {
   Precond* pc;
   double rtol, atol, dtol;
   int maxIter;
+  const Csr* setup_for;  // the matrix of the last setup (nullptr: none)
+  Context* ctx;
 };
 SolverView solver_view(Solver& s);
 // One pressure system of an ensemble member: A x = b with the member's

@@ -367,7 +367,7 @@ __global__ void k_diag_apply(int n, const T* __restrict__ inv, const T* __restri
 // contiguous blocks (owner = row * C / n); each dependency level is split
 // into plan levels of at most W * 32 rows per CTA.
 struct HostRing {
-  int C = 0, nlev = 0, R = 0, slack = 0;
+  int C = 0, nlev = 0, R = 0, slack = 0, maxlen = 0;
   std::vector<int> slice_base, row, len, ridx, src, diag_src, expect;
   std::vector<unsigned short> pmask, nbr;
 };
@@ -457,6 +457,7 @@ static bool plan_ring(int n, const std::vector<int>& rp, const std::vector<int>&
     const size_t slot = (size_t)plev[i] * RING_SLOT + ppos[i];
     H.row[slot] = i;
     H.len[slot] = q1 - q0;
+    H.maxlen = std::max(H.maxlen, q1 - q0);
     H.diag_src[slot] = dg[i];
     width[slot / 32] = std::max(width[slot / 32], q1 - q0);
   }
@@ -697,6 +698,7 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
     G.nlev = H.nlev;
     G.R = H.R;
     G.slack = H.slack;
+    G.maxlen = H.maxlen;
     G.slice_base.resize(H.slice_base.size());
     G.row.resize(H.row.size());
     G.len.resize(H.len.size());
@@ -844,9 +846,13 @@ static bool ring_schedulable(Kernel kern, int ctas, size_t smem) {
   return e == cudaSuccess && nclusters >= 1;
 }
 
-template <int KIND, typename T, int CTAS>
+// MAXW: the entries of a row held in registers.  Every unrolled step costs
+// issue slots whether its lanes are active or not, so the kernel is built
+// for 13 entries (the 27-point stencil's triangles) and for 16; longer rows
+// read their remaining entries from memory.
+template <int KIND, typename T, int CTAS, int MAXW>
 static bool launch_ring_n(Context& ctx, const char* name, const RingPlan& G, const RingVals<T>& a, size_t smem) {
-  auto kern = k_sweep_ring<KIND, T, 16, CTAS>;
+  auto kern = k_sweep_ring<KIND, T, MAXW, CTAS>;
   static std::atomic<int> ok{0};  // per instantiation: 0 not probed, 1 schedulable, -1 not
   if (!ok) {
     std::lock_guard<std::mutex> lk(g_probe_mu);
@@ -893,8 +899,13 @@ static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, cons
   const size_t smem = ring_smem_bytes<T>(P.ring.R);
   if (smem > RING_SMEM_MAX) return false;
   const RingVals<T> a{val, diag, b, x, active};
-  if (P.ring.C == 16) return launch_ring_n<KIND, T, 16>(ctx, name, P.ring, a, smem);
-  if (P.ring.C == 8) return launch_ring_n<KIND, T, 8>(ctx, name, P.ring, a, smem);
+  const bool narrow = P.ring.maxlen <= 13;
+  if (P.ring.C == 16)
+    return narrow ? launch_ring_n<KIND, T, 16, 13>(ctx, name, P.ring, a, smem)
+                  : launch_ring_n<KIND, T, 16, 16>(ctx, name, P.ring, a, smem);
+  if (P.ring.C == 8)
+    return narrow ? launch_ring_n<KIND, T, 8, 13>(ctx, name, P.ring, a, smem)
+                  : launch_ring_n<KIND, T, 8, 16>(ctx, name, P.ring, a, smem);
   return false;
 }
 

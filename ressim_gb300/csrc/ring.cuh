@@ -230,7 +230,10 @@ __device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& 
     const int exp_nxt = (threadIdx.x == 0 && l + 1 < g.nlev) ? g.expect[(l + 1) * RING_CTAS + rank] : 0;
     const RingMeta m2 = ring_meta(g, l + 2, gwarp, lane);
     ring_coeffs<KIND, T, MAXW>(g, a, m1, nxt);
-    const int late = (l > 0) ? !mbar_wait(bar0 + 8 * slot_p, par_p) : 0;
+    // one thread waits for the level's values and tokens; the barrier below
+    // releases the others (fewer instructions in flight than every thread
+    // polling the mbarrier)
+    const int late = (l > 0 && threadIdx.x == 0) ? !mbar_wait(bar0 + 8 * slot_p, par_p) : 0;
     if (__syncthreads_or(late)) {
       if (threadIdx.x == 0) atomicCAS(g.err, 0, 1 + l);
       ok = false;

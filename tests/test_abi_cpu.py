@@ -142,7 +142,7 @@ def test_null_arguments_are_rejected(lib):
                 args.append(0.0)
             else:
                 args.append(None)
-        if name in ("rsg_ensemble_step", "rsg_ensemble_step_batched"):
+        if name in ("rsg_ensemble_step", "rsg_ensemble_step_batched", "rsg_solver_solve_batched"):
             args[0] = 1  # one member, given as a null array
         assert f(*args) == abi.BAD_ARG, name
         checked.append(name)
