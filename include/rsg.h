@@ -312,6 +312,20 @@ typedef struct {
 } rsg_corey;
 
 enum { RSG_SOURCE_FIXED = 0, RSG_SOURCE_REGULAR = 1 };
+/* Tabular rock-fluid models in place of Corey (rsg_sim_set_rock_tables):
+ * RSG_RF_TABULAR is rock/TabularRockFluid.java:31-93: 1D tables krw(Sw),
+ * krg(Sg), krow(So), krog(So + Sw), kro = (Sg krog(So + Sw) + Sw krow(So)) /
+ * (Sg + Sw) (water must be present), pcow(Sw), pcgo(Sg);
+ * RSG_RF_THREE_PHASE_TABULAR is rock/ThreePhaseTabularRockFluid.java:31-80:
+ * 2D tables krw, krg, kro, pcow, pcgo of (Sw, Sg).  Relative permeability
+ * tables must stay within [0, 1]; capillary pressures default to the
+ * constant 0 (kind RSG_FN_CONSTANT, value 0). */
+enum { RSG_RF_COREY = 0, RSG_RF_TABULAR = 1, RSG_RF_THREE_PHASE_TABULAR = 2 };
+typedef struct {
+  int32_t kind;
+  rsg_function krw, krg, krow, krog, kro, pcow, pcgo;
+} rsg_rock_tables;
+
 /* field/Source.java: Fixed (locked cells) and Regular (mol/s per element) */
 typedef struct {
   int32_t type;
@@ -381,6 +395,24 @@ rsg_status rsg_sim_retract(rsg_sim* s);
  * (numerics/Main.java:86-105). */
 rsg_status rsg_sim_save_state(rsg_sim* s);
 rsg_status rsg_sim_restore_state(rsg_sim* s);
+/* Replaces the simulator's rock-fluid model (RockFluid.create's "Tabular" and
+ * "ThreePhaseTabular" choices) and recomputes the secondaries.  RSG_RF_COREY
+ * returns to the Corey model the simulator was created with.  Table
+ * arrays are copied.  RSG_BAD_ARG for wrong table dimensions or relative
+ * permeabilities outside [0, 1]. */
+rsg_status rsg_sim_set_rock_tables(rsg_sim* s, const rsg_rock_tables* t);
+/* Restart files (numerics/Main.java:86-105 saves the Field at report times;
+ * field/Field.java:207-262 restarts from its primary variables).  The file
+ * holds time, p, reference pressure, T and N: "RSGRST01", int32 n, nc, 1, 0,
+ * float64 time, then float64 p[n], p0[n], T[n], N[nc][n].
+ * rsg_sim_read_restart needs a simulator of the same n and nc (RSG_BAD_ARG
+ * otherwise), loads the primaries, drops the per-phase records of earlier
+ * evaluations as new control volumes would, and recomputes the secondaries.
+ * Fixed source cells keep the values in the file (Field's constructor
+ * re-balances them, which returns the same values while their pressure,
+ * temperature and composition are those of the run that wrote the file). */
+rsg_status rsg_sim_write_restart(rsg_sim* s, const char* path);
+rsg_status rsg_sim_read_restart(rsg_sim* s, const char* path);
 /* Discrete adjoint of a simulator run (Discretisation's sequential pressure
  * Newton step and explicit molar update, numerics/Discretisation.java:280-919;
  * black-oil fluids with at most 3 components).  rsg_sim_forward runs nsteps

@@ -425,6 +425,18 @@ int orc_sim_step_to(void* h, double end_time, const rsg_dt_control* c, double* d
   }
 }
 
+int orc_sim_set_rock_tables(void* h, const rsg_rock_tables* t, char* err, int errlen) {
+  try {
+    Simulator* s = (Simulator*)h;
+    s->rockFluid.setTables(*t);
+    s->calculateSecondaries();
+    return 0;
+  } catch (Failure& f) {
+    put_err(err, errlen, f.what());
+    return f.status;
+  }
+}
+
 int orc_sim_retract(void* h) {
   ((Simulator*)h)->retract();
   return 0;

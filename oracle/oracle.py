@@ -61,6 +61,8 @@ def _declare(L):
                                        P(abi.rsg_source), P(abi.rsg_initial), P(abi.rsg_runspec), P(i), C.c_char_p, i]
     L.orc_sim_step.argtypes = [vp, d, P(abi.rsg_step_info), C.c_char_p, i]
     L.orc_sim_retract.argtypes = [vp]
+    L.orc_sim_set_rock_tables.argtypes = [vp, P(abi.rsg_rock_tables), C.c_char_p, i]
+    L.orc_sim_set_rock_tables.restype = i
     L.orc_sim_state.argtypes = [vp, P(d), P(d), P(d)]
     L.orc_sim_jacobian.argtypes = [vp, P(d), P(d)]
     L.orc_sim_residual_volume.argtypes = [vp, P(d), P(d)]
@@ -334,6 +336,14 @@ class Simulator:
 
     def retract(self):
         lib().orc_sim_retract(self.h)
+
+    def set_rock_tables(self, tables):
+        """TabularRockFluid / ThreePhaseTabularRockFluid in place of Corey."""
+        self._tables = tables
+        err = C.create_string_buffer(512)
+        st = lib().orc_sim_set_rock_tables(self.h, C.byref(tables), err, 512)
+        if st != 0:
+            raise OracleError(st, err.value.decode())
 
     def state(self):
         p = np.zeros(self.n)

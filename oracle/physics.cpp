@@ -422,10 +422,66 @@ double Corey::effectiveSaturation(int phase, double S) const {
   Se /= denom;
   return Se;
 }
+// TabularRockFluid (rock/TabularRockFluid.java:31-57): relative
+// permeability tables must have outputs in [0, 1] (getRelPermTable :52-57),
+// capillary pressures default to zero
+void Corey::setTables(const rsg_rock_tables& t) {
+  if (t.kind == RSG_RF_COREY) {
+    kind = RSG_RF_COREY;
+    return;
+  }
+  if (t.kind != RSG_RF_TABULAR && t.kind != RSG_RF_THREE_PHASE_TABULAR) throw Failure(ST_BAD_ARG, "rock-fluid kind");
+  const int dim = t.kind == RSG_RF_TABULAR ? 1 : 2;
+  auto relperm_table = [&](const rsg_function& f) {
+    Function k(f);
+    if (f.kind != RSG_FN_CONSTANT && f.dim != dim) throw Failure(ST_BAD_ARG, "relative permeability table dimension");
+    if (k.minOutput() < 0 || k.maxOutput() > 1)
+      throw Failure(ST_BAD_ARG, "relative permeabilities must have values between 0 and 1");
+    return k;
+  };
+  auto pc_table = [&](const rsg_function& f) {
+    if (f.kind != RSG_FN_CONSTANT && f.dim != dim) throw Failure(ST_BAD_ARG, "capillary pressure table dimension");
+    return Function(f);
+  };
+  krw = relperm_table(t.krw);
+  krg = relperm_table(t.krg);
+  if (t.kind == RSG_RF_TABULAR) {
+    krow = relperm_table(t.krow);
+    krog = relperm_table(t.krog);
+  } else {
+    kro = relperm_table(t.kro);
+  }
+  pcowF = pc_table(t.pcow);
+  pcgoF = pc_table(t.pcgo);
+  kind = t.kind;
+}
+
 void Corey::relperm(const double* S, double* kr) const {
+  if (kind == RSG_RF_TABULAR) {
+    // TabularRockFluid.calculateRelativePermeability (:60-73)
+    kr[WATER] = krw.get(&S[WATER]);
+    kr[GAS] = krg.get(&S[GAS]);
+    if (S[WATER] <= 0) throw Failure(ST_PHYSICS, "Water is not present");
+    const double sow = S[OIL] + S[WATER];
+    kr[OIL] = (S[GAS] * krog.get(&sow) + S[WATER] * krow.get(&S[OIL])) / (S[GAS] + S[WATER]);
+    return;
+  }
+  if (kind == RSG_RF_THREE_PHASE_TABULAR) {
+    // ThreePhaseTabularRockFluid.calculateRelativePermeability (:72-78)
+    const double wg[2] = {S[WATER], S[GAS]};
+    kr[WATER] = krw.get(wg);
+    kr[GAS] = krg.get(wg);
+    kr[OIL] = kro.get(wg);
+    return;
+  }
   for (int ph = 0; ph < 3; ++ph) kr[ph] = c.ke[ph] * jpow(effectiveSaturation(ph, S[ph]), c.n[ph]);
 }
 double Corey::pcow(const double* S) const {
+  if (kind == RSG_RF_TABULAR) return pcowF.get(&S[WATER]);
+  if (kind == RSG_RF_THREE_PHASE_TABULAR) {
+    const double wg[2] = {S[WATER], S[GAS]};
+    return pcowF.get(wg);
+  }
   double Sw = effectiveSaturation(WATER, S[WATER]), So = effectiveSaturation(OIL, S[OIL]);
   double pc = 0;
   if (Sw > 0) pc += c.cw / jpow(Sw, c.aw);
@@ -433,6 +489,11 @@ double Corey::pcow(const double* S) const {
   return pc;
 }
 double Corey::pcgo(const double* S) const {
+  if (kind == RSG_RF_TABULAR) return pcgoF.get(&S[GAS]);
+  if (kind == RSG_RF_THREE_PHASE_TABULAR) {
+    const double wg[2] = {S[WATER], S[GAS]};
+    return pcgoF.get(wg);
+  }
   double Sg = effectiveSaturation(GAS, S[GAS]), So = effectiveSaturation(OIL, S[OIL]);
   double pc = 0;
   if (Sg > 0) pc += c.cg / jpow(Sg, c.ag);

@@ -62,8 +62,13 @@ struct BlackOil {
   void calculatePhaseState(double p, const double* N, double T, EOSData* data) const;
 };
 
+// CoreyRockFluid, or (kind != RSG_RF_COREY) TabularRockFluid /
+// ThreePhaseTabularRockFluid
 struct Corey {
   rsg_corey c;
+  int kind = RSG_RF_COREY;
+  Function krw, krg, krow, krog, kro, pcowF, pcgoF;
+  void setTables(const rsg_rock_tables& t);
   double effectiveSaturation(int phase, double S) const;
   void relperm(const double* S, double* kr) const;
   double pcow(const double* S) const;

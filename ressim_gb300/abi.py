@@ -73,6 +73,22 @@ class rsg_blackoil(C.Structure):
     ]
 
 
+RF_COREY, RF_TABULAR, RF_THREE_PHASE_TABULAR = 0, 1, 2
+
+
+class rsg_rock_tables(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("krw", rsg_function),
+        ("krg", rsg_function),
+        ("krow", rsg_function),
+        ("krog", rsg_function),
+        ("kro", rsg_function),
+        ("pcow", rsg_function),
+        ("pcgo", rsg_function),
+    ]
+
+
 class rsg_corey(C.Structure):
     _fields_ = [
         ("Sr", C.c_double * 3),

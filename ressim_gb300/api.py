@@ -127,6 +127,9 @@ def _declare(L):
         "rsg_ensemble_step": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
         "rsg_ensemble_step_batched": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
         "rsg_solver_solve_batched": (i32, [i32, P(vp), P(vp), P(vp), P(vp), i32, P(abi.rsg_solve_info), P(i32)]),
+        "rsg_sim_set_rock_tables": (i32, [vp, P(abi.rsg_rock_tables)]),
+        "rsg_sim_write_restart": (i32, [vp, C.c_char_p]),
+        "rsg_sim_read_restart": (i32, [vp, C.c_char_p]),
         "rsg_mm_read_matrix_size": (i32, [C.c_char_p, P(i32), P(i32), P(C.c_int64)]),
         "rsg_mm_read_csr": (i32, [C.c_char_p, i32, C.c_int64, P(i32), P(i32), P(d)]),
         "rsg_mm_write_csr": (i32, [C.c_char_p, i32, i32, P(i32), P(i32), P(d)]),
@@ -556,6 +559,19 @@ class Discretisation:
 
     def retract(self):
         self.ctx.check(lib().rsg_sim_retract(self.h), "retract")
+
+    def set_rock_tables(self, tables):
+        """TabularRockFluid / ThreePhaseTabularRockFluid (abi.rsg_rock_tables)
+        in place of the Corey model; the tables are copied."""
+        self.ctx.check(lib().rsg_sim_set_rock_tables(self.h, C.byref(tables)), "set_rock_tables")
+
+    def write_restart(self, path):
+        """The primary state (time, p, reference p, T, N) to a restart file."""
+        self.ctx.check(lib().rsg_sim_write_restart(self.h, os.fsencode(path)), "write_restart")
+
+    def read_restart(self, path):
+        """Restart from a file written by write_restart (Field(Field, ...))."""
+        self.ctx.check(lib().rsg_sim_read_restart(self.h, os.fsencode(path)), "read_restart")
 
     def time(self):
         """Field.getTime [s]."""

@@ -202,7 +202,7 @@ __device__ S mole_fraction(const S* N, int nc, int nu) {
 
 // Flags raised by the property chain (first one wins)
 enum { FL_NONE = 0, FL_DRDP = 1, FL_DENSITY = 2, FL_WATER_DERIV = 3, FL_BLACKOIL_CHECK = 4, FL_ENTHALPY = 5, FL_PATTERN = 6,
-       FL_CUBIC = 16 };  // FL_CUBIC + CUBIC_* code
+       FL_NO_WATER = 7, FL_CUBIC = 16 };  // FL_CUBIC + CUBIC_* code
 
 // S = double for the simulator; a dual number for the adjoint's local derivatives
 template <class S>
@@ -396,6 +396,8 @@ struct SimDev {
   const DCubic* cub;  // cubic equation of state (nullptr: black-oil)
   DFluid fl;
   DCorey co;
+  int rf_kind;        // RSG_RF_*: Corey (co) or the tables below
+  DFunc krw, krg, krow, krog, kro, pcow_t, pcgo_t;
   const double* phi0;
   const double* cr;
   const double* vol;
@@ -454,11 +456,30 @@ __device__ void cell_eval(const SimDev& d, int i, S p, double p0, const PhaseT<S
   S Vf = 0;
   for (int a = 0; a < 3; ++a) Vf += ph[a].V;
   for (int a = 0; a < 3; ++a) o.sat[a] = ph[a].V / Vf;
-  // Corey relative permeability and capillary pressures
+  // relative permeability and capillary pressures
   S kr[3];
-  for (int a = 0; a < 3; ++a) kr[a] = d.co.ke[a] * jpow(eff_sat(d.co, a, o.sat[a]), d.co.n[a]);
   S pcow = 0, pcgo = 0;
-  {
+  if (d.rf_kind == RSG_RF_TABULAR) {
+    // TabularRockFluid.calculateRelativePermeability and capillary pressures
+    // (rock/TabularRockFluid.java:60-91)
+    kr[0] = f_eval(d.krw, -1, &o.sat[0]);
+    kr[2] = f_eval(d.krg, -1, &o.sat[2]);
+    if (o.sat[0] <= 0) atomicCAS(d.flag, 0, FL_NO_WATER);
+    const S sow = o.sat[1] + o.sat[0];
+    kr[1] = (o.sat[2] * f_eval(d.krog, -1, &sow) + o.sat[0] * f_eval(d.krow, -1, &o.sat[1])) / (o.sat[2] + o.sat[0]);
+    pcow = f_eval(d.pcow_t, -1, &o.sat[0]);
+    pcgo = f_eval(d.pcgo_t, -1, &o.sat[2]);
+  } else if (d.rf_kind == RSG_RF_THREE_PHASE_TABULAR) {
+    // ThreePhaseTabularRockFluid (rock/ThreePhaseTabularRockFluid.java:60-78)
+    const S wg[2] = {o.sat[0], o.sat[2]};
+    kr[0] = f_eval(d.krw, -1, wg);
+    kr[2] = f_eval(d.krg, -1, wg);
+    kr[1] = f_eval(d.kro, -1, wg);
+    pcow = f_eval(d.pcow_t, -1, wg);
+    pcgo = f_eval(d.pcgo_t, -1, wg);
+  } else {
+    // CoreyRockFluid
+    for (int a = 0; a < 3; ++a) kr[a] = d.co.ke[a] * jpow(eff_sat(d.co, a, o.sat[a]), d.co.n[a]);
     S Sw = eff_sat(d.co, 0, o.sat[0]), So = eff_sat(d.co, 1, o.sat[1]);
     if (Sw > 0) pcow += d.co.cw / jpow(Sw, d.co.aw);
     if (So > 0) pcow -= d.co.cow / jpow(So, d.co.aow);
@@ -1268,6 +1289,8 @@ struct Sim {
   rsg_runspec spec;
   int n, nc, nconn;
   HostFunc funcs[11];
+  int rf_kind = RSG_RF_COREY;
+  HostFunc rock_tab[7];  // krw, krg, krow, krog, kro, pcow, pcgo
   HostFunc initT, initC[NCM];
   DFluid fl{};
   DCorey co{};
@@ -1298,6 +1321,14 @@ struct Sim {
     d.nconn = nconn;
     d.fl = fl;
     d.co = co;
+    d.rf_kind = rf_kind;
+    d.krw = rock_tab[0].d;
+    d.krg = rock_tab[1].d;
+    d.krow = rock_tab[2].d;
+    d.krog = rock_tab[3].d;
+    d.kro = rock_tab[4].d;
+    d.pcow_t = rock_tab[5].d;
+    d.pcgo_t = rock_tab[6].d;
     d.cub = cubic.size() ? cubic.get() : nullptr;
     d.phi0 = phi0.get();
     d.cr = cr.get();
@@ -1338,6 +1369,7 @@ struct Sim {
     RSG_CUDA(cudaMemcpyAsync(&h, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
     if (h == FL_DRDP) throw Error(RSG_PHYSICS, "dR/dp must be positive (check PVT data or datum depth/pressure)");
+    if (h == FL_NO_WATER) throw Error(RSG_PHYSICS, "Water is not present");
     if (h == FL_CUBIC + 2) throw Error(RSG_SINGULAR, "MatrixSingularException in the flash");
     if (h > FL_CUBIC) throw Error(RSG_PHYSICS, "cubic equation of state failed (code " + std::to_string(h - FL_CUBIC) + ")");
     if (h) throw Error(RSG_PHYSICS, "equation-of-state data check failed (code " + std::to_string(h) + ")");
@@ -2296,6 +2328,124 @@ rsg_status rsg_sim_restore_state(rsg_sim* s) {
     if (!m.has_saved) throw rsg::Error(RSG_BAD_ARG, "no saved state: call rsg_sim_save_state first");
     m.unsnap(m.saved);
     m.ctx->sync();
+    m.check_flag();
+  });
+}
+
+// Restart files.  RS saves the whole Field object at every report time
+// (numerics/Main.java:86-105) and a restarted run keeps only its primary
+// variables (field/Field.java:207-262, copyPrimary: time, pressure,
+// reference pressure, temperature, moles) and recomputes everything else.
+// The file holds exactly those, in this layout (little-endian as written):
+//   8 bytes  "RSGRST01"
+//   int32    n, nc, 1 (layout version), 0
+//   float64  time
+//   float64  p[n], p0[n] (reference pressure), T[n], N[nc][n] (component major)
+namespace {
+constexpr char kRestartMagic[8] = {'R', 'S', 'G', 'R', 'S', 'T', '0', '1'};
+}
+
+rsg_status rsg_sim_write_restart(rsg_sim* s, const char* path) {
+  if (!s || !path) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    const size_t n = (size_t)m.n, nc = (size_t)m.nc;
+    std::vector<double> buf((3 + nc) * n);
+    RSG_CUDA(cudaMemcpyAsync(buf.data(), m.p.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(buf.data() + n, m.p0.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(buf.data() + 2 * n, m.T.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, m.ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(buf.data() + 3 * n, m.N.get(), sizeof(double) * nc * n, cudaMemcpyDeviceToHost,
+                             m.ctx->stream));
+    m.ctx->sync();
+    FILE* f = std::fopen(path, "wb");
+    if (!f) throw rsg::Error(RSG_BAD_ARG, std::string("cannot write ") + path);
+    const int32_t hdr[4] = {m.n, m.nc, 1, 0};
+    const bool ok = std::fwrite(kRestartMagic, 1, 8, f) == 8 && std::fwrite(hdr, sizeof hdr, 1, f) == 1 &&
+                    std::fwrite(&m.time, sizeof(double), 1, f) == 1 &&
+                    std::fwrite(buf.data(), sizeof(double), buf.size(), f) == buf.size();
+    if (std::fclose(f) != 0 || !ok) throw rsg::Error(RSG_BAD_ARG, std::string("cannot write ") + path);
+  });
+}
+
+rsg_status rsg_sim_read_restart(rsg_sim* s, const char* path) {
+  if (!s || !path) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) throw rsg::Error(RSG_BAD_ARG, std::string("cannot read ") + path);
+    char magic[8];
+    int32_t hdr[4];
+    double t = 0;
+    const size_t n = (size_t)m.n, nc = (size_t)m.nc;
+    std::vector<double> buf((3 + nc) * n);
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::fread(hdr, sizeof hdr, 1, f) == 1;
+    ok = ok && std::memcmp(magic, kRestartMagic, 8) == 0 && hdr[0] == m.n && hdr[1] == m.nc && hdr[2] == 1;
+    ok = ok && std::fread(&t, sizeof(double), 1, f) == 1 && std::fread(buf.data(), sizeof(double), buf.size(), f) ==
+                                                                  buf.size();
+    std::fclose(f);
+    if (!ok) throw rsg::Error(RSG_BAD_ARG, std::string("not a restart file of this simulator: ") + path);
+    RSG_CUDA(cudaMemcpyAsync(m.p.get(), buf.data(), sizeof(double) * n, cudaMemcpyHostToDevice, m.ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(m.p0.get(), buf.data() + n, sizeof(double) * n, cudaMemcpyHostToDevice, m.ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(m.T.get(), buf.data() + 2 * n, sizeof(double) * n, cudaMemcpyHostToDevice, m.ctx->stream));
+    RSG_CUDA(cudaMemcpyAsync(m.N.get(), buf.data() + 3 * n, sizeof(double) * nc * n, cudaMemcpyHostToDevice,
+                             m.ctx->stream));
+    // new control volumes: no phase records from earlier evaluations
+    RSG_CUDA(cudaMemsetAsync(m.phN.get(), 0, sizeof(double) * m.phN.size(), m.ctx->stream));
+    RSG_CUDA(cudaMemsetAsync(m.phdVdN.get(), 0, sizeof(double) * m.phdVdN.size(), m.ctx->stream));
+    RSG_CUDA(cudaMemsetAsync(m.present.get(), 0, sizeof(int) * n, m.ctx->stream));
+    m.time = t;
+    m.secondaries();
+    m.ctx->sync();  // buf goes out of scope
+    m.check_flag();
+  });
+}
+
+rsg_status rsg_sim_set_rock_tables(rsg_sim* s, const rsg_rock_tables* t) {
+  if (!s || !t) return RSG_BAD_ARG;
+  rsg::Sim& m = *s->s;
+  return guarded(m.ctx, [&] {
+    if (t->kind == RSG_RF_COREY) {
+      m.rf_kind = RSG_RF_COREY;
+    } else {
+      if (t->kind != RSG_RF_TABULAR && t->kind != RSG_RF_THREE_PHASE_TABULAR)
+        throw rsg::Error(RSG_BAD_ARG, "unknown rock-fluid kind");
+      const int dim = t->kind == RSG_RF_TABULAR ? 1 : 2;
+      // TabularRockFluid.getRelPermTable: outputs within [0, 1]
+      auto check = [&](const rsg_function& f, bool relperm) {
+        if (f.kind == RSG_FN_CONSTANT) {
+          if (relperm && (f.value < 0 || f.value > 1))
+            throw rsg::Error(RSG_BAD_ARG, "relative permeabilities must have values between 0 and 1");
+          return;
+        }
+        if (f.dim != dim) throw rsg::Error(RSG_BAD_ARG, "rock-fluid table of the wrong dimension");
+        if (!relperm) return;
+        size_t total = 1;
+        for (int a = 0; a < f.dim; ++a) total *= (size_t)std::max(f.n[a], 0);
+        for (size_t q = 0; q < total; ++q)
+          if (f.data[q] < 0 || f.data[q] > 1)
+            throw rsg::Error(RSG_BAD_ARG, "relative permeabilities must have values between 0 and 1");
+      };
+      const bool two = t->kind == RSG_RF_TABULAR;
+      check(t->krw, true);
+      check(t->krg, true);
+      if (two) {
+        check(t->krow, true);
+        check(t->krog, true);
+      } else {
+        check(t->kro, true);
+      }
+      check(t->pcow, false);
+      check(t->pcgo, false);
+      const rsg_function* f[7] = {&t->krw, &t->krg, &t->krow, &t->krog, &t->kro, &t->pcow, &t->pcgo};
+      for (int q = 0; q < 7; ++q) {
+        const bool used = two ? q != 4 : (q != 2 && q != 3);
+        rsg_function zero{};
+        zero.kind = RSG_FN_CONSTANT;
+        rsg::upload_func(*m.ctx, used ? *f[q] : zero, m.rock_tab[q]);
+      }
+      m.rf_kind = t->kind;
+    }
+    m.secondaries();
     m.check_flag();
   });
 }

@@ -166,6 +166,41 @@ def corey(swc=0.2, sor=0.2, n=2.0):
     return c
 
 
+def rock_tables(keep, kind=abi.RF_TABULAR, swc=0.2, sor=0.2, points=21, pc_kpa=5.0):
+    """Tabular rock-fluid curves (rsg_rock_tables) sampled from power laws
+    with end points swc and sor: RF_TABULAR gives TabularRockFluid's 1D
+    krw(Sw) (exponent 2), krg(Sg) (2), krow(So) (3), krog(So + Sw) (2) and a
+    capillary pressure pcow(Sw) falling from pc_kpa kPa; RF_THREE_PHASE_TABULAR
+    gives ThreePhaseTabularRockFluid's 2D krw, krg, kro and pcow of (Sw, Sg)
+    on a points x points grid of [0, 1]^2 (pcgo 0)."""
+    t = abi.rsg_rock_tables()
+    t.kind = kind
+    s = np.linspace(0.0, 1.0, points)
+
+    def ramp(x, lo, hi, e):
+        return np.clip((x - lo) / (hi - lo), 0.0, 1.0) ** e
+
+    if kind == abi.RF_TABULAR:
+        t.krw = abi.table(keep, [s], ramp(s, swc, 1 - sor, 2.0))
+        t.krg = abi.table(keep, [s], ramp(s, 0.0, 1 - swc, 2.0))
+        t.krow = abi.table(keep, [s], ramp(s, sor, 1 - swc, 3.0))
+        t.krog = abi.table(keep, [s], ramp(s, swc + sor, 1.0, 2.0))
+        t.kro = abi.constant(0.0)
+        t.pcow = abi.table(keep, [s], pc_kpa * 1e3 * (1 - ramp(s, swc, 1 - sor, 1.0)))
+        t.pcgo = abi.constant(0.0)
+    else:
+        W_, G_ = np.meshgrid(s, s, indexing="ij")
+        O_ = 1 - W_ - G_
+        t.krw = abi.table(keep, [s, s], ramp(W_, swc, 1 - sor, 2.0))
+        t.krg = abi.table(keep, [s, s], ramp(G_, 0.0, 1 - swc, 2.0))
+        t.kro = abi.table(keep, [s, s], ramp(O_, sor, 1 - swc, 2.0))
+        t.krow = abi.constant(0.0, 2)
+        t.krog = abi.constant(0.0, 2)
+        t.pcow = abi.table(keep, [s, s], pc_kpa * 1e3 * (1 - ramp(W_, swc, 1 - sor, 1.0)))
+        t.pcgo = abi.constant(0.0, 2)
+    return t
+
+
 def runspec(method=abi.BICGSTAB, precond=abi.PC_ILU, rtol=1e-8, atol=1e-50, max_linear=5000,
             max_newton=10, ptol=1e-6, stop_rule=0, inner_iterations=0, inner_tolerance=0.0, omega=0.0, ax=0.0,
             ay=0.0):
