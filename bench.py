@@ -505,9 +505,9 @@ def ensemble_leg(args):
       threads;
     * batched: rsg_ensemble_step_batched, all members' pressure solves in
       one persistent launch per Newton iteration, FP64 ILU(0) walks;
-    * batched_mixed: the same with the factors' FP32 copies inside the FP64
-      BiCGstab (mixed precision), with its largest pressure difference
-      against the serial FP64 step.
+    * batched_mixed: the same launch with the mixed-precision solver (FP64
+      flexible GMRES around 10 FP32 BiCGstab + FP32 ILU(0) steps), with its
+      largest pressure difference against the serial FP64 step.
     Wall time around each call (host-driven Newton loop included).  The
     members stop Newton on max |dp/p| (RunSpec's alternative rule): the
     reference rule's signed pressure change of one cell sits at the linear

@@ -539,9 +539,11 @@ rsg_status rsg_ensemble_step(int32_t count, rsg_sim* const* sims, const double* 
  * (BiCGstab, mtj/.../sparse/BiCGstab.java:65-116, with ILU(0)) through
  * per-member offsets, and each member updates its pressure and tests its
  * Newton convergence; converged members leave the loop.  Members must use
- * RSG_BICGSTAB with RSG_PC_ILU.  precision 0 walks the FP64 factors; 1 walks
- * their FP32 copies (mixed precision: vectors, SpMV, dots and the stopping
- * test stay FP64, so the relative residual is met in FP64).  A member whose
+ * RSG_BICGSTAB with RSG_PC_ILU.  precision 0: BiCGstab in FP64 with the
+ * FP64 ILU(0) factors; 1: the mixed-precision solver of RSG_FGMRES_MIXED
+ * (FP64 flexible GMRES with the solver's restart around its inner FP32
+ * BiCGstab steps on the FP32 factors and the FP32 copy of A), so the
+ * relative residual is met in FP64.  A member whose
  * step fails stops there (statuses[i], infos[i]); the others go on.  Returns
  * the first failing member's status.  Results agree with rsg_sim_step per
  * member to the Krylov solver's rounding (the dot products are summed in a

@@ -754,9 +754,10 @@ def write_matrix_market_vector(path, x):
 def ensemble_step_batched(sims, dts, precision=0):
     """One time step of every Discretisation of `sims` in lockstep, with the
     pressure solves of all members in one persistent launch per Newton
-    iteration (rsg_ensemble_step_batched).  precision 0: FP64 ILU(0) walks;
-    1: the factors' FP32 copies inside the FP64 BiCGstab.  Returns
-    (per-member rsg_step_info list, statuses)."""
+    iteration (rsg_ensemble_step_batched).  precision 0: FP64 BiCGstab +
+    ILU(0); 1: the mixed-precision solver (FP64 flexible GMRES around FP32
+    BiCGstab + FP32 ILU(0)).  Returns (per-member rsg_step_info list,
+    statuses)."""
     n = len(sims)
     hs = (C.c_void_p * n)(*[s.h for s in sims])
     d = np.ascontiguousarray(np.broadcast_to(np.asarray(dts, np.float64), (n,)))

@@ -18,11 +18,11 @@
 //   through distributed shared memory in a fixed tree, so every CTA holds
 //   the same scalars and the result does not depend on the cluster shape
 //   (16 CTAs of 4 warps or 8 CTAs of 8 warps give identical bits);
-// * the ILU(0) triangular solves are the level walks of ring.cuh, in FP64
-//   (plain mode) or on the FP32 copies of the factors (mixed precision: the
-//   Krylov vectors, SpMV, dots and updates stay FP64; BiCGstab's recursively
-//   updated residual equals b - A x whatever the preconditioner applies, so
-//   the FP64 stopping test keeps its meaning).
+// * the ILU(0) triangular solves are the level walks of ring.cuh.
+// Precision 0 is BiCGstab in FP64 with the FP64 factors.  Precision 1 is the
+// mixed-precision solver of krylov.cu's run_fgmres_mixed (FP64 flexible
+// GMRES around a short FP32 BiCGstab with the FP32 factors and the FP32
+// copy of A) in the same persistent form (k_ens_fgmres).
 //
 // The scalar recurrences, monitor and zero tests follow BiCGstab.java and
 // DefaultIterationMonitor.java as krylov.cu's BiCGstab does; only the
@@ -52,15 +52,20 @@ struct EnsMember {
   const float* udiagf;
   const double* b;
   double* x;  // initial guess in, solution out
-  double* w;  // 9 vectors of n: r, rtilde, p, v, phat, s, shat, t, y
-  float* f;   // 3 vectors of n (FP32 walks)
+  double* w;  // FP64 BiCGstab: 9 vectors of n (r, rtilde, p, v, phat, s, shat, t, y);
+              // FGMRES: r, w, then V (restart + 1 vectors) and Z (restart vectors)
+  float* f;   // FGMRES: the 10 FP32 vectors of the inner BiCGstab and its ILU(0) solves
+  const float* valf;  // FP32 SELL values of A (inner SpMV)
   double rtol, atol, dtol;
   int maxIter;
+  int restart, inner_iters;
+  double inner_rtol;
 };
 
 struct EnsResult {
   double residual, initR;
   int iterations, status;
+  int inner;  // FGMRES: inner FP32 iterations summed
 };
 
 struct EnsArgs {
@@ -117,34 +122,23 @@ __device__ __noinline__ bool walk(const RingArgs& g, const RingVals<T>& a, unsig
   return ring_walk<KIND, T, 13, CTAS>(g, a, smem);
 }
 
-// out = M^-1 in (ILU(0): L y = in, U out = y) on the cluster; ends with a
-// cluster barrier, so out is complete for every thread of the cluster.
-template <typename TW, int CTAS>
+// out = M^-1 in (ILU(0): L y = in, U out = y, FP64 factors) on the cluster;
+// ends with a cluster barrier, so out is complete for every thread of the
+// cluster.
+template <int CTAS>
 __device__ __noinline__ bool ens_precond(const EnsMember& m, const double* in, double* out, unsigned char* smem,
-                                            int gtid, int nt, cg::cluster_group& cluster) {
-  const int n = m.n;
-  if constexpr (sizeof(TW) == 4) {
-    float *fb = m.f, *fy = m.f + n, *fz = m.f + 2 * (size_t)n;
-    for (int i = gtid; i < n; i += nt) fb[i] = (float)in[i];
-    // the walk starts with a cluster barrier, which publishes fb
-    const RingVals<float> lo{m.lvalf, nullptr, fb, fy, nullptr};
-    if (!walk<SW_ILU_LOWER, float, CTAS>(m.gl, lo, smem)) return false;
-    const RingVals<float> up{m.uvalf, m.udiagf, fy, fz, nullptr};
-    if (!walk<SW_ILU_UPPER, float, CTAS>(m.gu, up, smem)) return false;
-    for (int i = gtid; i < n; i += nt) out[i] = (double)__ldcg(fz + i);
-  } else {
-    double* y = m.w + 8 * (size_t)n;
-    const RingVals<double> lo{m.lval, nullptr, in, y, nullptr};
-    if (!walk<SW_ILU_LOWER, double, CTAS>(m.gl, lo, smem)) return false;
-    const RingVals<double> up{m.uval, m.udiag, y, out, nullptr};
-    if (!walk<SW_ILU_UPPER, double, CTAS>(m.gu, up, smem)) return false;
-  }
+                                         cg::cluster_group& cluster) {
+  double* y = m.w + 8 * (size_t)m.n;
+  const RingVals<double> lo{m.lval, nullptr, in, y, nullptr};
+  if (!walk<SW_ILU_LOWER, double, CTAS>(m.gl, lo, smem)) return false;
+  const RingVals<double> up{m.uval, m.udiag, y, out, nullptr};
+  if (!walk<SW_ILU_UPPER, double, CTAS>(m.gu, up, smem)) return false;
   cluster.sync();
   return true;
 }
 
-template <typename TW, int CTAS>
-__global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArgs e) {
+template <int CTAS>
+__global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArgs e, size_t) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double part[2 * 3 * (RING_SLICES / CTAS)];
   __shared__ double tot[3];
@@ -224,7 +218,7 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArg
         temp += p[i];
         p[i] = (beta == 0) ? r[i] : r[i] + beta * temp;
       }
-      if (!(walked = ens_precond<TW, CTAS>(m, p, phat, smem, gtid, nt, cluster))) break;
+      if (!(walked = ens_precond<CTAS>(m, p, phat, smem, cluster))) break;
       {
         // v = A phat; alpha = rho_1 / (rtilde . v)
         double a1[1] = {0};
@@ -260,7 +254,7 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArg
           break;
         }
       }
-      if (!(walked = ens_precond<TW, CTAS>(m, s, shat, smem, gtid, nt, cluster))) break;
+      if (!(walked = ens_precond<CTAS>(m, s, shat, smem, cluster))) break;
       {
         // t = A shat; omega = (t . s) / (t . t)
         double a2[2] = {0, 0};
@@ -298,12 +292,385 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArg
     if (!walked) {
       if (gtid == 0) {
         atomicExch(e.abort, 1);
-        e.res[mi] = EnsResult{resid, initR, iter, RSG_TIMEOUT};
+        e.res[mi] = EnsResult{resid, initR, iter, RSG_TIMEOUT, 0};
       }
       return;  // this cluster's shared memory may still receive pushes
     }
     cluster.sync();  // the last updates of x are in place before the next instance
-    if (gtid == 0) e.res[mi] = EnsResult{resid, initR, iter, status == KS_CONVERGED ? RSG_OK : -status};
+    if (gtid == 0) e.res[mi] = EnsResult{resid, initR, iter, status == KS_CONVERGED ? RSG_OK : -status, 0};
+  }
+}
+
+// ------------------------------------------------------------ FGMRES ----
+// Mixed precision: FP64 flexible GMRES(m) (right preconditioned, modified
+// Gram-Schmidt, Givens rotations as GMRES.java:84-176 and krylov.cu's
+// run_fgmres_mixed) whose preconditioner is a short FP32 BiCGstab with the
+// FP32 ILU(0) factors and the FP32 copy of A.  The outer monitor sees the
+// true FP64 residual at each restart and the rotated estimate inside a cycle.
+// The Hessenberg matrix, rotations and outer scalars live in each CTA's
+// shared memory; thread 0 of every CTA applies each epilogue to its copy
+// from the same cluster-wide sums, so the copies stay identical.
+struct GmShared {
+  double rho, vscale, resid, initR;
+  int iter, status, gi, gexit, inner;
+};
+
+__device__ __forceinline__ int gm_monitor(GmShared& g, const EnsMember& m, double r) {
+  g.resid = r;
+  if (g.iter == 0) g.initR = r;
+  if (r < jmax2(m.rtol * g.initR, m.atol)) return 1;
+  if (r > m.dtol * g.initR) return -RSG_NOT_CONVERGED_DIVERGENCE;
+  if (g.iter >= m.maxIter) return -RSG_NOT_CONVERGED_ITERATIONS;
+  if (r != r) return -RSG_NOT_CONVERGED_DIVERGENCE;
+  return 0;
+}
+
+// GivensRotation(x, y) (mtj/src/no/uib/cipr/matrix/GivensRotation.java:42-58)
+__device__ __forceinline__ void ens_givens(double x, double y, double* c, double* sn) {
+  double roe = fabs(x) > fabs(y) ? x : y;
+  double scale = fabs(x) + fabs(y);
+  if (scale != 0) {
+    double xs = x / scale, ys = y / scale;
+    double r = scale * sqrt(xs * xs + ys * ys);
+    if (roe < 0) r *= -1;
+    *c = x / r;
+    *sn = y / r;
+  } else {
+    *c = 1;
+    *sn = 0;
+  }
+}
+
+// out = M^-1 in with the FP32 factors (L y = in, U out = y)
+template <int CTAS>
+__device__ __noinline__ bool ens_ilu_f32(const EnsMember& m, const float* in, float* y, float* out,
+                                         unsigned char* smem) {
+  const RingVals<float> lo{m.lvalf, nullptr, in, y, nullptr};
+  if (!walk<SW_ILU_LOWER, float, CTAS>(m.gl, lo, smem)) return false;
+  const RingVals<float> up{m.uvalf, m.udiagf, y, out, nullptr};
+  return walk<SW_ILU_UPPER, float, CTAS>(m.gu, up, smem);
+}
+
+// y = A_f32 x (each product fused, as k_f32_spmv_dot) for the rows of this
+// thread; x was written earlier in the launch by other SMs (read from L2)
+__device__ __forceinline__ float sell_row_f32(const EnsMember& m, const float* x, int i) {
+  const int base = m.sb[i >> 5] + (i & 31), len = m.rl[i];
+  float d = 0;
+#pragma unroll 8
+  for (int k = 0; k < len; ++k) {
+    const int q = base + 32 * k;
+    d = fmaf(m.valf[q], __ldcg(x + m.col[q]), d);
+  }
+  return d;
+}
+
+// The FP32 inner BiCGstab from x = 0 on v (krylov.cu k_inner_reset,
+// k_f32_*): inner_iters steps at most, inner_rtol against its own initial
+// residual, no divergence test; z = its iterate.  Returns false when a walk
+// timed out.  Every thread ends with the same inner iteration count.
+template <int CTAS>
+__device__ bool ens_inner(const EnsMember& m, const double* v, double* z, unsigned char* smem, double* part,
+                          double* tot, int& ph, int gtid, int nt, cg::cluster_group& cluster, int& inner_its) {
+  const int n = m.n;
+  float *ir = m.f, *irt = m.f + (size_t)n, *ip = m.f + 2 * (size_t)n, *iv = m.f + 3 * (size_t)n;
+  float *iph = m.f + 4 * (size_t)n, *is = m.f + 5 * (size_t)n, *ish = m.f + 6 * (size_t)n;
+  float *it = m.f + 7 * (size_t)n, *ix = m.f + 8 * (size_t)n, *iy = m.f + 9 * (size_t)n;
+  double rho_1 = 1, rho_2 = 1, alpha = 1, beta = 1, omega = 1, initR = 0;
+  int iter = 0, first = 1, status = KS_RUNNING;
+  auto monitor = [&](double rn) -> int {
+    if (iter == 0) initR = rn;
+    if (rn < jmax2(m.inner_rtol * initR, 0.0)) return 1;
+    if (iter >= m.inner_iters) return -RSG_NOT_CONVERGED_ITERATIONS;
+    if (rn != rn) return -RSG_NOT_CONVERGED_DIVERGENCE;
+    return 0;
+  };
+  auto top = [&](double rr, double rtr) {
+    const int mo = monitor(sqrt(rr));
+    if (mo != 0) {
+      status = mo;
+      return;
+    }
+    rho_1 = rtr;
+    if (rho_1 == 0 || omega == 0) {
+      status = -RSG_NOT_CONVERGED_BREAKDOWN;
+      return;
+    }
+    if (!first) beta = (rho_1 / rho_2) * (alpha / omega);
+  };
+  {
+    double a2[2] = {0, 0};
+    for (int i = gtid; i < n; i += nt) {
+      const float ri = (float)v[i];
+      ir[i] = ri;
+      irt[i] = ri;
+      ix[i] = 0.f;
+      a2[0] += (double)ri * ri;
+      a2[1] += (double)ri * ri;
+    }
+    cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
+    top(a2[0], a2[1]);
+  }
+  while (status == KS_RUNNING) {
+    for (int i = gtid; i < n; i += nt) {
+      if (first) {
+        ip[i] = ir[i];
+        continue;
+      }
+      const float mo = (float)(-omega), bf = (float)beta;
+      const float temp = mo * iv[i] + ip[i];
+      ip[i] = ir[i] + bf * temp;
+    }
+    if (!ens_ilu_f32<CTAS>(m, ip, iy, iph, smem)) return false;
+    {
+      double a1[1] = {0};
+      for (int i = gtid; i < n; i += nt) {
+        const float d = sell_row_f32(m, iph, i);
+        iv[i] = d;
+        a1[0] += (double)irt[i] * d;
+      }
+      cluster_sum<CTAS, 1>(a1, part, tot, ph, cluster);
+      alpha = rho_1 / a1[0];
+    }
+    {
+      double a1[1] = {0};
+      const float ma = (float)(-alpha);
+      for (int i = gtid; i < n; i += nt) {
+        const float si = ir[i] + ma * iv[i];
+        is[i] = si;
+        a1[0] += (double)si * si;
+      }
+      cluster_sum<CTAS, 1>(a1, part, tot, ph, cluster);
+      // the inner s check keeps the initial residual (krylov.cu EPI_BICG_S_IN)
+      if (sqrt(a1[0]) < jmax2(m.inner_rtol * initR, 0.0)) {
+        const float af = (float)alpha;
+        for (int i = gtid; i < n; i += nt) ix[i] += af * __ldcg(iph + i);
+        status = KS_CONVERGED;
+        break;
+      }
+    }
+    if (!ens_ilu_f32<CTAS>(m, is, iy, ish, smem)) return false;
+    {
+      double a2[2] = {0, 0};
+      for (int i = gtid; i < n; i += nt) {
+        const float d = sell_row_f32(m, ish, i);
+        it[i] = d;
+        a2[0] += (double)d * is[i];
+        a2[1] += (double)d * d;
+      }
+      cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
+      omega = a2[0] / a2[1];
+    }
+    {
+      double a2[2] = {0, 0};
+      const float af = (float)alpha, of = (float)omega;
+      for (int i = gtid; i < n; i += nt) {
+        ix[i] = ix[i] + af * __ldcg(iph + i) + of * __ldcg(ish + i);
+        const float ri = is[i] - of * it[i];
+        ir[i] = ri;
+        a2[0] += (double)ri * ri;
+        a2[1] += (double)irt[i] * ri;
+      }
+      cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
+      rho_2 = rho_1;
+      iter++;
+      first = 0;
+      top(a2[0], a2[1]);
+    }
+  }
+  for (int i = gtid; i < n; i += nt) z[i] = (double)ix[i];
+  inner_its += iter;
+  return true;
+}
+
+template <int CTAS>
+__global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_fgmres(EnsArgs e, size_t ring_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double part[2 * 3 * (RING_SLICES / CTAS)];
+  __shared__ double tot[3];
+  __shared__ int take;
+  __shared__ GmShared g;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int nt = CTAS * (int)blockDim.x, gtid = rank * (int)blockDim.x + (int)threadIdx.x;
+  const bool lead = threadIdx.x == 0;
+  int ph = 0;
+  for (;;) {
+    if (rank == 0 && lead) take = *(volatile int*)e.abort ? e.count : atomicAdd(e.queue, 1);
+    cluster.sync();
+    const int mi = *cluster.map_shared_rank(&take, 0);
+    cluster.sync();
+    if (mi >= e.count) return;
+    const EnsMember& m = e.mem[mi];
+    const int n = m.n, mr = m.restart, ld = mr + 1;
+    double* H = reinterpret_cast<double*>(smem + ring_bytes);  // (m + 1) x m, column major
+    double *sv = H + (size_t)ld * mr, *gc = sv + ld, *gs = gc + ld;
+    double *r = m.w, *w = m.w + (size_t)n, *V = m.w + 2 * (size_t)n, *Z = V + (size_t)ld * n, *x = m.x;
+    if (lead) {
+      g.iter = 0;
+      g.status = 0;
+      g.inner = 0;
+      g.initR = g.resid = 0;
+      for (int q = 0; q < ld * mr; ++q) H[q] = 0;
+    }
+    __syncthreads();
+    bool walked = true;
+    int inner = 0;
+    for (;;) {
+      // r = b - A x (A.multAdd order: unfused row sums); |r|
+      double a1[1] = {0};
+      for (int i = gtid; i < n; i += nt) {
+        const int base = m.sb[i >> 5] + (i & 31), len = m.rl[i];
+        double d = 0;
+        for (int k = 0; k < len; ++k) {
+          const int q = base + 32 * k;
+          d += m.val[q] * __ldcg(x + m.col[q]);
+        }
+        const double ri = m.b[i] + -1.0 * d;
+        r[i] = ri;
+        a1[0] += ri * ri;
+      }
+      cluster_sum<CTAS, 1>(a1, part, tot, ph, cluster);
+      if (lead) {
+        // outer loop test, then the first inner test on |s_0| = |r|
+        int mo = gm_monitor(g, m, sqrt(a1[0]));
+        if (mo != 0) {
+          g.status = mo;
+        } else {
+          g.rho = sqrt(a1[0]);
+          g.vscale = 1 / g.rho;
+          for (int q = 0; q <= mr; ++q) sv[q] = 0;
+          sv[0] = g.rho;
+          g.gi = 0;
+          g.gexit = 0;
+          mo = gm_monitor(g, m, fabs(sv[0]));
+          if (mo == 1) g.gexit = 1;
+          else if (mo < 0) g.status = mo;
+        }
+      }
+      __syncthreads();
+      if (g.status != 0) break;
+      {
+        const double a = g.vscale;
+        for (int i = gtid; i < n; i += nt) V[i] = (a == 0) ? 0.0 : a * r[i];
+      }
+      while (!g.gexit && g.status == 0) {
+        const int i = g.gi;
+        double* vi = V + (size_t)i * n;
+        double* zi = Z + (size_t)i * n;
+        // z_i = M(v_i): the inner walks start with a cluster barrier, which publishes v_i
+        if (!(walked = ens_inner<CTAS>(m, vi, zi, smem, part, tot, ph, gtid, nt, cluster, inner))) break;
+        cluster.sync();  // z_i complete before the SpMV gathers it
+        // w = A z_i (mult: unfused row sums, exact zeros stored as +0)
+        for (int q = gtid; q < n; q += nt) {
+          const int base = m.sb[q >> 5] + (q & 31), len = m.rl[q];
+          double d = 0;
+          for (int k = 0; k < len; ++k) {
+            const int c = base + 32 * k;
+            d += m.val[c] * __ldcg(zi + m.col[c]);
+          }
+          w[q] = (d != 0) ? d : 0.0;
+        }
+        // modified Gram-Schmidt (GMRES.java:146-162), one reduction per basis vector
+        for (int k2 = 0; k2 <= i + 1; ++k2) {
+          const double h = (k2 > 0) ? -H[(k2 - 1) + i * ld] : 0.0;
+          const double* vprev = k2 > 0 ? V + (size_t)(k2 - 1) * n : nullptr;
+          const double* vk = k2 <= i ? V + (size_t)k2 * n : nullptr;
+          double acc[1] = {0};
+          for (int q = gtid; q < n; q += nt) {
+            double we = w[q];
+            if (k2 > 0 && h != 0) {
+              we += h * vprev[q];
+              w[q] = we;
+            }
+            acc[0] += vk ? we * vk[q] : we * we;
+          }
+          cluster_sum<CTAS, 1>(acc, part, tot, ph, cluster);
+          if (k2 <= i) {
+            if (lead) H[k2 + i * ld] = acc[0];
+            __syncthreads();
+          } else if (lead) {
+            // H(i+1,i) = |w|, rotations (krylov.cu EPI_GM_NORMW)
+            H[i + 1 + i * ld] = sqrt(acc[0]);
+            g.vscale = 1. / H[i + 1 + i * ld];
+            for (int q = 0; q < i; ++q) {
+              const double a = H[q + i * ld], b = H[q + 1 + i * ld];
+              const double temp = gc[q] * a + gs[q] * b;
+              H[q + 1 + i * ld] = -gs[q] * a + gc[q] * b;
+              H[q + i * ld] = temp;
+            }
+            ens_givens(H[i + i * ld], H[i + 1 + i * ld], &gc[i], &gs[i]);
+            {
+              const double a = H[i + i * ld], b = H[i + 1 + i * ld];
+              const double temp = gc[i] * a + gs[i] * b;
+              H[i + 1 + i * ld] = -gs[i] * a + gc[i] * b;
+              H[i + i * ld] = temp;
+            }
+            {
+              const double a = sv[i], b = sv[i + 1];
+              const double temp = gc[i] * a + gs[i] * b;
+              sv[i + 1] = -gs[i] * a + gc[i] * b;
+              sv[i] = temp;
+            }
+            g.gi = i + 1;
+            g.iter++;
+            if (g.gi < mr) {
+              const int mo = gm_monitor(g, m, fabs(sv[g.gi]));
+              if (mo == 1) g.gexit = 1;
+              else if (mo < 0) g.status = mo;
+            } else {
+              g.gexit = 1;
+            }
+          }
+        }
+        __syncthreads();
+        {
+          const double a = g.vscale;
+          double* vn = V + (size_t)(i + 1) * n;
+          for (int q = gtid; q < n; q += nt) vn[q] = (a == 0) ? 0.0 : a * w[q];
+        }
+      }
+      if (!walked || g.status != 0) break;
+      // UpperTriangDenseMatrix(H, i).solve(s, s), then x += sum_j s_j z_j
+      if (lead) {
+        const int mm = g.gi;
+        bool singular = false;
+        for (int q = 0; q < mm; ++q)
+          if (H[q + q * ld] == 0) singular = true;
+        if (singular) {
+          g.status = -RSG_SINGULAR;
+        } else {
+          for (int k = mm - 1; k >= 0; --k)
+            if (sv[k] != 0) {
+              sv[k] = sv[k] / H[k + k * ld];
+              for (int q = 0; q < k; ++q) sv[q] -= sv[k] * H[q + k * ld];
+            }
+        }
+      }
+      __syncthreads();
+      if (g.status != 0) break;
+      for (int q = gtid; q < n; q += nt) {
+        double xe = x[q];
+        for (int j = 0; j < g.gi; ++j) {
+          const double sj = sv[j];
+          if (sj != 0) xe += sj * Z[(size_t)j * n + q];
+        }
+        x[q] = xe;
+      }
+      cluster.sync();  // x complete before the residual gathers it
+      if (lead) g.iter++;
+      __syncthreads();
+    }
+    if (!walked) {
+      if (gtid == 0) {
+        atomicExch(e.abort, 1);
+        e.res[mi] = EnsResult{g.resid, g.initR, g.iter, RSG_TIMEOUT, inner};
+      }
+      return;
+    }
+    cluster.sync();  // every CTA is done with this member's vectors and g
+    if (gtid == 0)
+      e.res[mi] = EnsResult{g.resid, g.initR, g.iter, g.status == KS_CONVERGED ? RSG_OK : -g.status, inner};
+    __syncthreads();
   }
 }
 
@@ -324,24 +691,24 @@ struct EnsDevice {
 std::mutex g_ens_mu;
 std::map<int, std::unique_ptr<EnsDevice>> g_ens;
 
-template <typename TW, int CTAS>
-int ens_clusters(EnsDevice& D, int key) {
+using EnsKernel = void (*)(EnsArgs, size_t);
+
+int ens_clusters(EnsDevice& D, int key, EnsKernel kern, int ctas) {
   auto it = D.max_clusters.find(key);
   if (it != D.max_clusters.end()) return it->second;
-  auto kern = k_ens_bicgstab<TW, CTAS>;
   int nclusters = 0;
   bool ok = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RING_SMEM_MAX) ==
             cudaSuccess;
-  if (ok && CTAS > 8)
+  if (ok && ctas > 8)
     ok = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
   if (ok) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(CTAS);
-    cfg.blockDim = dim3(RING_SLICES / CTAS * 32);
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(RING_SLICES / ctas * 32);
     cfg.dynamicSmemBytes = RING_SMEM_MAX;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CTAS;
+    attr[0].val.clusterDim.x = ctas;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
@@ -353,26 +720,25 @@ int ens_clusters(EnsDevice& D, int key) {
   return nclusters;
 }
 
-template <typename TW, int CTAS>
-void ens_launch(EnsDevice& D, int count, int key, size_t smem) {
-  const int fit = ens_clusters<TW, CTAS>(D, key);
+void ens_launch(EnsDevice& D, int count, int key, EnsKernel kern, int ctas, size_t smem, size_t ring_bytes) {
+  const int fit = ens_clusters(D, key, kern, ctas);
   if (fit < 1) throw Error(RSG_UNSUPPORTED, "the ensemble solver's clusters cannot be scheduled on this device");
+  if (smem > RING_SMEM_MAX) throw Error(RSG_UNSUPPORTED, "walk schedule too deep for the ensemble solver");
   const int nclusters = std::min(count, fit);
-  auto kern = k_ens_bicgstab<TW, CTAS>;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(CTAS * nclusters);
-  cfg.blockDim = dim3(RING_SLICES / CTAS * 32);
+  cfg.gridDim = dim3(ctas * nclusters);
+  cfg.blockDim = dim3(RING_SLICES / ctas * 32);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = D.stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = CTAS;
+  attr[0].val.clusterDim.x = ctas;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   EnsArgs a{count, D.mem.get(), D.res.get(), D.ctl.get(), D.ctl.get() + 1};
-  RSG_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+  RSG_CUDA(cudaLaunchKernelEx(&cfg, kern, a, ring_bytes));
 }
 
 }  // namespace
@@ -383,13 +749,13 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
   info.assign(count, rsg_solve_info{});
   status.assign(count, RSG_OK);
   if (count == 0) return;
-  if (precision != 0 && precision != 1) throw Error(RSG_BAD_ARG, "precision must be 0 (FP64) or 1 (FP32 factors)");
+  if (precision != 0 && precision != 1) throw Error(RSG_BAD_ARG, "precision must be 0 (FP64) or 1 (mixed)");
   const int device = sys[0].ctx->device;
   // members the kernel cannot take are reported one by one; the rest run
   std::vector<int> idx;
   std::vector<EnsMember> h;
-  int C = 0, R = 0;
-  size_t nw = 0;
+  int C = 0, R = 0, mr = 0;
+  size_t nw = 0, nf = 0;
   for (int i = 0; i < count; ++i) {
     const EnsSystem& q = sys[i];
     SolverView sv = solver_view(*q.solver);
@@ -433,15 +799,26 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
     m.atol = sv.atol;
     m.dtol = sv.dtol;
     m.maxIter = sv.maxIter;
-    nw += (size_t)A.n;
+    m.restart = std::max(1, sv.restart);
+    m.inner_iters = sv.inner_iters;
+    m.inner_rtol = sv.inner_rtol;
+    if (precision) {
+      A.refresh_sell_f32();
+      m.valf = A.sell_valf.get();
+      mr = std::max(mr, m.restart);
+    }
+    nw += (size_t)A.n * (precision ? (size_t)(3 + 2 * m.restart) : 9);
+    nf += precision ? (size_t)A.n * 10 : 0;
     RSG_CUDA(cudaStreamSynchronize(q.ctx->stream));  // matrix, factors and b are ready
     idx.push_back(i);
     h.push_back(m);
   }
   const int nrun = (int)idx.size();
   if (nrun == 0) return;
-  const size_t smem = precision ? ring_smem_bytes<float>(R) : ring_smem_bytes<double>(R);
-  if (smem > RING_SMEM_MAX) throw Error(RSG_UNSUPPORTED, "walk schedule too deep for the ensemble solver");
+  // shared memory: the ring of the walks (FP64 or FP32 values), then for
+  // FGMRES the Hessenberg matrix, right-hand side and rotations
+  const size_t ring_bytes = precision ? ring_smem_bytes<float>(R) : ring_smem_bytes<double>(R);
+  const size_t smem = ring_bytes + (precision ? sizeof(double) * ((size_t)(mr + 1) * mr + 3 * (size_t)(mr + 1)) : 0);
   EnsDevice* D;
   {
     std::lock_guard<std::mutex> lk(g_ens_mu);
@@ -452,13 +829,14 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
   std::lock_guard<std::mutex> lk(D->mu);
   RSG_CUDA(cudaSetDevice(device));
   if (!D->stream) RSG_CUDA(cudaStreamCreateWithFlags(&D->stream, cudaStreamNonBlocking));
-  if (D->work.size() < nw * 9) D->work.resize(nw * 9);
-  if (precision && D->workf.size() < nw * 3) D->workf.resize(nw * 3);
-  size_t off = 0;
+  if (D->work.size() < nw) D->work.resize(nw);
+  if (nf && D->workf.size() < nf) D->workf.resize(nf);
+  size_t off = 0, offf = 0;
   for (int i = 0; i < nrun; ++i) {
-    h[i].w = D->work.get() + off * 9;
-    h[i].f = precision ? D->workf.get() + off * 3 : nullptr;
-    off += (size_t)h[i].n;
+    h[i].w = D->work.get() + off;
+    h[i].f = precision ? D->workf.get() + offf : nullptr;
+    off += (size_t)h[i].n * (precision ? (size_t)(3 + 2 * h[i].restart) : 9);
+    offf += precision ? (size_t)h[i].n * 10 : 0;
   }
   if (D->mem.size() < (size_t)nrun) D->mem.resize(nrun);
   if (D->res.size() < (size_t)nrun) D->res.resize(nrun);
@@ -468,18 +846,15 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
   RSG_CUDA(cudaMemsetAsync(D->errs.get(), 0, sizeof(int) * nrun, D->stream));
   RSG_CUDA(cudaMemcpyAsync(D->mem.get(), h.data(), sizeof(EnsMember) * nrun, cudaMemcpyHostToDevice, D->stream));
   // instances no cluster reaches (after a walk timed out) report the timeout
-  std::vector<EnsResult> hr(nrun, EnsResult{0, 0, 0, RSG_TIMEOUT});
+  std::vector<EnsResult> hr(nrun, EnsResult{0, 0, 0, RSG_TIMEOUT, 0});
   RSG_CUDA(cudaMemcpyAsync(D->res.get(), hr.data(), sizeof(EnsResult) * nrun, cudaMemcpyHostToDevice, D->stream));
   RSG_CUDA(cudaMemsetAsync(D->ctl.get(), 0, 2 * sizeof(int), D->stream));
   const int key = precision * 100 + C;
-  if (C == 16) {
-    if (precision) ens_launch<float, 16>(*D, nrun, key, smem);
-    else ens_launch<double, 16>(*D, nrun, key, smem);
-  } else if (C == 8) {
-    if (precision) ens_launch<float, 8>(*D, nrun, key, smem);
-    else ens_launch<double, 8>(*D, nrun, key, smem);
-  } else
-    throw Error(RSG_UNSUPPORTED, "ensemble walk schedules must be for clusters of 8 or 16 CTAs");
+  EnsKernel kern = nullptr;
+  if (C == 16) kern = precision ? k_ens_fgmres<16> : k_ens_bicgstab<16>;
+  else if (C == 8) kern = precision ? k_ens_fgmres<8> : k_ens_bicgstab<8>;
+  else throw Error(RSG_UNSUPPORTED, "ensemble walk schedules must be for clusters of 8 or 16 CTAs");
+  ens_launch(*D, nrun, key, kern, C, smem, ring_bytes);
   RSG_CUDA(cudaMemcpyAsync(hr.data(), D->res.get(), sizeof(EnsResult) * nrun, cudaMemcpyDeviceToHost, D->stream));
   RSG_CUDA(cudaStreamSynchronize(D->stream));
   RSG_CUDA(cudaGetLastError());
@@ -488,6 +863,7 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
     info[i].iterations = hr[k].iterations;
     info[i].residual = hr[k].residual;
     info[i].initial_residual = hr[k].initR;
+    info[i].inner_iterations = hr[k].inner;
     info[i].reason = hr[k].status;
     status[i] = hr[k].status;
   }

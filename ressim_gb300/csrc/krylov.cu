@@ -905,7 +905,7 @@ void solver_setup(Solver& s, Csr& A) {
 void solver_solve(Solver& s, Csr& A, const double* b, double* x, rsg_solve_info* info) { s.solve(A, b, x, info); }
 
 SolverView solver_view(Solver& s) {
-  return SolverView{s.method, s.pc_kind, s.pc.get(), s.rtol, s.atol, s.dtol, s.maxIter, s.setup_for, s.ctx};
+  return SolverView{s.method, s.pc_kind, s.pc.get(), s.rtol, s.atol, s.dtol, s.maxIter, s.setup_for, s.ctx, s.restart, s.inner_iters, s.inner_rtol};
 }
 
 void solver_set_inner(Solver& s, int iterations, double rtol) {

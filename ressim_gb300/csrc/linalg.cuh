@@ -135,6 +135,9 @@ struct SolverView {
   int maxIter;
   const Csr* setup_for;  // the matrix of the last setup (nullptr: none)
   Context* ctx;
+  int restart;          // GMRES restart (default 30)
+  int inner_iters;      // mixed precision: FP32 inner BiCGstab steps per outer step
+  double inner_rtol;
 };
 SolverView solver_view(Solver& s);
 // One pressure system of an ensemble member: A x = b with the member's

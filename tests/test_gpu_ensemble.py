@@ -106,8 +106,9 @@ def test_batched_ensemble_is_deterministic_and_order_free():
 
 
 def test_batched_ensemble_mixed_precision():
-    """FP32 factors inside the FP64 BiCGstab (max |dp/p| Newton stop rule, as
-    above): the same Newton counts as the serial FP64 path, pressures within
+    """The mixed-precision solver (FP64 flexible GMRES around FP32 BiCGstab
+    and FP32 ILU(0)) in the persistent launch, max |dp/p| Newton stop rule as
+    above: the same Newton counts as the serial FP64 path, pressures within
     1e-6 of it, mass balance within 1e-12."""
     bat = _members(41, stop_rule=1)
     ser = _members(41, stop_rule=1)
@@ -164,8 +165,8 @@ def test_solve_batched_matches_single_solves(ctx, precision):
     """rsg_solver_solve_batched against rsg_solver_solve system by system
     (BiCGstab + ILU(0) to 1e-10): FP64 walks give the single solves'
     solutions to 1e-8 of their largest entry with iteration counts within a
-    few; FP32 factors (precision 1) meet the tolerance on the true FP64
-    residual."""
+    few; the mixed-precision solver (precision 1) meets the tolerance on the
+    true FP64 residual."""
     from ressim_gb300 import abi
     systems = [_first_jacobian(ctx, *d, seed=s) for d, s in (((10, 8, 4), 3), ((16, 16, 6), 4), ((20, 12, 5), 5))]
     mats, solvers, singles, bs = [], [], [], []
