@@ -170,6 +170,19 @@ rsg_status rsg_solver_setup(rsg_solver* s, rsg_csr* A);
 /* IterativeSolver.solve(A, b, x): x is the initial guess on entry and the
  * solution on exit (host arrays of length n). */
 rsg_status rsg_solver_solve(rsg_solver* s, rsg_csr* A, const double* b, double* x, rsg_solve_info* info);
+/* Level-walk shape of an ILU(0) solver (no counterpart in the reference).
+ * The ILU(0) triangular solves walk the levels on one thread-block cluster,
+ * planned for 16 CTAs of 4 warps and for 8 CTAs of 8 warps; the first setup on
+ * a pattern times both on the factors and keeps the faster per sweep and per
+ * precision (the walk autotuner).  Every shape gives the same bits.
+ * rsg_solver_set_walk_shape(s, 16 or 8) fixes the shape, 0 returns to the
+ * timed choice (applied at the next rsg_solver_setup); rsg_solver_walk_shapes
+ * reports the clusters in use: FP64 lower, upper, FP32 lower, upper (0: no
+ * cluster walk).  RSG_UNSUPPORTED for other preconditioners. */
+rsg_status rsg_solver_set_walk_shape(rsg_solver* s, int32_t ctas);
+rsg_status rsg_solver_walk_shapes(rsg_solver* s, int32_t* shapes);
+/* The same for a simulator's pressure solver. */
+rsg_status rsg_sim_walk_shapes(rsg_sim* s, int32_t* shapes);
 /* Same with device-resident b and x (device pointers from this context). */
 rsg_status rsg_solver_solve_device(rsg_solver* s, rsg_csr* A, const double* d_b, double* d_x, rsg_solve_info* info);
 /* Preconditioner.apply(b, x) on host vectors (after rsg_solver_setup). */
@@ -253,6 +266,31 @@ rsg_status rsg_mesh_get_pattern(rsg_mesh* m, int32_t which, int32_t* row_ptr, in
 /* PotentialCalculator.discretizeFlux into a CSR created with pattern 1:
  * A(here,k) += t_k, A(there,k) -= t_k (numerics/PotentialCalculator.java:319-333). */
 rsg_status rsg_mesh_assemble_potential(rsg_mesh* m, rsg_csr* A);
+/* Connection fluxes: flux[c] = sum over c's MD list of t_k p[element_k], in
+ * list order (PotentialCalculator.calculateFlux, numerics/
+ * PotentialCalculator.java:265-280; LocalFlowRateAverage.computeDarcyFlux,
+ * upscale/LocalFlowRateAverage.java:123-137).  p: elements doubles, flux:
+ * connections doubles (host).  Valid after MPFA or TPFA. */
+rsg_status rsg_mesh_connection_flux(rsg_mesh* m, const double* p, double* flux);
+/* Centre of each connection's here interface (Connection.hereInterface()
+ * .center, which meshgen/partition/PartitionData.java:318,365 classifies):
+ * 3 doubles per connection (host). */
+rsg_status rsg_mesh_get_interface_centers(rsg_mesh* m, double* centers);
+
+/* ------------------------------------------------------- upscaling ----- */
+/* upscale/PressureDiscretisation(mesh, bc) (upscale/PressureDiscretisation
+ * .java:59-196): the steady single-phase pressure problem of flow-based
+ * upscaling.  Pattern without the explicit diagonal; A(here,k) += t_k,
+ * A(there,k) -= t_k over every connection; for each of the nbc boundary
+ * cells b_i = values[q] and row i := e_i (Matrices.zeroRows(A, 1.0, {i})),
+ * every other b_i = 0 (a cell listed twice keeps its last value).  Solved on
+ * the GPU by GMRES(30) + ILU(0) from x = 0 with the reference's
+ * DefaultIterationMonitor (10000 iterations, rtol 1e-50, atol 1e-10, dtol
+ * 1e5).  x: elements doubles out (host), also on failure; info (may be NULL)
+ * the solve.  Returns the solve's status (RSG_NOT_CONVERGED_* as
+ * IterativeSolverNotConvergedException's reasons). */
+rsg_status rsg_upscale_pressure(rsg_mesh* m, int32_t nbc, const int32_t* cells, const double* values, double* x,
+                                rsg_solve_info* info);
 
 /* ------------------------------------------------ discrete adjoint ------ */
 /* No reference counterpart: reverse-mode derivatives of the MPFA-O

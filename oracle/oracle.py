@@ -279,6 +279,41 @@ def potential_matrix(mesh, rowptr, col):
     return val
 
 
+def connection_flux(mesh, p):
+    """PotentialCalculator.calculateFlux (numerics/PotentialCalculator.java:
+    265-280) and LocalFlowRateAverage.computeDarcyFlux (upscale/
+    LocalFlowRateAverage.java:123-137): flux[c] = 0 + t_1 p[el_1] + t_2 p[el_2]
+    + ... in MD list order, one product and one sum rounded at a time."""
+    ptr, el, kk = mesh.transmissibilities()
+    p = _f64(p)
+    flux = np.zeros(len(ptr) - 1)
+    lens = np.diff(ptr)
+    for q in range(int(lens.max()) if len(lens) else 0):
+        m = lens > q
+        idx = ptr[:-1][m] + q
+        flux[m] += kk[idx] * p[el[idx]]
+    return flux
+
+
+def pressure_discretisation(mesh, bc):
+    """upscale/PressureDiscretisation(mesh, bc) (upscale/
+    PressureDiscretisation.java:59-187): the potential pattern and matrix,
+    boundary rows e_i with b_i = p_i, GMRES(30) + ILU(0) from x = 0 with
+    maxIterations 10000, rtol 1e-50, atol 1e-10, dtol 1e5.  bc: {cell: p}.
+    Returns (x, iterations, matrix values, b)."""
+    rp, col = mesh.pattern(1)
+    cells = np.fromiter(bc.keys(), dtype=np.int32, count=len(bc))
+    vals = np.fromiter(bc.values(), dtype=np.float64, count=len(bc))
+    val = potential_matrix(mesh, rp, col)
+    if len(cells):
+        val = zero_rows(rp, col, val, 1.0, cells)
+    b = np.zeros(len(rp) - 1)
+    b[cells] = vals
+    x, it, _, _, _ = solve(abi.GMRES, abi.PC_ILU, rp, col, val, b, np.zeros(len(b)), rtol=1e-50, atol=1e-10,
+                           dtol=1e5, maxit=10000, restart=30)
+    return x, it, val, b
+
+
 class Simulator:
     """Field + Discretisation on the CPU."""
 

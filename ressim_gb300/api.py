@@ -106,6 +106,9 @@ def _declare(L):
         "rsg_mesh_get_transmissibilities": (i32, [vp, P(i32), P(i32), P(d)]),
         "rsg_mesh_get_pattern": (i32, [vp, i32, P(i32), P(i32), P(i64)]),
         "rsg_mesh_assemble_potential": (i32, [vp, vp]),
+        "rsg_mesh_connection_flux": (i32, [vp, P(d), P(d)]),
+        "rsg_mesh_get_interface_centers": (i32, [vp, P(d)]),
+        "rsg_upscale_pressure": (i32, [vp, i32, P(i32), P(d), P(d), P(abi.rsg_solve_info)]),
         "rsg_mesh_transmissibility_adjoint": (i32, [vp, i32, P(d), P(d), P(d)]),
         "rsg_potential_adjoint": (i32, [vp, vp, vp, i32, P(i32), P(d), P(d), P(d), P(d), P(abi.rsg_solve_info)]),
         "rsg_sim_create": (i32, [vp, vp, P(abi.rsg_blackoil), P(abi.rsg_corey), P(d), P(d), i32, P(abi.rsg_source),
@@ -126,6 +129,9 @@ def _declare(L):
         "rsg_sim_backward": (i32, [vp, d, P(d), P(d), P(d), P(abi.rsg_adjoint_info)]),
         "rsg_ensemble_step": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
         "rsg_ensemble_step_batched": (i32, [i32, P(vp), P(d), i32, P(abi.rsg_step_info), P(i32)]),
+        "rsg_solver_set_walk_shape": (i32, [vp, i32]),
+        "rsg_solver_walk_shapes": (i32, [vp, P(i32)]),
+        "rsg_sim_walk_shapes": (i32, [vp, P(i32)]),
         "rsg_solver_solve_batched": (i32, [i32, P(vp), P(vp), P(vp), P(vp), i32, P(abi.rsg_solve_info), P(i32)]),
         "rsg_sim_set_rock_tables": (i32, [vp, P(abi.rsg_rock_tables)]),
         "rsg_sim_write_restart": (i32, [vp, C.c_char_p]),
@@ -333,6 +339,18 @@ class IterativeSolver:
         """Preconditioner.setMatrix(A)"""
         self.ctx.check(lib().rsg_solver_setup(self.h, A.h), "setMatrix")
 
+    def set_walk_shape(self, ctas):
+        """ILU(0) level-walk cluster: 16 or 8 CTAs, 0 for the autotuner's timed
+        choice (applied at the next set_matrix)."""
+        self.ctx.check(lib().rsg_solver_set_walk_shape(self.h, int(ctas)), "set_walk_shape")
+
+    def walk_shapes(self):
+        """Clusters of the ILU(0) walks in use: FP64 lower, upper, FP32 lower,
+        upper (0: no cluster walk)."""
+        v = np.zeros(4, np.int32)
+        self.ctx.check(lib().rsg_solver_walk_shapes(self.h, abi.iptr(v)), "walk_shapes")
+        return v.tolist()
+
     def solve(self, A, b, x0, raise_on_fail=True):
         """IterativeSolver.solve(A, b, x): returns the new x."""
         b = _f64(b)
@@ -486,6 +504,20 @@ class Mesh:
     def assemble_potential(self, A):
         self.ctx.check(lib().rsg_mesh_assemble_potential(self.h, A.h), "assemble_potential")
 
+    def connection_flux(self, p):
+        """flux[c] = sum_k t_k p[el_k] per connection (PotentialCalculator.calculateFlux,
+        LocalFlowRateAverage.computeDarcyFlux)."""
+        p = _f64(p)
+        out = np.zeros(self.counts()["connections"])
+        self.ctx.check(lib().rsg_mesh_connection_flux(self.h, abi.dptr(p), abi.dptr(out)), "connection_flux")
+        return out
+
+    def interface_centers(self):
+        """Centre of each connection's here interface, (connections, 3)."""
+        out = np.zeros((self.counts()["connections"], 3))
+        self.ctx.check(lib().rsg_mesh_get_interface_centers(self.h, abi.dptr(out)), "interface_centers")
+        return out
+
     def transmissibility_adjoint(self, conn_weights, cell_potentials):
         """sum_k sum_c mu_k[c] d(sum_m t_cm phi_k[el_m]) / d log K_e for every element e."""
         mu = np.ascontiguousarray(np.atleast_2d(_f64(conn_weights)))
@@ -564,6 +596,13 @@ class Discretisation:
         """TabularRockFluid / ThreePhaseTabularRockFluid (abi.rsg_rock_tables)
         in place of the Corey model; the tables are copied."""
         self.ctx.check(lib().rsg_sim_set_rock_tables(self.h, C.byref(tables)), "set_rock_tables")
+
+    def walk_shapes(self):
+        """Clusters of the pressure solver's ILU(0) walks (see
+        IterativeSolver.walk_shapes)."""
+        v = np.zeros(4, np.int32)
+        self.ctx.check(lib().rsg_sim_walk_shapes(self.h, abi.iptr(v)), "walk_shapes")
+        return v.tolist()
 
     def write_restart(self, path):
         """The primary state (time, p, reference p, T, N) to a restart file."""

@@ -8,17 +8,22 @@
 // factors, walk schedules and vectors through per-instance offsets (a
 // descriptor table).  Nothing returns to the host between iterations.
 //
-// Inside a cluster:
-// * SpMV, BLAS-1 and the BiCGstab recurrences run over the cluster's 2,048
-//   threads (thread t owns rows t, t + 2048, ...); values that other SMs
-//   wrote earlier in the launch (the walks' outputs, the vectors the walks
-//   read) are loaded from L2 (ld.global.cg), never from a possibly stale L1
-//   line or the read-only cache;
-// * dot products reduce per warp, then across the cluster's 64 warps
+// Inside a cluster (CTAs of 256 threads, one per SM):
+// * SpMV, BLAS-1 and the BiCGstab recurrences run over 4,096 virtual
+//   threads (virtual thread t owns rows t, t + 4096, ...): one per thread in
+//   a 16-CTA cluster, two per thread in an 8-CTA cluster.  Values that other
+//   SMs wrote earlier in the launch (the walks' outputs, the vectors the
+//   walks read) are loaded from L2 (ld.global.cg), never from a possibly
+//   stale L1 line or the read-only cache;
+// * dot products reduce per virtual warp, then across the 128 virtual warps
 //   through distributed shared memory in a fixed tree, so every CTA holds
 //   the same scalars and the result does not depend on the cluster shape
-//   (16 CTAs of 4 warps or 8 CTAs of 8 warps give identical bits);
-// * the ILU(0) triangular solves are the level walks of ring.cuh.
+//   (16 or 8 CTAs give identical bits);
+// * the ILU(0) triangular solves are the level walks of ring.cuh, walked by
+//   the first RING_SLICES / CTAS warps of each CTA (all 8 warps of an 8-CTA
+//   cluster, 4 of the 8 in a 16-CTA cluster, whose other warps only help
+//   with the streaming phases: a 16-SM cluster with 4 warps per SM keeps too
+//   few loads in flight to stream a member's matrix).
 // Precision 0 is BiCGstab in FP64 with the FP64 factors.  Precision 1 is the
 // mixed-precision solver of krylov.cu's run_fgmres_mixed (FP64 flexible
 // GMRES around a short FP32 BiCGstab with the FP32 factors and the FP32
@@ -80,36 +85,92 @@ __device__ __forceinline__ double jmax2(double a, double b) {
   return (a != a || b != b) ? NAN : (a >= b ? a : b);
 }
 
-// Sum of K per-thread values over the cluster; every thread gets the total.
-// part: shared [2][3][warps per CTA], tot: shared [3]; ph alternates the two
-// halves of part so one barrier per reduction suffices.
+constexpr int ENS_THREADS = 256;  // threads per CTA, both cluster shapes
+constexpr int ENS_VT = 4096;      // virtual threads of the row loops
+constexpr int ENS_WPC = ENS_THREADS / 32;
+
+template <int CTAS>
+struct EnsShape {
+  static constexpr int NT = CTAS * ENS_THREADS;  // threads of the cluster
+  static constexpr int VPT = ENS_VT / NT;        // virtual threads per thread
+  static_assert(VPT * NT == ENS_VT, "the cluster must tile the virtual threads");
+};
+
+// The rows of a member, virtual thread by virtual thread: thread gtid runs
+// virtual threads gtid + u * NT (u < VPT), virtual thread vt owns rows vt,
+// vt + ENS_VT, ..., visited in that order.  f(u, i) for each row i.
+template <int CTAS, typename F>
+__device__ __forceinline__ void ens_rows(int n, int gtid, F&& f) {
+  for (int i0 = gtid; i0 < n; i0 += ENS_VT)
+#pragma unroll
+    for (int u = 0; u < EnsShape<CTAS>::VPT; ++u) {
+      const int i = i0 + u * EnsShape<CTAS>::NT;
+      if (i < n) f(u, i);
+    }
+}
+
+// Row i of a SELL-32 matrix times x, entries summed in column-slot order
+// (FUSED: one rounding per entry, else the product rounded, then the sum);
+// x comes from L2 (written by other SMs in the launch).  Unrolled by 8 so
+// that the loads of 8 entries can be in flight together.  (Loading 16
+// entries into register arrays first made the kernel's register demand
+// spill into the level walks it calls, which then ran 2.5x slower.)
+template <bool FUSED, typename T>
+__device__ __forceinline__ T ens_row(const T* __restrict__ val, const int* __restrict__ col, const T* x, int base,
+                                     int len) {
+  T d = 0;
+#pragma unroll 8
+  for (int k = 0; k < len; ++k) {
+    const int q = base + 32 * k;
+    if constexpr (!FUSED) d += val[q] * __ldcg(x + col[q]);
+    else if constexpr (sizeof(T) == 4) d = fmaf(val[q], __ldcg(x + col[q]), d);
+    else d = __fma_rn(val[q], __ldcg(x + col[q]), d);
+  }
+  return d;
+}
+
+// Sum over the member's virtual threads of K values each (v[u][q]: virtual
+// thread gtid + u * NT); every thread gets the totals.  The lanes of each
+// virtual warp (32 consecutive virtual threads, the lanes of one warp) are
+// summed first; then lane l of each CTA's warp 0 adds virtual warps
+// (l + l+32) + (l+64 + l+96) and the lanes are summed again, the same tree
+// for either cluster shape.  part: shared [2][3][VPT * ENS_WPC], tot:
+// shared [3]; ph alternates the two halves of part so one barrier per
+// reduction suffices.
 template <int CTAS, int K>
-__device__ __forceinline__ void cluster_sum(double (&v)[K], double* part, double* tot, int& ph,
+__device__ __forceinline__ void cluster_sum(double (&v)[EnsShape<CTAS>::VPT][K], double* part, double* tot, int& ph,
                                             cg::cluster_group& cluster) {
-  constexpr int WPC = RING_SLICES / CTAS;
+  constexpr int VPT = EnsShape<CTAS>::VPT, VW = VPT * ENS_WPC, WARPS = EnsShape<CTAS>::NT / 32;
+  static_assert(ENS_VT / 32 == 128, "the fixed tree adds 128 virtual warps");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int q = 0; q < K; ++q) {
-    double x = v[q];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) part[(ph * 3 + q) * WPC + w] = x;
-  }
+  for (int u = 0; u < VPT; ++u)
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      double x = v[u][q];
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) part[(ph * 3 + q) * VW + u * ENS_WPC + w] = x;
+    }
   cluster.sync();
   if (w == 0) {
 #pragma unroll
     for (int q = 0; q < K; ++q) {
-      // the 64 warps of the cluster in global order: lane l adds warps l and l + 32
-      const int g0 = lane, g1 = lane + 32;
-      const double* p0 = cluster.map_shared_rank(part + (ph * 3 + q) * WPC + g0 % WPC, g0 / WPC);
-      const double* p1 = cluster.map_shared_rank(part + (ph * 3 + q) * WPC + g1 % WPC, g1 / WPC);
-      double x = *p0 + *p1;
+      double y[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int vw = lane + 32 * j, u = vw / WARPS, rw = vw % WARPS;
+        y[j] = *cluster.map_shared_rank(part + (ph * 3 + q) * VW + u * ENS_WPC + rw % ENS_WPC, rw / ENS_WPC);
+      }
+      double x = (y[0] + y[1]) + (y[2] + y[3]);
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
       if (lane == 0) tot[q] = x;
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int q = 0; q < K; ++q) v[q] = tot[q];
+  for (int u = 0; u < VPT; ++u)
+#pragma unroll
+    for (int q = 0; q < K; ++q) v[u][q] = tot[q];
   ph ^= 1;
 }
 
@@ -117,9 +178,14 @@ __device__ __forceinline__ void cluster_sum(double (&v)[K], double* part, double
 // solver loop's, which keeps both free of spills.
 // (13 entries of a row in registers, as for the 27-point stencil; longer
 // rows read the rest from memory)
+// The schedule and vectors are copied into local variables first: through
+// the caller's references they would live in global memory, and every store
+// of the walk would force the compiler to load them again.
 template <int KIND, typename T, int CTAS>
 __device__ __noinline__ bool walk(const RingArgs& g, const RingVals<T>& a, unsigned char* smem) {
-  return ring_walk<KIND, T, 13, CTAS>(g, a, smem);
+  const RingArgs gl = g;
+  const RingVals<T> al = a;
+  return ring_walk<KIND, T, 13, CTAS, ENS_THREADS>(gl, al, smem);
 }
 
 // out = M^-1 in (ILU(0): L y = in, U out = y, FP64 factors) on the cluster;
@@ -138,14 +204,15 @@ __device__ __noinline__ bool ens_precond(const EnsMember& m, const double* in, d
 }
 
 template <int CTAS>
-__global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArgs e, size_t) {
+__global__ void __launch_bounds__(ENS_THREADS) k_ens_bicgstab(EnsArgs e, size_t) {
+  constexpr int VPT = EnsShape<CTAS>::VPT;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double part[2 * 3 * (RING_SLICES / CTAS)];
+  __shared__ double part[2 * 3 * VPT * ENS_WPC];
   __shared__ double tot[3];
   __shared__ int take;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
-  const int nt = CTAS * (int)blockDim.x, gtid = rank * (int)blockDim.x + (int)threadIdx.x;
+  const int gtid = rank * ENS_THREADS + (int)threadIdx.x;
   int ph = 0;
   for (;;) {
     if (rank == 0 && threadIdx.x == 0) take = *(volatile int*)e.abort ? e.count : atomicAdd(e.queue, 1);
@@ -153,7 +220,7 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArg
     const int mi = *cluster.map_shared_rank(&take, 0);
     cluster.sync();  // CTA 0 rewrites take only after every CTA has read it
     if (mi >= e.count) return;
-    const EnsMember& m = e.mem[mi];
+    const EnsMember m = e.mem[mi];  // a local copy: global stores do not force reloads
     const int n = m.n;
     double *r = m.w, *rt = m.w + (size_t)n, *p = m.w + 2 * (size_t)n, *v = m.w + 3 * (size_t)n;
     double *phat = m.w + 4 * (size_t)n, *s = m.w + 5 * (size_t)n, *shat = m.w + 6 * (size_t)n;
@@ -189,63 +256,61 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArg
     bool walked = true;
     {
       // r = b + (-1) A x, rtilde = r (unfused row sums, as A.multAdd)
-      double a2[2] = {0, 0};
-      for (int i = gtid; i < n; i += nt) {
-        const int base = m.sb[i >> 5] + (i & 31), len = m.rl[i];
-        double d = 0;
-        for (int k = 0; k < len; ++k) {
-          const int q = base + 32 * k;
-          d += m.val[q] * __ldcg(x + m.col[q]);
-        }
+      double a2[VPT][2] = {};
+      ens_rows<CTAS>(n, gtid, [&](int u, int i) {
+        const double d = ens_row<false>(m.val, m.col, x, m.sb[i >> 5] + (i & 31), m.rl[i]);
         const double ri = m.b[i] + -1.0 * d;
         r[i] = ri;
         rt[i] = ri;
-        a2[0] += ri * ri;
-        a2[1] += ri * ri;
-      }
+        a2[u][0] += ri * ri;
+        a2[u][1] += ri * ri;
+      });
       cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
-      top(a2[0], a2[1]);
+      top(a2[0][0], a2[0][1]);
     }
     while (status == KS_RUNNING) {
       // p = r + beta (p - omega v)
-      for (int i = gtid; i < n; i += nt) {
-        if (first) {
-          p[i] = r[i];
-          continue;
-        }
-        const double mo = -omega;
-        double temp = (mo == 0) ? 0.0 : mo * v[i];
-        temp += p[i];
-        p[i] = (beta == 0) ? r[i] : r[i] + beta * temp;
+      {
+        const double mo = -omega, bt = beta;
+        const bool fst = first;
+        ens_rows<CTAS>(n, gtid, [&](int, int i) {
+          if (fst) {
+            p[i] = r[i];
+            return;
+          }
+          double temp = (mo == 0) ? 0.0 : mo * v[i];
+          temp += p[i];
+          p[i] = (bt == 0) ? r[i] : r[i] + bt * temp;
+        });
       }
       if (!(walked = ens_precond<CTAS>(m, p, phat, smem, cluster))) break;
       {
         // v = A phat; alpha = rho_1 / (rtilde . v)
-        double a1[1] = {0};
-        for (int i = gtid; i < n; i += nt) {
-          const double d = sell_row_fma<false>(m.val, m.col, phat, m.sb[i >> 5] + (i & 31), m.rl[i]);
+        double a1[VPT][1] = {};
+        ens_rows<CTAS>(n, gtid, [&](int u, int i) {
+          const double d = ens_row<true>(m.val, m.col, (const double*)phat, m.sb[i >> 5] + (i & 31), m.rl[i]);
           const double yi = (d != 0) ? d : 0.0;
           v[i] = yi;
-          a1[0] = __fma_rn(rt[i], yi, a1[0]);
-        }
+          a1[u][0] = __fma_rn(rt[i], yi, a1[u][0]);
+        });
         cluster_sum<CTAS, 1>(a1, part, tot, ph, cluster);
-        alpha = rho_1 / a1[0];
+        alpha = rho_1 / a1[0][0];
       }
       {
         // s = r - alpha v; monitor |s|
-        double a1[1] = {0};
+        double a1[VPT][1] = {};
         const double ma = -alpha;
-        for (int i = gtid; i < n; i += nt) {
+        ens_rows<CTAS>(n, gtid, [&](int u, int i) {
           const double si = (ma == 0) ? r[i] : r[i] + ma * v[i];
           s[i] = si;
-          a1[0] += si * si;
-        }
+          a1[u][0] += si * si;
+        });
         cluster_sum<CTAS, 1>(a1, part, tot, ph, cluster);
-        const int mo = monitor(sqrt(a1[0]));
+        const int mo = monitor(sqrt(a1[0][0]));
         if (mo == 1) {
           // x.add(alpha, phat) and stop
-          if (alpha != 0)
-            for (int i = gtid; i < n; i += nt) x[i] += alpha * __ldcg(phat + i);
+          const double al = alpha;
+          if (al != 0) ens_rows<CTAS>(n, gtid, [&](int, int i) { x[i] += al * __ldcg(phat + i); });
           status = KS_CONVERGED;
           break;
         }
@@ -257,36 +322,36 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_bicgstab(EnsArg
       if (!(walked = ens_precond<CTAS>(m, s, shat, smem, cluster))) break;
       {
         // t = A shat; omega = (t . s) / (t . t)
-        double a2[2] = {0, 0};
-        for (int i = gtid; i < n; i += nt) {
-          const double d = sell_row_fma<false>(m.val, m.col, shat, m.sb[i >> 5] + (i & 31), m.rl[i]);
+        double a2[VPT][2] = {};
+        ens_rows<CTAS>(n, gtid, [&](int u, int i) {
+          const double d = ens_row<true>(m.val, m.col, (const double*)shat, m.sb[i >> 5] + (i & 31), m.rl[i]);
           const double yi = (d != 0) ? d : 0.0;
           t[i] = yi;
-          a2[0] = __fma_rn(yi, s[i], a2[0]);
-          a2[1] = __fma_rn(yi, yi, a2[1]);
-        }
+          a2[u][0] = __fma_rn(yi, s[i], a2[u][0]);
+          a2[u][1] = __fma_rn(yi, yi, a2[u][1]);
+        });
         cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
-        omega = a2[0] / a2[1];
+        omega = a2[0][0] / a2[0][1];
       }
       {
         // x += alpha phat + omega shat; r = s - omega t; reduce r.r, rtilde.r
-        double a2[2] = {0, 0};
-        const double mo = -omega;
-        for (int i = gtid; i < n; i += nt) {
+        double a2[VPT][2] = {};
+        const double al = alpha, om = omega, mo = -omega;
+        ens_rows<CTAS>(n, gtid, [&](int u, int i) {
           double xi = x[i];
-          if (alpha != 0) xi += alpha * __ldcg(phat + i);
-          if (omega != 0) xi += omega * __ldcg(shat + i);
+          if (al != 0) xi += al * __ldcg(phat + i);
+          if (om != 0) xi += om * __ldcg(shat + i);
           x[i] = xi;
           const double ri = (mo == 0) ? s[i] : s[i] + mo * t[i];
           r[i] = ri;
-          a2[0] += ri * ri;
-          a2[1] += rt[i] * ri;
-        }
+          a2[u][0] += ri * ri;
+          a2[u][1] += rt[i] * ri;
+        });
         cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
         rho_2 = rho_1;
         iter++;
         first = 0;
-        top(a2[0], a2[1]);
+        top(a2[0][0], a2[0][1]);
       }
     }
     if (!walked) {
@@ -351,26 +416,15 @@ __device__ __noinline__ bool ens_ilu_f32(const EnsMember& m, const float* in, fl
   return walk<SW_ILU_UPPER, float, CTAS>(m.gu, up, smem);
 }
 
-// y = A_f32 x (each product fused, as k_f32_spmv_dot) for the rows of this
-// thread; x was written earlier in the launch by other SMs (read from L2)
-__device__ __forceinline__ float sell_row_f32(const EnsMember& m, const float* x, int i) {
-  const int base = m.sb[i >> 5] + (i & 31), len = m.rl[i];
-  float d = 0;
-#pragma unroll 8
-  for (int k = 0; k < len; ++k) {
-    const int q = base + 32 * k;
-    d = fmaf(m.valf[q], __ldcg(x + m.col[q]), d);
-  }
-  return d;
-}
-
 // The FP32 inner BiCGstab from x = 0 on v (krylov.cu k_inner_reset,
 // k_f32_*): inner_iters steps at most, inner_rtol against its own initial
-// residual, no divergence test; z = its iterate.  Returns false when a walk
-// timed out.  Every thread ends with the same inner iteration count.
+// residual, no divergence test; z = its iterate.  Its SpMV fuses each
+// product (as k_f32_spmv_dot).  Returns false when a walk timed out.  Every
+// thread ends with the same inner iteration count.
 template <int CTAS>
 __device__ bool ens_inner(const EnsMember& m, const double* v, double* z, unsigned char* smem, double* part,
-                          double* tot, int& ph, int gtid, int nt, cg::cluster_group& cluster, int& inner_its) {
+                          double* tot, int& ph, int gtid, cg::cluster_group& cluster, int& inner_its) {
+  constexpr int VPT = EnsShape<CTAS>::VPT;
   const int n = m.n;
   float *ir = m.f, *irt = m.f + (size_t)n, *ip = m.f + 2 * (size_t)n, *iv = m.f + 3 * (size_t)n;
   float *iph = m.f + 4 * (size_t)n, *is = m.f + 5 * (size_t)n, *ish = m.f + 6 * (size_t)n;
@@ -398,100 +452,104 @@ __device__ bool ens_inner(const EnsMember& m, const double* v, double* z, unsign
     if (!first) beta = (rho_1 / rho_2) * (alpha / omega);
   };
   {
-    double a2[2] = {0, 0};
-    for (int i = gtid; i < n; i += nt) {
+    double a2[VPT][2] = {};
+    ens_rows<CTAS>(n, gtid, [&](int u, int i) {
       const float ri = (float)v[i];
       ir[i] = ri;
       irt[i] = ri;
       ix[i] = 0.f;
-      a2[0] += (double)ri * ri;
-      a2[1] += (double)ri * ri;
-    }
+      a2[u][0] += (double)ri * ri;
+      a2[u][1] += (double)ri * ri;
+    });
     cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
-    top(a2[0], a2[1]);
+    top(a2[0][0], a2[0][1]);
   }
   while (status == KS_RUNNING) {
-    for (int i = gtid; i < n; i += nt) {
-      if (first) {
-        ip[i] = ir[i];
-        continue;
-      }
+    {
       const float mo = (float)(-omega), bf = (float)beta;
-      const float temp = mo * iv[i] + ip[i];
-      ip[i] = ir[i] + bf * temp;
+      const bool fst = first;
+      ens_rows<CTAS>(n, gtid, [&](int, int i) {
+        if (fst) {
+          ip[i] = ir[i];
+          return;
+        }
+        const float temp = mo * iv[i] + ip[i];
+        ip[i] = ir[i] + bf * temp;
+      });
     }
     if (!ens_ilu_f32<CTAS>(m, ip, iy, iph, smem)) return false;
     {
-      double a1[1] = {0};
-      for (int i = gtid; i < n; i += nt) {
-        const float d = sell_row_f32(m, iph, i);
+      double a1[VPT][1] = {};
+      ens_rows<CTAS>(n, gtid, [&](int u, int i) {
+        const float d = ens_row<true>(m.valf, m.col, (const float*)iph, m.sb[i >> 5] + (i & 31), m.rl[i]);
         iv[i] = d;
-        a1[0] += (double)irt[i] * d;
-      }
+        a1[u][0] += (double)irt[i] * d;
+      });
       cluster_sum<CTAS, 1>(a1, part, tot, ph, cluster);
-      alpha = rho_1 / a1[0];
+      alpha = rho_1 / a1[0][0];
     }
     {
-      double a1[1] = {0};
+      double a1[VPT][1] = {};
       const float ma = (float)(-alpha);
-      for (int i = gtid; i < n; i += nt) {
+      ens_rows<CTAS>(n, gtid, [&](int u, int i) {
         const float si = ir[i] + ma * iv[i];
         is[i] = si;
-        a1[0] += (double)si * si;
-      }
+        a1[u][0] += (double)si * si;
+      });
       cluster_sum<CTAS, 1>(a1, part, tot, ph, cluster);
       // the inner s check keeps the initial residual (krylov.cu EPI_BICG_S_IN)
-      if (sqrt(a1[0]) < jmax2(m.inner_rtol * initR, 0.0)) {
+      if (sqrt(a1[0][0]) < jmax2(m.inner_rtol * initR, 0.0)) {
         const float af = (float)alpha;
-        for (int i = gtid; i < n; i += nt) ix[i] += af * __ldcg(iph + i);
+        ens_rows<CTAS>(n, gtid, [&](int, int i) { ix[i] += af * __ldcg(iph + i); });
         status = KS_CONVERGED;
         break;
       }
     }
     if (!ens_ilu_f32<CTAS>(m, is, iy, ish, smem)) return false;
     {
-      double a2[2] = {0, 0};
-      for (int i = gtid; i < n; i += nt) {
-        const float d = sell_row_f32(m, ish, i);
+      double a2[VPT][2] = {};
+      ens_rows<CTAS>(n, gtid, [&](int u, int i) {
+        const float d = ens_row<true>(m.valf, m.col, (const float*)ish, m.sb[i >> 5] + (i & 31), m.rl[i]);
         it[i] = d;
-        a2[0] += (double)d * is[i];
-        a2[1] += (double)d * d;
-      }
+        a2[u][0] += (double)d * is[i];
+        a2[u][1] += (double)d * d;
+      });
       cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
-      omega = a2[0] / a2[1];
+      omega = a2[0][0] / a2[0][1];
     }
     {
-      double a2[2] = {0, 0};
+      double a2[VPT][2] = {};
       const float af = (float)alpha, of = (float)omega;
-      for (int i = gtid; i < n; i += nt) {
+      ens_rows<CTAS>(n, gtid, [&](int u, int i) {
         ix[i] = ix[i] + af * __ldcg(iph + i) + of * __ldcg(ish + i);
         const float ri = is[i] - of * it[i];
         ir[i] = ri;
-        a2[0] += (double)ri * ri;
-        a2[1] += (double)irt[i] * ri;
-      }
+        a2[u][0] += (double)ri * ri;
+        a2[u][1] += (double)irt[i] * ri;
+      });
       cluster_sum<CTAS, 2>(a2, part, tot, ph, cluster);
       rho_2 = rho_1;
       iter++;
       first = 0;
-      top(a2[0], a2[1]);
+      top(a2[0][0], a2[0][1]);
     }
   }
-  for (int i = gtid; i < n; i += nt) z[i] = (double)ix[i];
+  ens_rows<CTAS>(n, gtid, [&](int, int i) { z[i] = (double)ix[i]; });
   inner_its += iter;
   return true;
 }
 
 template <int CTAS>
-__global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_fgmres(EnsArgs e, size_t ring_bytes) {
+__global__ void __launch_bounds__(ENS_THREADS) k_ens_fgmres(EnsArgs e, size_t ring_bytes) {
+  constexpr int VPT = EnsShape<CTAS>::VPT;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double part[2 * 3 * (RING_SLICES / CTAS)];
+  __shared__ double part[2 * 3 * VPT * ENS_WPC];
   __shared__ double tot[3];
   __shared__ int take;
   __shared__ GmShared g;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
-  const int nt = CTAS * (int)blockDim.x, gtid = rank * (int)blockDim.x + (int)threadIdx.x;
+  const int gtid = rank * ENS_THREADS + (int)threadIdx.x;
   const bool lead = threadIdx.x == 0;
   int ph = 0;
   for (;;) {
@@ -500,7 +558,7 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_fgmres(EnsArgs 
     const int mi = *cluster.map_shared_rank(&take, 0);
     cluster.sync();
     if (mi >= e.count) return;
-    const EnsMember& m = e.mem[mi];
+    const EnsMember m = e.mem[mi];  // a local copy: global stores do not force reloads
     const int n = m.n, mr = m.restart, ld = mr + 1;
     double* H = reinterpret_cast<double*>(smem + ring_bytes);  // (m + 1) x m, column major
     double *sv = H + (size_t)ld * mr, *gc = sv + ld, *gs = gc + ld;
@@ -517,26 +575,21 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_fgmres(EnsArgs 
     int inner = 0;
     for (;;) {
       // r = b - A x (A.multAdd order: unfused row sums); |r|
-      double a1[1] = {0};
-      for (int i = gtid; i < n; i += nt) {
-        const int base = m.sb[i >> 5] + (i & 31), len = m.rl[i];
-        double d = 0;
-        for (int k = 0; k < len; ++k) {
-          const int q = base + 32 * k;
-          d += m.val[q] * __ldcg(x + m.col[q]);
-        }
+      double a1[VPT][1] = {};
+      ens_rows<CTAS>(n, gtid, [&](int u, int i) {
+        const double d = ens_row<false>(m.val, m.col, (const double*)x, m.sb[i >> 5] + (i & 31), m.rl[i]);
         const double ri = m.b[i] + -1.0 * d;
         r[i] = ri;
-        a1[0] += ri * ri;
-      }
+        a1[u][0] += ri * ri;
+      });
       cluster_sum<CTAS, 1>(a1, part, tot, ph, cluster);
       if (lead) {
         // outer loop test, then the first inner test on |s_0| = |r|
-        int mo = gm_monitor(g, m, sqrt(a1[0]));
+        int mo = gm_monitor(g, m, sqrt(a1[0][0]));
         if (mo != 0) {
           g.status = mo;
         } else {
-          g.rho = sqrt(a1[0]);
+          g.rho = sqrt(a1[0][0]);
           g.vscale = 1 / g.rho;
           for (int q = 0; q <= mr; ++q) sv[q] = 0;
           sv[0] = g.rho;
@@ -551,46 +604,41 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_fgmres(EnsArgs 
       if (g.status != 0) break;
       {
         const double a = g.vscale;
-        for (int i = gtid; i < n; i += nt) V[i] = (a == 0) ? 0.0 : a * r[i];
+        ens_rows<CTAS>(n, gtid, [&](int, int i) { V[i] = (a == 0) ? 0.0 : a * r[i]; });
       }
       while (!g.gexit && g.status == 0) {
         const int i = g.gi;
         double* vi = V + (size_t)i * n;
         double* zi = Z + (size_t)i * n;
         // z_i = M(v_i): the inner walks start with a cluster barrier, which publishes v_i
-        if (!(walked = ens_inner<CTAS>(m, vi, zi, smem, part, tot, ph, gtid, nt, cluster, inner))) break;
+        if (!(walked = ens_inner<CTAS>(m, vi, zi, smem, part, tot, ph, gtid, cluster, inner))) break;
         cluster.sync();  // z_i complete before the SpMV gathers it
         // w = A z_i (mult: unfused row sums, exact zeros stored as +0)
-        for (int q = gtid; q < n; q += nt) {
-          const int base = m.sb[q >> 5] + (q & 31), len = m.rl[q];
-          double d = 0;
-          for (int k = 0; k < len; ++k) {
-            const int c = base + 32 * k;
-            d += m.val[c] * __ldcg(zi + m.col[c]);
-          }
+        ens_rows<CTAS>(n, gtid, [&](int, int q) {
+          const double d = ens_row<false>(m.val, m.col, (const double*)zi, m.sb[q >> 5] + (q & 31), m.rl[q]);
           w[q] = (d != 0) ? d : 0.0;
-        }
+        });
         // modified Gram-Schmidt (GMRES.java:146-162), one reduction per basis vector
         for (int k2 = 0; k2 <= i + 1; ++k2) {
           const double h = (k2 > 0) ? -H[(k2 - 1) + i * ld] : 0.0;
           const double* vprev = k2 > 0 ? V + (size_t)(k2 - 1) * n : nullptr;
           const double* vk = k2 <= i ? V + (size_t)k2 * n : nullptr;
-          double acc[1] = {0};
-          for (int q = gtid; q < n; q += nt) {
+          double acc[VPT][1] = {};
+          ens_rows<CTAS>(n, gtid, [&](int u, int q) {
             double we = w[q];
             if (k2 > 0 && h != 0) {
               we += h * vprev[q];
               w[q] = we;
             }
-            acc[0] += vk ? we * vk[q] : we * we;
-          }
+            acc[u][0] += vk ? we * vk[q] : we * we;
+          });
           cluster_sum<CTAS, 1>(acc, part, tot, ph, cluster);
           if (k2 <= i) {
-            if (lead) H[k2 + i * ld] = acc[0];
+            if (lead) H[k2 + i * ld] = acc[0][0];
             __syncthreads();
           } else if (lead) {
             // H(i+1,i) = |w|, rotations (krylov.cu EPI_GM_NORMW)
-            H[i + 1 + i * ld] = sqrt(acc[0]);
+            H[i + 1 + i * ld] = sqrt(acc[0][0]);
             g.vscale = 1. / H[i + 1 + i * ld];
             for (int q = 0; q < i; ++q) {
               const double a = H[q + i * ld], b = H[q + 1 + i * ld];
@@ -626,7 +674,7 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_fgmres(EnsArgs 
         {
           const double a = g.vscale;
           double* vn = V + (size_t)(i + 1) * n;
-          for (int q = gtid; q < n; q += nt) vn[q] = (a == 0) ? 0.0 : a * w[q];
+          ens_rows<CTAS>(n, gtid, [&](int, int q) { vn[q] = (a == 0) ? 0.0 : a * w[q]; });
         }
       }
       if (!walked || g.status != 0) break;
@@ -648,13 +696,16 @@ __global__ void __launch_bounds__(RING_SLICES / CTAS * 32) k_ens_fgmres(EnsArgs 
       }
       __syncthreads();
       if (g.status != 0) break;
-      for (int q = gtid; q < n; q += nt) {
-        double xe = x[q];
-        for (int j = 0; j < g.gi; ++j) {
-          const double sj = sv[j];
-          if (sj != 0) xe += sj * Z[(size_t)j * n + q];
-        }
-        x[q] = xe;
+      {
+        const int gi = g.gi;
+        ens_rows<CTAS>(n, gtid, [&](int, int q) {
+          double xe = x[q];
+          for (int j = 0; j < gi; ++j) {
+            const double sj = sv[j];
+            if (sj != 0) xe += sj * Z[(size_t)j * n + q];
+          }
+          x[q] = xe;
+        });
       }
       cluster.sync();  // x complete before the residual gathers it
       if (lead) g.iter++;
@@ -704,7 +755,7 @@ int ens_clusters(EnsDevice& D, int key, EnsKernel kern, int ctas) {
   if (ok) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ctas);
-    cfg.blockDim = dim3(RING_SLICES / ctas * 32);
+    cfg.blockDim = dim3(ENS_THREADS);
     cfg.dynamicSmemBytes = RING_SMEM_MAX;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -727,7 +778,7 @@ void ens_launch(EnsDevice& D, int count, int key, EnsKernel kern, int ctas, size
   const int nclusters = std::min(count, fit);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(ctas * nclusters);
-  cfg.blockDim = dim3(RING_SLICES / ctas * 32);
+  cfg.blockDim = dim3(ENS_THREADS);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = D.stream;
   cudaLaunchAttribute attr[1];
@@ -756,6 +807,11 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
   std::vector<EnsMember> h;
   int C = 0, R = 0, mr = 0;
   size_t nw = 0, nf = 0;
+  // 8-CTA clusters when planned: twice as many members in flight as with
+  // 16-CTA clusters (measured on 152 SMs: with 16-CTA clusters one to four
+  // members took the same time and eight took twice as long, so about six
+  // such clusters were resident at once)
+  const int prefer = 8;
   for (int i = 0; i < count; ++i) {
     const EnsSystem& q = sys[i];
     SolverView sv = solver_view(*q.solver);
@@ -768,7 +824,7 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
       status[i] = RSG_BAD_ARG;  // the solver must have been set up with this matrix
       continue;
     }
-    if (sv.method != RSG_BICGSTAB || sv.pc_kind != RSG_PC_ILU || !ilu_ring_plans(sv.pc, &L, &U) ||
+    if (sv.method != RSG_BICGSTAB || sv.pc_kind != RSG_PC_ILU || !ilu_ring_plans(sv.pc, prefer, &L, &U) ||
         (C != 0 && (L->C != C || U->C != C)) || (L->C != 8 && L->C != 16) || U->C != L->C) {
       status[i] = RSG_UNSUPPORTED;  // BiCGstab + ILU(0) with level-walk schedules for one cluster shape
       continue;
@@ -815,6 +871,21 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
   }
   const int nrun = (int)idx.size();
   if (nrun == 0) return;
+  // largest systems first: the clusters take members in this order, so the
+  // launch does not end waiting for a big member taken last
+  {
+    std::vector<int> ord(nrun);
+    for (int k = 0; k < nrun; ++k) ord[k] = k;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return h[a].n > h[b].n; });
+    std::vector<int> idx2(nrun);
+    std::vector<EnsMember> h2(nrun);
+    for (int k = 0; k < nrun; ++k) {
+      idx2[k] = idx[ord[k]];
+      h2[k] = h[ord[k]];
+    }
+    idx.swap(idx2);
+    h.swap(h2);
+  }
   // shared memory: the ring of the walks (FP64 or FP32 values), then for
   // FGMRES the Hessenberg matrix, right-hand side and rotations
   const size_t ring_bytes = precision ? ring_smem_bytes<float>(R) : ring_smem_bytes<double>(R);

@@ -53,7 +53,13 @@ struct SweepPlan {
   DeviceBuffer<double> diag;  // diagonal per slot row (upper sweeps)
   DeviceBuffer<float> diagf;
   int max_rows_per_level = 0;
-  RingPlan ring;              // ILU sweeps only
+  // ILU sweeps only: ring schedules for clusters of 16 CTAs (4 warps each)
+  // and of 8 CTAs (8 warps each); pick[0] / pick[1] is the one the walk
+  // autotuner chose for the FP64 / FP32 values (R == 0: no schedule)
+  RingPlan rings[2];
+  int pick[2] = {0, 0};
+  bool tuned = false;
+  const RingPlan& ring(int prec) const { return rings[pick[prec]]; }
 };
 
 constexpr int RING_SLICES = 64;
@@ -66,6 +72,7 @@ struct Csr {
   DeviceBuffer<double> val;
   // SELL-32 copy used by SpMV
   int nslices = 0;
+  int sell_wmax = 0;  // widest slice (entries per row slot)
   int64_t sell_size = 0;
   DeviceBuffer<int> slice_base, row_len, sell_col, sell_src;
   DeviceBuffer<double> sell_val;
@@ -155,8 +162,14 @@ struct EnsSystem {
 void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vector<rsg_solve_info>& info,
                     std::vector<int>& status);
 // the ring schedules and factor values of an ILU(0) preconditioner after its
-// setup (false for other preconditioners or patterns without ring schedules)
-bool ilu_ring_plans(Precond* p, const RingPlan** lower, const RingPlan** upper);
+// setup, for clusters of `prefer` CTAs when planned, else the other shape
+// (false for other preconditioners or patterns without ring schedules)
+bool ilu_ring_plans(Precond* p, int prefer, const RingPlan** lower, const RingPlan** upper);
+// walk autotuner of an ILU(0) preconditioner: force >= 0 sets the cluster
+// shape (0: timed choice, 16 or 8 CTAs), applied at the next setup; shapes
+// (when given) receives the clusters in use: FP64 lower, upper, FP32 lower,
+// upper (0: no ring schedule).  false for other preconditioners.
+bool ilu_walk_shape(Precond* p, int force, int* shapes);
 // the solver no longer refers to the matrix of its last setup (rsg_solver_setup is needed again)
 void solver_forget_matrix(Solver& s);
 

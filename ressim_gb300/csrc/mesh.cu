@@ -959,6 +959,39 @@ __global__ void k_potential_rows(int nel, const int* __restrict__ cc, const int*
   }
 }
 
+// flux[c] = sum_k t_k p[el_k] over connection c's MD list, in list order
+// (PotentialCalculator.calculateFlux, numerics/PotentialCalculator.java:265-280;
+// LocalFlowRateAverage.computeDarcyFlux, upscale/LocalFlowRateAverage.java:123-137).
+__global__ void k_connection_flux(int nconn, const int* __restrict__ md_ptr, const int* __restrict__ md_el,
+                                  const double* __restrict__ md_k, const double* __restrict__ p, double* flux) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nconn) return;
+  double f = 0;
+  for (int q = md_ptr[c]; q < md_ptr[c + 1]; ++q) f += md_k[q] * p[md_el[q]];
+  flux[c] = f;
+}
+
+// Centre of each connection's here interface (the here element's face that
+// points to the there element): Connection.hereInterface().center.
+__global__ void k_connection_icenter(Grid g, const int* __restrict__ conn, const double* __restrict__ icenter,
+                                     double* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nconn) return;
+  const int ei = conn[2 * c], ej = conn[2 * c + 1];
+  int i, j, k;
+  el_ijk(g, ei, i, j, k);
+  const int nfe = g.dim == 3 ? 6 : 4;
+  int o = 1;
+  for (int q = 0; q < nfe; ++q) {
+    int ne, no;
+    if (face_neighbour(g, i, j, k, q, ne, no) && ne == ej) {
+      o = q;
+      break;
+    }
+  }
+  for (int a = 0; a < 3; ++a) out[3 * (int64_t)c + a] = icenter[3 * ((int64_t)ei * nfe + o) + a];
+}
+
 }  // namespace
 
 static void make_grid(Grid& g, int dim, int ni, int nj, int nk) {
@@ -1237,6 +1270,69 @@ rsg_status rsg_mesh_get_pattern(rsg_mesh* mh, int32_t which, int32_t* row_ptr, i
   if (row_ptr) std::copy(r.begin(), r.end(), row_ptr);
   if (col) std::copy(c.begin(), c.end(), col);
   return RSG_OK;
+}
+
+rsg_status rsg_mesh_connection_flux(rsg_mesh* mh, const double* p, double* flux) {
+  if (!mh || !p || !flux) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  if (!m.have_md) return RSG_BAD_ARG;
+  return guarded(m.ctx, [&] {
+    rsg::DeviceBuffer<double> dp(m.g.nel), df(std::max(m.g.nconn, 1));
+    RSG_CUDA(cudaMemcpyAsync(dp.get(), p, sizeof(double) * m.g.nel, cudaMemcpyHostToDevice, m.ctx->stream));
+    if (m.g.nconn > 0)
+      RSG_LAUNCH(*m.ctx, "connection_flux", rsg::k_connection_flux, rsg::blocks_for(m.g.nconn, 256), 256, 0,
+                 m.g.nconn, m.md_ptr.get(), m.md_elem.get(), m.md_k.get(), (const double*)dp.get(), df.get());
+    RSG_CUDA(cudaMemcpyAsync(flux, df.get(), sizeof(double) * m.g.nconn, cudaMemcpyDeviceToHost, m.ctx->stream));
+    m.ctx->sync();
+  });
+}
+
+rsg_status rsg_mesh_get_interface_centers(rsg_mesh* mh, double* centers) {
+  if (!mh || !centers) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  return guarded(m.ctx, [&] {
+    rsg::DeviceBuffer<double> d((size_t)3 * std::max(m.g.nconn, 1));
+    if (m.g.nconn > 0)
+      RSG_LAUNCH(*m.ctx, "connection_icenter", rsg::k_connection_icenter, rsg::blocks_for(m.g.nconn, 256), 256, 0,
+                 m.g, m.conn.get(), m.icenter.get(), d.get());
+    RSG_CUDA(cudaMemcpyAsync(centers, d.get(), sizeof(double) * 3 * m.g.nconn, cudaMemcpyDeviceToHost,
+                             m.ctx->stream));
+    m.ctx->sync();
+  });
+}
+
+rsg_status rsg_upscale_pressure(rsg_mesh* mh, int32_t nbc, const int32_t* cells, const double* values, double* x,
+                                rsg_solve_info* info) {
+  if (!mh || !x || nbc < 0 || (nbc > 0 && (!cells || !values))) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  if (!m.have_md) return RSG_BAD_ARG;
+  const int n = m.g.nel;
+  for (int q = 0; q < nbc; ++q)
+    if (cells[q] < 0 || cells[q] >= n) return RSG_BAD_ARG;
+  // the matrix and the solver of PressureDiscretisation(mesh, bc)
+  // (PressureDiscretisation.java:59-87): pattern without the explicit
+  // diagonal, GMRES(30) + ILU(0), DefaultIterationMonitor with
+  // maxIterations 10000, rtol 1e-50, atol 1e-10, dtol 1e5, x = 0
+  rsg_csr A;
+  rsg_solver S;
+  rsg_status st = guarded(m.ctx, [&] {
+    A.m.build(m.ctx, n, (int32_t)m.h_qcol.size(), m.h_qrow.data(), m.h_qcol.data());
+    S.s = rsg::make_solver(m.ctx, RSG_GMRES, RSG_PC_ILU, 1e-50, 1e-10, 1e5, 10000, 30);
+  });
+  // assemble(): A(here,k) += t_k, A(there,k) -= t_k; then for each boundary
+  // cell b_i = p_i and row i := e_i (Matrices.zeroRows(A, 1.0, {i}))
+  if (st == RSG_OK) st = rsg_mesh_assemble_potential(mh, &A);
+  if (st == RSG_OK && nbc > 0) st = rsg_csr_zero_rows(&A, 1.0, nbc, cells);
+  if (st == RSG_OK) st = rsg_solver_setup(&S, &A);
+  if (st == RSG_OK) {
+    std::vector<double> b(n, 0.0);
+    for (int q = 0; q < nbc; ++q) b[cells[q]] = values[q];
+    std::fill(x, x + n, 0.0);
+    rsg_solve_info local{};
+    st = rsg_solver_solve(&S, &A, b.data(), x, info ? info : &local);
+  }
+  cudaStreamSynchronize(m.ctx->stream);
+  return st;
 }
 
 rsg_status rsg_mesh_assemble_potential(rsg_mesh* mh, rsg_csr* A) {

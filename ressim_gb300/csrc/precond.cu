@@ -207,8 +207,9 @@ __global__ void __launch_bounds__(256) k_sweep_pipelined(SweepArgs<T> a) {
   }
 }
 
-// RSG_SWEEP=pipelined switches the ring walks off; RSG_RING_CTAS=8 plans
-// them for clusters of 8 CTAs with 8 warps each instead of 16 with 4.
+// RSG_SWEEP=pipelined switches the ring walks off; RSG_RING_CTAS=8 or 16
+// plans them for that cluster shape only (8 CTAs of 8 warps, 16 of 4);
+// otherwise both are planned and the walk autotuner picks.
 static bool ring_enabled() {
   static const bool on = [] {
     const char* e = getenv("RSG_SWEEP");
@@ -220,7 +221,7 @@ static bool ring_enabled() {
 static int ring_ctas() {
   static const int c = [] {
     const char* e = getenv("RSG_RING_CTAS");
-    return (e && atoi(e) == 8) ? 8 : 16;
+    return e ? (atoi(e) == 8 ? 8 : (atoi(e) == 16 ? 16 : 0)) : 0;
   }();
   return c;
 }
@@ -667,9 +668,15 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
         src[base[s] + 32 * k + lane] = q;
       }
     }
-  // push-ring schedule (lower or upper ILU parts only)
-  HostRing H;
-  const bool ring = entries != 2 && plan_ring(n, rp, cl, dg, upper_levels, entries, ring_ctas(), RING_SMEM_MAX, H);
+  // push-ring schedules (lower or upper ILU parts only), for both cluster
+  // shapes unless RSG_RING_CTAS fixes one
+  HostRing H[2];
+  bool ring[2] = {false, false};
+  for (int v = 0; v < 2; ++v) {
+    const int C = v == 0 ? 16 : 8;
+    if (ring_ctas() != 0 && ring_ctas() != C) continue;
+    ring[v] = entries != 2 && plan_ring(n, rp, cl, dg, upper_levels, entries, C, RING_SMEM_MAX, H[v]);
+  }
   Context& ctx = *A.ctx;
   P.nlev = nlev;
   P.nslices = ns;
@@ -691,39 +698,44 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
   up(P.len, len);
   up(P.col, col);
   up(P.src, src);
-  RingPlan& G = P.ring;
-  G.R = 0;
-  if (ring) {
-    G.C = H.C;
-    G.nlev = H.nlev;
-    G.R = H.R;
-    G.slack = H.slack;
-    G.maxlen = H.maxlen;
-    G.slice_base.resize(H.slice_base.size());
-    G.row.resize(H.row.size());
-    G.len.resize(H.len.size());
-    G.ridx.resize(H.ridx.size());
-    G.src.resize(H.src.size());
-    G.pmask.resize(H.pmask.size());
-    G.expect.resize(H.expect.size());
-    G.nbr.resize(H.nbr.size());
-    G.val.resize(H.src.size());
-    G.valf.resize(H.src.size());
-    up(G.slice_base, H.slice_base);
-    up(G.row, H.row);
-    up(G.len, H.len);
-    up(G.ridx, H.ridx);
-    up(G.src, H.src);
-    up(G.pmask, H.pmask);
-    up(G.expect, H.expect);
-    up(G.nbr, H.nbr);
+  for (int v = 0; v < 2; ++v) {
+    RingPlan& G = P.rings[v];
+    G.R = 0;
+    if (!ring[v]) continue;
+    const HostRing& Hv = H[v];
+    G.C = Hv.C;
+    G.nlev = Hv.nlev;
+    G.R = Hv.R;
+    G.slack = Hv.slack;
+    G.maxlen = Hv.maxlen;
+    G.slice_base.resize(Hv.slice_base.size());
+    G.row.resize(Hv.row.size());
+    G.len.resize(Hv.len.size());
+    G.ridx.resize(Hv.ridx.size());
+    G.src.resize(Hv.src.size());
+    G.pmask.resize(Hv.pmask.size());
+    G.expect.resize(Hv.expect.size());
+    G.nbr.resize(Hv.nbr.size());
+    G.val.resize(Hv.src.size());
+    G.valf.resize(Hv.src.size());
+    up(G.slice_base, Hv.slice_base);
+    up(G.row, Hv.row);
+    up(G.len, Hv.len);
+    up(G.ridx, Hv.ridx);
+    up(G.src, Hv.src);
+    up(G.pmask, Hv.pmask);
+    up(G.expect, Hv.expect);
+    up(G.nbr, Hv.nbr);
     if (with_diag) {
-      G.diag_src.resize(H.diag_src.size());
-      G.diag.resize(H.diag_src.size());
-      G.diagf.resize(H.diag_src.size());
-      up(G.diag_src, H.diag_src);
+      G.diag_src.resize(Hv.diag_src.size());
+      G.diag.resize(Hv.diag_src.size());
+      G.diagf.resize(Hv.diag_src.size());
+      up(G.diag_src, Hv.diag_src);
     }
   }
+  // until the autotuner has timed them: 16 CTAs where that schedule exists
+  P.pick[0] = P.pick[1] = P.rings[0].R ? 0 : 1;
+  P.tuned = false;
   if (with_diag) {
     P.diag_src.resize(dsrc.size());
     P.diag.resize(dsrc.size());
@@ -731,6 +743,12 @@ static void build_plan(Csr& A, SweepPlan& P, bool upper_levels, int entries, boo
     up(P.diag_src, dsrc);
   }
   ctx.sync();
+}
+
+template <typename T>
+__global__ void k_fill_one(int n, T* x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = T(1);
 }
 
 static void plan_values(Context& ctx, SweepPlan& P, const double* csr_vals, bool with_diag, bool f32) {
@@ -748,8 +766,8 @@ static void plan_values(Context& ctx, SweepPlan& P, const double* csr_vals, bool
       RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<float>, blocks_for(ds, 256), 256, 0, ds, P.diag_src.get(),
                  csr_vals, P.diagf.get());
   }
-  RingPlan& G = P.ring;
-  if (!G.R) return;
+  for (RingPlan& G : P.rings) {
+  if (!G.R) continue;
   const int64_t gs = (int64_t)G.src.size();
   RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<double>, blocks_for(gs, 256), 256, 0, gs, G.src.get(), csr_vals,
              G.val.get());
@@ -764,6 +782,7 @@ static void plan_values(Context& ctx, SweepPlan& P, const double* csr_vals, bool
       RSG_LAUNCH(ctx, "plan_gather", k_plan_gather<float>, blocks_for(ds, 256), 256, 0, ds, G.diag_src.get(),
                  csr_vals, G.diagf.get());
   }
+}
 }
 
 // Cluster launch of a level walk; falls back to one launch per level when
@@ -895,17 +914,18 @@ struct RingPick<float> {
 template <int KIND, typename T>
 static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, const T* val, const T* diag, const T* b,
                         T* x, const int* active) {
-  if (!ring_enabled() || !P.ring.R) return false;
-  const size_t smem = ring_smem_bytes<T>(P.ring.R);
+  const RingPlan& G = P.ring(sizeof(T) == 4 ? 1 : 0);
+  if (!ring_enabled() || !G.R) return false;
+  const size_t smem = ring_smem_bytes<T>(G.R);
   if (smem > RING_SMEM_MAX) return false;
   const RingVals<T> a{val, diag, b, x, active};
-  const bool narrow = P.ring.maxlen <= 13;
-  if (P.ring.C == 16)
-    return narrow ? launch_ring_n<KIND, T, 16, 13>(ctx, name, P.ring, a, smem)
-                  : launch_ring_n<KIND, T, 16, 16>(ctx, name, P.ring, a, smem);
-  if (P.ring.C == 8)
-    return narrow ? launch_ring_n<KIND, T, 8, 13>(ctx, name, P.ring, a, smem)
-                  : launch_ring_n<KIND, T, 8, 16>(ctx, name, P.ring, a, smem);
+  const bool narrow = G.maxlen <= 13;
+  if (G.C == 16)
+    return narrow ? launch_ring_n<KIND, T, 16, 13>(ctx, name, G, a, smem)
+                  : launch_ring_n<KIND, T, 16, 16>(ctx, name, G, a, smem);
+  if (G.C == 8)
+    return narrow ? launch_ring_n<KIND, T, 8, 13>(ctx, name, G, a, smem)
+                  : launch_ring_n<KIND, T, 8, 16>(ctx, name, G, a, smem);
   return false;
 }
 
@@ -915,8 +935,9 @@ static void run_sweep(Context& ctx, const char* name, const SweepPlan& P, const 
   SweepArgs<T> a{P.nlev, P.level_slices.get(), P.slice_base.get(), P.row.get(), P.len.get(), P.col.get(), val, diag,
                  b, x, xx, omega, active};
   if constexpr (KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER) {
-    const bool ring = launch_ring<KIND, T>(ctx, name, P, RingPick<T>::val(P.ring),
-                                           KIND == SW_ILU_UPPER ? RingPick<T>::diag(P.ring) : nullptr, b, x, active);
+    const RingPlan& G = P.ring(sizeof(T) == 4 ? 1 : 0);
+    const bool ring = launch_ring<KIND, T>(ctx, name, P, RingPick<T>::val(G),
+                                           KIND == SW_ILU_UPPER ? RingPick<T>::diag(G) : nullptr, b, x, active);
     if (ring) return;
   }
   if ((KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER) && P.nlev <= SWEEP_MAX_LEVELS) {
@@ -1030,6 +1051,72 @@ struct ILUPrecond : Precond {
     if (h) throw Error(RSG_ZERO_PIVOT, "Zero pivot encountered on row " + std::to_string(h));
     plan_values(*ctx, Lp, LU.get(), false, true);
     plan_values(*ctx, Up, LU.get(), true, true);
+    if (!Lp.tuned || !Up.tuned) tune_walks();
+  }
+
+  // Walk autotuner: the first setup on a pattern times each sweep's ring
+  // schedules (16 CTAs of 4 warps, 8 CTAs of 8 warps) on the factor values,
+  // for the FP64 and the FP32 walks, and keeps the faster per sweep and
+  // precision.  Every schedule sums each row in CSR order, so the choice
+  // never changes a result bit.  force_ctas (rsg_solver_set_walk_shape)
+  // replaces the timing by a fixed shape.
+  int force_ctas = 0;
+  void tune_walks() {
+    const int n = A->n;
+    DeviceBuffer<double> bd(n), xd(n);
+    DeviceBuffer<float> bf(n), xf(n);
+    RSG_LAUNCH(*ctx, "tune_fill", k_fill_one<double>, blocks_for(n, 256), 256, 0, n, bd.get());
+    RSG_LAUNCH(*ctx, "tune_fill", k_fill_one<float>, blocks_for(n, 256), 256, 0, n, bf.get());
+    cudaEvent_t e0, e1;
+    RSG_CUDA(cudaEventCreate(&e0));
+    RSG_CUDA(cudaEventCreate(&e1));
+    auto time_ms = [&](auto&& run) {
+      run();  // warm-up
+      RSG_CUDA(cudaEventRecord(e0, ctx->stream));
+      for (int r = 0; r < 3; ++r) run();
+      RSG_CUDA(cudaEventRecord(e1, ctx->stream));
+      RSG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      RSG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms;
+    };
+    for (SweepPlan* P : {&Lp, &Up}) {
+      const bool lower = P == &Lp;
+      for (int prec = 0; prec < 2; ++prec) {
+        int best = P->pick[prec];
+        float best_ms = 1e30f;
+        for (int v = 0; v < 2; ++v) {
+          if (!P->rings[v].R) continue;
+          if (force_ctas && P->rings[v].C != force_ctas) continue;
+          P->pick[prec] = v;
+          float ms;
+          if (prec == 0) {
+            ms = time_ms([&] {
+              if (lower) run_sweep<SW_ILU_LOWER, double>(*ctx, "ilu_tune", Lp, Lp.val.get(), nullptr, bd.get(),
+                                                          xd.get(), nullptr, 0.0, nullptr);
+              else run_sweep<SW_ILU_UPPER, double>(*ctx, "ilu_tune", Up, Up.val.get(), Up.diag.get(), bd.get(),
+                                                   xd.get(), nullptr, 0.0, nullptr);
+            });
+          } else {
+            ms = time_ms([&] {
+              if (lower) run_sweep<SW_ILU_LOWER, float>(*ctx, "ilu_tune", Lp, Lp.valf.get(), nullptr, bf.get(),
+                                                         xf.get(), nullptr, 0.0f, nullptr);
+              else run_sweep<SW_ILU_UPPER, float>(*ctx, "ilu_tune", Up, Up.valf.get(), Up.diagf.get(), bf.get(),
+                                                  xf.get(), nullptr, 0.0f, nullptr);
+            });
+          }
+          if (ms < best_ms) {
+            best_ms = ms;
+            best = v;
+          }
+        }
+        P->pick[prec] = best;
+      }
+      P->tuned = true;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->check_device_error();
   }
 
   void apply(const double* b, double* x, const int* active) override {
@@ -1208,12 +1295,35 @@ std::unique_ptr<Precond> make_precond(Context* ctx, int kind) {
   throw Error(RSG_UNSUPPORTED, "preconditioner not implemented");
 }
 
-bool ilu_ring_plans(Precond* p, const RingPlan** lower, const RingPlan** upper) {
+bool ilu_walk_shape(Precond* p, int force, int* shapes) {
   auto* ilu = dynamic_cast<ILUPrecond*>(p);
-  if (!ilu || !ilu->A || !ilu->Lp.ring.R || !ilu->Up.ring.R) return false;
-  *lower = &ilu->Lp.ring;
-  *upper = &ilu->Up.ring;
+  if (!ilu) return false;
+  if (force >= 0) {
+    ilu->force_ctas = force;
+    ilu->Lp.tuned = ilu->Up.tuned = false;  // the next setup re-tunes
+  }
+  if (shapes) {
+    const SweepPlan* P[2] = {&ilu->Lp, &ilu->Up};
+    for (int prec = 0; prec < 2; ++prec)
+      for (int s = 0; s < 2; ++s) {
+        const RingPlan& G = P[s]->ring(prec);
+        shapes[prec * 2 + s] = G.R ? G.C : 0;
+      }
+  }
   return true;
+}
+
+bool ilu_ring_plans(Precond* p, int prefer, const RingPlan** lower, const RingPlan** upper) {
+  auto* ilu = dynamic_cast<ILUPrecond*>(p);
+  if (!ilu || !ilu->A) return false;
+  for (int pass = 0; pass < 2; ++pass)
+    for (int v = 0; v < 2; ++v)
+      if (ilu->Lp.rings[v].R && ilu->Up.rings[v].R && (pass == 1 || ilu->Lp.rings[v].C == prefer)) {
+        *lower = &ilu->Lp.rings[v];
+        *upper = &ilu->Up.rings[v];
+        return true;
+      }
+  return false;
 }
 
 void set_ssor_params(Precond* p, double wf, double wr, int reverse) {

@@ -194,26 +194,34 @@ __device__ __forceinline__ void ring_coeffs(const RingArgs& g, const RingVals<T>
     }
 }
 
-// One walk of the levels by the calling cluster (all its threads call it,
-// with blockDim.x == RING_SLICES / RING_CTAS * 32).  smem: the dynamic
-// shared memory, at least ring_smem_bytes<T>(g.R).  Returns false when a
-// wait ran out (g.err is set); the caller must then stop using the cluster's
-// shared memory for walks.  On success every mbarrier is invalidated again,
-// so the same memory can hold the next walk.
-template <int KIND, typename T, int MAXW, int RING_CTAS>
-__device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& a, unsigned char* smem) {
+// OR of pred over the first NT threads of the CTA (named barrier ID; the
+// other threads do not take part).
+template <int ID, int NT>
+__device__ __forceinline__ int bar_red_or(int pred) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.s32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, %2, %3, p;\n\t"
+      "selp.s32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"(pred), "n"(ID), "n"(NT)
+      : "memory");
+  return r;
+}
+
+// The level loop of ring_walk, run by the walking warps only (the first
+// RING_SLICES / RING_CTAS warps of each CTA; their barrier is the CTA barrier
+// when they are the whole CTA, else named barrier 1).  Ends when everything
+// owed to this CTA has landed; false when a wait ran out (g.err is set).
+template <int KIND, typename T, int MAXW, int RING_CTAS, int CTA_THREADS>
+__device__ __forceinline__ bool ring_levels(const RingArgs& g, const RingVals<T>& a, T* ring, unsigned ring0,
+                                            unsigned bar0, unsigned tok0, unsigned rank) {
   constexpr int RING_WARPS = RING_SLICES / RING_CTAS;
-  T* ring = reinterpret_cast<T*>(smem);
-  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + sizeof(T) * (size_t)g.R * RING_SLOT);
-  unsigned long long* tok = bar + g.R;
-  cg::cluster_group cluster = cg::this_cluster();
-  const unsigned rank = cluster.block_rank();
+  constexpr int WALK_THREADS = RING_WARPS * 32;
   const int lane = threadIdx.x & 31;
   const int gwarp = (int)rank * RING_WARPS + (threadIdx.x >> 5);
-  const unsigned ring0 = smem_addr(ring), bar0 = smem_addr(bar), tok0 = smem_addr(tok);
-  if (threadIdx.x < g.R) mbar_init(bar0 + 8 * threadIdx.x, 1);
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  cluster.sync();  // every replica's barriers exist before the first push
+  bool ok = true;
   const unsigned nbr = g.nbr[rank];
   const unsigned token_tx = RING_TOKEN_BYTES * __popc(nbr);
   RingRow<T, MAXW> cur, nxt;
@@ -224,7 +232,6 @@ __device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& 
   }
   int exp_cur = (threadIdx.x == 0 && g.nlev > 0) ? g.expect[rank] : 0;
   int slot_l = 0, par_l = 0, slot_p = 0, par_p = 0;  // level l and level l-1
-  bool ok = true;
   for (int l = 0; l < g.nlev; ++l) {
     if (threadIdx.x == 0) mbar_arm(bar0 + 8 * slot_l, (unsigned)(exp_cur * sizeof(T)) + (l >= g.slack ? token_tx : 0u));
     const int exp_nxt = (threadIdx.x == 0 && l + 1 < g.nlev) ? g.expect[(l + 1) * RING_CTAS + rank] : 0;
@@ -234,7 +241,10 @@ __device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& 
     // releases the others (fewer instructions in flight than every thread
     // polling the mbarrier)
     const int late = (l > 0 && threadIdx.x == 0) ? !mbar_wait(bar0 + 8 * slot_p, par_p) : 0;
-    if (__syncthreads_or(late)) {
+    int any_late;
+    if constexpr (CTA_THREADS == WALK_THREADS) any_late = __syncthreads_or(late);
+    else any_late = bar_red_or<1, WALK_THREADS>(late);
+    if (any_late) {
       if (threadIdx.x == 0) atomicCAS(g.err, 0, 1 + l);
       ok = false;
       break;
@@ -293,6 +303,35 @@ __device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& 
       ok = false;
     }
   }
+  return ok;
+}
+
+// One walk of the levels by the calling cluster (all its threads call it,
+// with blockDim.x == CTA_THREADS).  The first RING_SLICES / RING_CTAS warps
+// of each CTA walk; further warps (a persistent kernel that wants more warps
+// for its other phases) only take part in the cluster barriers at the start
+// and the end.  smem: the dynamic shared memory, at least
+// ring_smem_bytes<T>(g.R).  Returns false when a wait ran out (g.err is
+// set); the caller must then stop using the cluster's shared memory for
+// walks.  On success every mbarrier is invalidated again, so the same memory
+// can hold the next walk.
+template <int KIND, typename T, int MAXW, int RING_CTAS, int CTA_THREADS = RING_SLICES / RING_CTAS * 32>
+__device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& a, unsigned char* smem) {
+  constexpr int RING_WARPS = RING_SLICES / RING_CTAS;
+  constexpr int WALK_THREADS = RING_WARPS * 32;
+  static_assert(CTA_THREADS >= WALK_THREADS && CTA_THREADS % 32 == 0, "the walk needs its warps");
+  T* ring = reinterpret_cast<T*>(smem);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + sizeof(T) * (size_t)g.R * RING_SLOT);
+  unsigned long long* tok = bar + g.R;
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned rank = cluster.block_rank();
+  const unsigned ring0 = smem_addr(ring), bar0 = smem_addr(bar), tok0 = smem_addr(tok);
+  if (threadIdx.x < g.R) mbar_init(bar0 + 8 * threadIdx.x, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  cluster.sync();  // every replica's barriers exist before the first push
+  bool ok = true;
+  if (CTA_THREADS == WALK_THREADS || threadIdx.x < WALK_THREADS)
+    ok = ring_levels<KIND, T, MAXW, RING_CTAS, CTA_THREADS>(g, a, ring, ring0, bar0, tok0, rank);
   cluster.sync();
   if (*(volatile int*)g.err != 0) {
     // a wait ran out somewhere: give pushes still in flight time to land

@@ -20,6 +20,8 @@
 #include <cmath>
 
 #include "dual.cuh"
+#include <cudaTypedefs.h>
+
 #include "mesh.cuh"
 
 namespace rsg {
@@ -202,7 +204,7 @@ __device__ S mole_fraction(const S* N, int nc, int nu) {
 
 // Flags raised by the property chain (first one wins)
 enum { FL_NONE = 0, FL_DRDP = 1, FL_DENSITY = 2, FL_WATER_DERIV = 3, FL_BLACKOIL_CHECK = 4, FL_ENTHALPY = 5, FL_PATTERN = 6,
-       FL_NO_WATER = 7, FL_CUBIC = 16 };  // FL_CUBIC + CUBIC_* code
+       FL_NO_WATER = 7, FL_TMA = 8, FL_CUBIC = 16 };  // FL_CUBIC + CUBIC_* code
 
 // S = double for the simulator; a dual number for the adjoint's local derivatives
 template <class S>
@@ -651,6 +653,123 @@ __global__ void k_flux_conn(SimDev d, ConnDev c, double* Jh, double* Jt, double*
   }
   rh[q] = ri;
   rt[q] = rj;
+}
+
+// The same assembly with each block's interaction-region stencils (the MD
+// lists of its 128 connections: element indices and transmissibilities,
+// contiguous in memory) staged into shared memory by TMA: one thread arms an
+// mbarrier and issues 1D tensor copies of 256 entries (cp.async.bulk.tensor,
+// box 256, x aligned to 16 bytes, the part past the array filled with
+// zeros); the block's Jacobian contributions are written back from shared
+// memory with coalesced stores.  Arithmetic and order as k_flux_conn, so the
+// results are identical.
+constexpr int FLUX_BLOCK = 128;
+constexpr int TMA_BOX = 256;
+
+__device__ __forceinline__ void tma_load_1d(unsigned dst, const CUtensorMap* map, int x, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.1d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2}], [%3];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ bool tma_wait(unsigned bar, unsigned parity) {
+  for (int i = 0; i < (1 << 22); ++i) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(FLUX_BLOCK) k_flux_conn_tma(SimDev d, ConnDev c, double* Jh, double* Jt, double* rh,
+                                                             double* rt, const __grid_constant__ CUtensorMap tm_el,
+                                                             const __grid_constant__ CUtensorMap tm_k, int chunks) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ __align__(8) unsigned long long bar;
+  int* s_el = reinterpret_cast<int*>(sm);
+  double* s_k = reinterpret_cast<double*>(sm + (size_t)chunks * TMA_BOX * sizeof(int));
+  double* s_jh = s_k + (size_t)chunks * TMA_BOX;
+  double* s_jt = s_jh + (size_t)chunks * TMA_BOX;
+  const int q0 = blockIdx.x * FLUX_BLOCK, q1 = min(q0 + FLUX_BLOCK, d.nconn);
+  const int m0 = c.md_ptr[q0], m1 = c.md_ptr[q1];
+  const int e0 = m0 & ~3, k0 = m0 & ~1;  // 16-byte aligned starts
+  const int ce = (m1 - e0 + TMA_BOX - 1) / TMA_BOX, ck = (m1 - k0 + TMA_BOX - 1) / TMA_BOX;
+  const unsigned b = (unsigned)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    // the barrier's initialisation is visible to the tensor copies
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b),
+                 "r"((unsigned)(ce * TMA_BOX * sizeof(int) + ck * TMA_BOX * sizeof(double)))
+                 : "memory");
+    for (int q = 0; q < ce; ++q)
+      tma_load_1d((unsigned)__cvta_generic_to_shared(s_el + q * TMA_BOX), &tm_el, e0 + q * TMA_BOX, b);
+    for (int q = 0; q < ck; ++q)
+      tma_load_1d((unsigned)__cvta_generic_to_shared(s_k + q * TMA_BOX), &tm_k, k0 + q * TMA_BOX, b);
+  }
+  __syncthreads();
+  if (!__syncthreads_and(tma_wait(b, 0))) {
+    // the copies did not land in time: give them time to end, report, stop
+    if (threadIdx.x == 0) {
+      tma_wait(b, 0);
+      atomicCAS(d.flag, 0, FL_TMA);
+    }
+    return;
+  }
+  const int q = q0 + threadIdx.x;
+  if (q < q1) {
+    const int i = c.conn[2 * q], j = c.conn[2 * q + 1];
+    const int n = d.n, nc = d.nc, ncn = d.nconn;
+    double dRh[NCM], dRt[NCM];
+    for (int nu = 0; nu < nc; ++nu) {
+      dRh[nu] = d.dRdN[(int64_t)nu * n + i];
+      dRt[nu] = d.dRdN[(int64_t)nu * n + j];
+    }
+    int up[3];
+    bool pres[3];
+    double rho[3];
+    for (int a = 0; a < 3; ++a) {
+      up[a] = c.up[(int64_t)a * ncn + q];
+      pres[a] = (d.present[up[a]] >> a) & 1;
+      rho[a] = c.rho_cs[(int64_t)a * ncn + q];
+    }
+    double ri = 0, rj = 0;
+    for (int m = c.md_ptr[q]; m < c.md_ptr[q + 1]; ++m) {
+      const int ik = s_el[m - e0];
+      const double tk = s_k[m - k0];
+      const double bfk = d.bf[ik];
+      double Ji = 0, Jj = 0;
+      for (int a = 0; a < 3; ++a) {
+        if (!pres[a]) continue;
+        double psi = phase_pressure(d, ik, a) + rho[a] * bfk;
+        const double lam = d.lambda[(int64_t)a * n + up[a]];
+        for (int nu = 0; nu < nc; ++nu) {
+          double phaseCompMob = d.Cxi[((int64_t)nu * 3 + a) * n + up[a]] * lam;
+          double dNdt = -phaseCompMob * tk * psi;
+          double d2Ndtp = -phaseCompMob * tk;
+          ri += dRh[nu] * dNdt;
+          rj += -dRt[nu] * dNdt;
+          Ji += dRh[nu] * d2Ndtp;
+          Jj += -dRt[nu] * d2Ndtp;
+        }
+      }
+      s_jh[m - k0] = Ji;
+      s_jt[m - k0] = Jj;
+    }
+    rh[q] = ri;
+    rt[q] = rj;
+  }
+  __syncthreads();
+  for (int m = m0 + threadIdx.x; m < m1; m += FLUX_BLOCK) {
+    Jh[m] = s_jh[m - k0];
+    Jt[m] = s_jt[m - k0];
+  }
 }
 
 struct AsmDev {
@@ -1208,6 +1327,26 @@ __global__ void k_adj_objective(int ncells, const int* __restrict__ cells, const
 }  // namespace
 
 // ----------------------------------------------------------------------
+// A 1D tensor map of n elements (boxes of TMA_BOX elements, zero fill past
+// the end) for cp.async.bulk.tensor; false when the driver offers no encoder.
+static bool tensor_map_1d(CUtensorMap* m, void* base, uint64_t n, CUtensorMapDataType type) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    cudaGetLastError();
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode || n == 0 || n > (1ull << 32)) return false;
+  cuuint64_t dim[1] = {n}, stride[1] = {0};
+  cuuint32_t box[1] = {(cuuint32_t)TMA_BOX}, es[1] = {1};
+  return encode(m, type, 1, base, dim, stride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 struct HostFunc {
   DFunc d{};
   DeviceBuffer<double> coord[3], data;
@@ -1291,6 +1430,10 @@ struct Sim {
   HostFunc funcs[11];
   int rf_kind = RSG_RF_COREY;
   HostFunc rock_tab[7];  // krw, krg, krow, krog, kro, pcow, pcgo
+  // TMA staging of the flux assembly (k_flux_conn_tma): 1D tensor maps of
+  // the MD lists and the number of 256-entry boxes a block of connections needs
+  CUtensorMap tm_el{}, tm_k{};
+  int tma_chunks = 0;
   HostFunc initT, initC[NCM];
   DFluid fl{};
   DCorey co{};
@@ -1370,6 +1513,7 @@ struct Sim {
     ctx->sync();
     if (h == FL_DRDP) throw Error(RSG_PHYSICS, "dR/dp must be positive (check PVT data or datum depth/pressure)");
     if (h == FL_NO_WATER) throw Error(RSG_PHYSICS, "Water is not present");
+    if (h == FL_TMA) throw Error(RSG_TIMEOUT, "the staging copies of the flux assembly did not complete");
     if (h == FL_CUBIC + 2) throw Error(RSG_SINGULAR, "MatrixSingularException in the flash");
     if (h > FL_CUBIC) throw Error(RSG_PHYSICS, "cubic equation of state failed (code " + std::to_string(h - FL_CUBIC) + ")");
     if (h) throw Error(RSG_PHYSICS, "equation-of-state data check failed (code " + std::to_string(h) + ")");
@@ -1413,8 +1557,13 @@ struct Sim {
   // the preconditioner's setMatrix
   void newton_assemble(double dt) {
     SimDev d = dev();
-    RSG_LAUNCH(*ctx, "flux_conn", k_flux_conn, blocks_for(nconn, 128), 128, 0, d, cdev(), Jh.get(), Jt.get(),
-               rh.get(), rt.get());
+    if (tma_chunks > 0)
+      RSG_LAUNCH(*ctx, "flux_conn", k_flux_conn_tma, blocks_for(nconn, FLUX_BLOCK), FLUX_BLOCK,
+                 (size_t)tma_chunks * TMA_BOX * (sizeof(int) + 3 * sizeof(double)), d, cdev(), Jh.get(), Jt.get(),
+                 rh.get(), rt.get(), tm_el, tm_k, tma_chunks);
+    else
+      RSG_LAUNCH(*ctx, "flux_conn", k_flux_conn, blocks_for(nconn, 128), 128, 0, d, cdev(), Jh.get(), Jt.get(),
+                 rh.get(), rt.get());
     RSG_LAUNCH(*ctx, "assemble_rows", k_assemble_rows, blocks_for(n, 128), 128, 0, d, adev(), Jh.get(), Jt.get(),
                rh.get(), rt.get(), dt, A.m.val.get(), b.get(), keep_jacobian ? rawJ.get() : nullptr,
                keep_jacobian ? rawB.get() : nullptr);
@@ -1998,6 +2147,28 @@ static rsg_status sim_create(rsg_ctx* ctx, rsg_mesh* mesh, const rsg_blackoil* f
     S.rh.resize(S.nconn);
     S.rt.resize(S.nconn);
     S.cf.resize((size_t)nc * S.nconn);
+    // TMA staging of the flux assembly: the boxes a block of FLUX_BLOCK
+    // connections needs (RSG_FLUX_TMA=0 keeps the plain-load kernel)
+    {
+      const char* env = getenv("RSG_FLUX_TMA");
+      const auto& mp = mesh->m.h_md_ptr;
+      int chunks = 0;
+      if (!(env && env[0] == '0') && S.nconn > 0 && (int64_t)mp.size() > S.nconn) {
+        for (int q0 = 0; q0 < S.nconn; q0 += FLUX_BLOCK) {
+          const int m0 = mp[q0], m1 = mp[std::min(q0 + FLUX_BLOCK, S.nconn)];
+          chunks = std::max(chunks, (m1 - (m0 & ~1) + TMA_BOX - 1) / TMA_BOX);
+          chunks = std::max(chunks, (m1 - (m0 & ~3) + TMA_BOX - 1) / TMA_BOX);
+        }
+        const size_t smem = (size_t)chunks * TMA_BOX * (sizeof(int) + 3 * sizeof(double));
+        const bool ok = smem <= 200 * 1024 &&
+                        tensor_map_1d(&S.tm_el, mesh->m.md_elem.get(), (uint64_t)nmd, CU_TENSOR_MAP_DATA_TYPE_INT32) &&
+                        tensor_map_1d(&S.tm_k, mesh->m.md_k.get(), (uint64_t)nmd, CU_TENSOR_MAP_DATA_TYPE_FLOAT64) &&
+                        cudaFuncSetAttribute(k_flux_conn_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             200 * 1024) == cudaSuccess;
+        cudaGetLastError();
+        S.tma_chunks = ok ? chunks : 0;
+      }
+    }
     // sources
     std::vector<std::vector<int>> cell_src(n);
     std::vector<double> q((size_t)std::max(nsources, 1) * RSG_MAX_COMPONENTS, 0.0);
@@ -2398,6 +2569,14 @@ rsg_status rsg_sim_read_restart(rsg_sim* s, const char* path) {
     m.ctx->sync();  // buf goes out of scope
     m.check_flag();
   });
+}
+
+rsg_status rsg_sim_walk_shapes(rsg_sim* s, int32_t* shapes) {
+  if (!s || !shapes) return RSG_BAD_ARG;
+  int v[4] = {0, 0, 0, 0};
+  if (!rsg::ilu_walk_shape(rsg::solver_view(*s->s->solver).pc, -1, v)) return RSG_UNSUPPORTED;
+  for (int q = 0; q < 4; ++q) shapes[q] = v[q];
+  return RSG_OK;
 }
 
 rsg_status rsg_sim_set_rock_tables(rsg_sim* s, const rsg_rock_tables* t) {

@@ -189,3 +189,53 @@ def test_solve_batched_matches_single_solves(ctx, precision):
         if precision == 0:
             assert abs(inf.iterations - it1) <= max(2, it1 // 20), (inf.iterations, it1)
             assert np.max(np.abs(x - x1)) <= 1e-8 * np.max(np.abs(x1))
+
+
+SCRIPT_SHAPE = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r}); sys.path.insert(0, {tests!r})
+from test_gpu_ensemble import _first_jacobian
+from ressim_gb300 import abi, api
+ctx = api.Context(0)
+mats, solvers, bs = [], [], []
+for d, s in (((10, 8, 4), 3), ((16, 16, 6), 4), ((20, 12, 5), 5)):
+    rp, col, val, b = _first_jacobian(ctx, *d, seed=s)
+    M = api.CompRowMatrix(ctx, len(rp) - 1, rp, col, val)
+    sv = api.BiCGstab(ctx, abi.PC_ILU, rtol=1e-10, max_iter=5000)
+    sv.set_matrix(M)
+    mats.append(M); solvers.append(sv); bs.append(b)
+out = {{}}
+for prec in (0, 1):
+    xs, infos, sts = api.solve_batched(solvers, mats, bs, [np.zeros(len(b)) for b in bs], precision=prec)
+    assert not sts.any(), sts
+    for k, x in enumerate(xs):
+        out["x%d_%d" % (prec, k)] = x
+        out["it%d_%d" % (prec, k)] = np.array([infos[k].iterations, infos[k].inner_iterations])
+np.savez({path!r}, **out)
+print("shapes", solvers[0].walk_shapes())
+"""
+
+
+def test_solve_batched_cluster_shapes_identical(tmp_path):
+    """The persistent solver sums every dot product over the same 4,096
+    virtual threads in the same tree whatever the cluster shape: 16-CTA
+    clusters (the default) and 8-CTA clusters (RSG_RING_CTAS=8, run in a
+    child process) give bit-identical solutions and iteration counts, for
+    the FP64 and the mixed-precision solver."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    here = os.path.dirname(os.path.abspath(__file__))
+    res = {}
+    for ctas in ("16", "8"):
+        path = str(tmp_path / f"shape{ctas}.npz")
+        env = dict(os.environ, RSG_RING_CTAS=ctas)
+        r = subprocess.run([sys.executable, "-c", SCRIPT_SHAPE.format(root=root, tests=here, path=path)], env=env,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert f"shapes [{ctas}, {ctas}, {ctas}, {ctas}]" in r.stdout, r.stdout
+        res[ctas] = dict(np.load(path))
+    assert res["16"].keys() == res["8"].keys()
+    for k in res["16"]:
+        assert np.array_equal(res["16"][k], res["8"][k]), k

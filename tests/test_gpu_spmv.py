@@ -1,0 +1,89 @@
+"""The SpMV + dot kernels of the Krylov solvers: the shared-memory staged
+kernel (k_spmv_dot_tma, tiles of the SELL-32 matrix copied with
+cp.async.bulk) against the oracle's solves, on tile-aligned, ragged and
+empty-row patterns, and the plain kernel for slices wider than a stage."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from oracle import oracle as O  # noqa: E402
+from ressim_gb300 import abi, api  # noqa: E402
+from test_gpu_sweeps import pattern27  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def random_pattern(n, maxlen, seed, empty_every=0):
+    """Random rows of up to maxlen entries (diagonal dominant), every
+    empty_every-th row with its diagonal only."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    rp, col, val = [0], [], []
+    for i in range(n):
+        if empty_every and i % empty_every == 0:
+            cs = np.array([i])
+        else:
+            k = int(g.integers(1, maxlen))
+            cs = np.unique(np.concatenate([[i], g.integers(0, n, k - 1)]))
+        v = -g.random(len(cs))
+        v[cs == i] = 2.0 * maxlen
+        col.extend(cs.tolist())
+        val.extend(v.tolist())
+        rp.append(len(col))
+    return np.array(rp, np.int32), np.array(col, np.int32), np.array(val)
+
+
+def _solve(ctx, rp, col, val, b, cls=api.BiCGstab):
+    n = len(rp) - 1
+    A = api.CompRowMatrix(ctx, n, rp, col, val)
+    s = cls(ctx, abi.PC_ILU, rtol=1e-10, max_iter=5000)
+    s.set_matrix(A)
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    x = s.solve(A, b, np.zeros(n))
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    return x, s.last_info, prof, A
+
+
+@pytest.mark.parametrize("case", ["27pt", "ragged", "empty_rows", "wide"])
+def test_spmv_kernels_in_bicgstab(ctx, case):
+    """BiCGstab + ILU(0) to 1e-10 against the oracle: iteration counts within
+    two, solutions within 1e-8 of the largest entry.  Patterns up to 32
+    entries per row run the staged kernel (its profile entry), wider ones
+    the plain kernel."""
+    if case == "27pt":
+        rp, col, val = pattern27(24, 20, 9, seed=4)  # 4,320 rows: 16.9 tiles of 256
+    elif case == "ragged":
+        rp, col, val = random_pattern(1000, 32, 5)
+    elif case == "empty_rows":
+        rp, col, val = random_pattern(777, 20, 6, empty_every=3)
+    else:
+        rp, col, val = random_pattern(600, 48, 7)
+    n = len(rp) - 1
+    b = np.random.Generator(np.random.PCG64(8)).standard_normal(n)
+    x, info, prof, _ = _solve(ctx, rp, col, val, b)
+    xo, it, _, _, _ = O.solve(abi.BICGSTAB, abi.PC_ILU, rp, col, val, b, np.zeros(n), rtol=1e-10, maxit=5000)
+    assert info.reason == 0
+    assert abs(info.iterations - it) <= 2, (info.iterations, it)
+    assert np.max(np.abs(x - xo)) <= 1e-8 * np.max(np.abs(xo))
+    wmax = max(int(np.max(np.diff(rp)[s:s + 32])) for s in range(0, n, 32))
+    staged = "spmv_dot_tma" in prof
+    assert staged == (wmax <= 32), (wmax, sorted(prof))
+    assert staged != ("spmv_dot" in prof)
+
+
+def test_staged_fp32_spmv_in_mixed_solver(ctx):
+    """The FP32 staged kernel inside the mixed-precision solver: the FP64
+    outer iteration meets 1e-10 on the true residual."""
+    rp, col, val = pattern27(40, 36, 10, seed=9)
+    n = len(rp) - 1
+    b = np.random.Generator(np.random.PCG64(10)).standard_normal(n)
+    x, info, prof, A = _solve(ctx, rp, col, val, b, cls=api.MixedFGMRES)
+    assert info.reason == 0
+    assert "inner_spmv_dot_tma" in prof and "inner_spmv_dot" not in prof
+    r = b - A.mult(x)
+    assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)

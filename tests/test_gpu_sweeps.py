@@ -124,3 +124,27 @@ def test_ring_walk_cluster_sizes(ctas):
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "mode 2 fp64 bitexact True" in r.stdout, r.stdout
+
+
+@pytest.mark.parametrize("cls", [api.BiCGstab, api.MixedFGMRES])
+def test_walk_shapes_give_identical_results(ctx, cls):
+    """The walk autotuner chooses between 16-CTA and 8-CTA cluster schedules
+    per sweep and precision; every choice sums the rows in CSR order, so the
+    solutions with either shape forced and with the timed choice are
+    bit-identical, and walk_shapes reports the forced shape."""
+    rp, col, val = pattern27(48, 40, 12, seed=3)
+    n = len(rp) - 1
+    A = api.CompRowMatrix(ctx, n, rp, col, val)
+    b = np.random.Generator(np.random.PCG64(5)).random(n)
+    xs = []
+    for shape in (16, 8, 0):
+        s = cls(ctx, abi.PC_ILU, rtol=1e-10, max_iter=2000)
+        s.set_walk_shape(shape)
+        s.set_matrix(A)
+        xs.append(s.solve(A, b, np.zeros(n)))
+        got = s.walk_shapes()
+        assert all(v in (8, 16) for v in got), got
+        if shape:
+            assert got == [shape] * 4
+        s.release()
+    assert np.array_equal(xs[0], xs[1]) and np.array_equal(xs[0], xs[2])
