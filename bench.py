@@ -406,12 +406,10 @@ def mixed_leg(args, ctx, mesh, case, fluid, co, srcs, init, fp64_sim, n, dt, fp6
     f32_bytes = 8 * len(col) + 16 * n
     hbm, peak_kind = peaks()
     inner = None
-    ikey = "inner_spmv_dot_tma" if "inner_spmv_dot_tma" in prof else "inner_spmv_dot"
-    if ikey in prof:
-        t_ms, cnt = prof[ikey]
+    if "inner_spmv_dot" in prof:
+        t_ms, cnt = prof["inner_spmv_dot"]
         gbs = f32_bytes / (t_ms / cnt / 1e3) / 1e9
-        kname = "k_spmv_dot_tma<float>" if ikey.endswith("_tma") else "k_f32_spmv_dot"
-        inner = {"kernel": kname, "launches": cnt, "avg_launch_us": round(t_ms / cnt * 1e3, 2),
+        inner = {"kernel": "k_f32_spmv_dot", "launches": cnt, "avg_launch_us": round(t_ms / cnt * 1e3, 2),
                  "bytes_per_launch": f32_bytes, "achieved_gbs": round(gbs, 1), "peak": hbm,
                  "frac": round(gbs / hbm, 4), "peak_source": peak_kind}
     out = {"value": units / dev_s, "unit": METRIC, "ms_per_step": ms, "steps": steps,
@@ -453,10 +451,9 @@ def finish(args, ctx, mesh, sim, n, world, units, dev_s, wall, launches, clk, ne
                 "frac": round(achieved / hbm, 5), "traffic": traffic,
                 "traffic_source": NCU_TRAFFIC_SOURCE if traffic else None, "peak_source": peak_kind,
                 "bytes_per_launch": fam_bytes[k], "avg_launch_us": round(per_launch * 1e6, 2)}
-    skey = "spmv_dot_tma" if "spmv_dot_tma" in prof else "spmv_dot"
-    spmv_ms = prof.get(skey, (0, 1))
+    spmv_ms = prof.get("spmv_dot", (0, 1))
     spmv_bytes = 12 * len(col) + 4 * (n + 1) + 16 * n + 8 * n
-    spmv = {"kernel": "k_spmv_dot_tma<double>" if skey.endswith("_tma") else "k_spmv_dot",
+    spmv = {"kernel": "k_spmv_dot",
             "achieved_gbs": round(spmv_bytes / (spmv_ms[0] / spmv_ms[1] / 1e3) / 1e9, 1) if spmv_ms[0] else None,
             "bytes_per_launch": spmv_bytes}
     if spmv["achieved_gbs"]:

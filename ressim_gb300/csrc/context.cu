@@ -43,7 +43,6 @@ void Context::check_device_error() {
     const int at = *h;
     RSG_CUDA(cudaMemsetAsync(dev_err.get(), 0, sizeof(int), stream));
     sync();
-    if (at >= 0x40000000) throw Error(RSG_TIMEOUT, "an SpMV tile's shared-memory copy did not land in time");
     throw Error(RSG_TIMEOUT, "a level walk's wait ran out at level " + std::to_string(at - 1));
   }
 }

@@ -142,7 +142,6 @@ void Csr::build(Context* c, int n_, int nnz_, const int* rp, const int* cl) {
   RSG_CUDA(cudaMemcpyAsync(diag.get(), h_diag.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
   // SELL-32
   nslices = (n + SELL_C - 1) / SELL_C;
-  sell_wmax = 0;
   std::vector<int> base(nslices + 1), len(n);
   int64_t pos = 0;
   for (int s = 0; s < nslices; ++s) {
@@ -153,7 +152,6 @@ void Csr::build(Context* c, int n_, int nnz_, const int* rp, const int* cl) {
       w = std::max(w, len[r]);
     }
     pos += (int64_t)w * SELL_C;
-    sell_wmax = std::max(sell_wmax, w);
   }
   base[nslices] = (int)pos;
   if (pos > INT32_MAX) throw Error(RSG_UNSUPPORTED, "matrix too large for 32-bit SELL offsets");

@@ -13,7 +13,6 @@
 #include <cmath>
 
 #include "linalg.cuh"
-#include "ring.cuh"
 
 namespace rsg {
 
@@ -551,162 +550,6 @@ __global__ void __launch_bounds__(RT, 8) k_f32_spmv_dot(int n, const int* __rest
   reduce_finish<K>(v, ra.part, ra.ticket, epi, ra.s, ra.hist, ra.g, 0);
 }
 
-// ---- SpMV + dot with the matrix streamed through shared memory ----------
-// A tile is SPMV_TILE_SLICES consecutive SELL-32 slices (256 rows), stored
-// contiguously in the SELL value and column arrays.  Persistent CTAs (one
-// per SM) take tiles b, b + grid, ...; thread 0 copies each tile's values and
-// columns into a ring of stages with cp.async.bulk (completion counted on the
-// stage's mbarrier) S - 1 tiles ahead of the one the 8 warps compute, so the
-// matrix stream needs no registers and many bytes are in flight per SM.
-// Warp w computes slice w of the tile, lane l its row l: columns and values
-// from shared memory, x gathered through L1 16 entries at a time.  The
-// per-row arithmetic and the dot-product epilogues are those of k_spmv_dot
-// (FP64: one fused multiply-add per entry, exact zeros stored as +0) and
-// k_f32_spmv_dot (FP32 fused multiply-adds, FP64 dot accumulation).  Slices
-// wider than SPMV_WMAX use the plain kernels.
-constexpr int SPMV_TILE_SLICES = RT / 32;
-constexpr int SPMV_WMAX = 32;
-constexpr int SPMV_CAP = SPMV_TILE_SLICES * SPMV_WMAX * 32;  // entries per stage
-template <typename T>
-__host__ __device__ constexpr int spmv_stages() {
-  return sizeof(T) == 8 ? 2 : 3;
-}
-template <typename T>
-__host__ __device__ constexpr size_t spmv_stage_bytes() {
-  return (size_t)SPMV_CAP * (sizeof(T) + sizeof(int));
-}
-template <typename T>
-__host__ __device__ constexpr size_t spmv_smem_bytes() {
-  return spmv_stages<T>() * spmv_stage_bytes<T>() + 8 * spmv_stages<T>();
-}
-
-__device__ __forceinline__ void bulk_g2s(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-
-template <typename T, int K>
-__global__ void __launch_bounds__(RT, 1) k_spmv_dot_tma(int n, int nslices, const int* __restrict__ sb,
-                                                        const int* __restrict__ rl, const int* __restrict__ col,
-                                                        const T* __restrict__ val, const T* __restrict__ x,
-                                                        T* __restrict__ y, const T* __restrict__ w, RedArgs ra,
-                                                        int epi, int* err) {
-  if (stopped(ra.s)) return;
-  constexpr int S = spmv_stages<T>();
-  extern __shared__ __align__(128) unsigned char smem[];
-  const unsigned bar0 = smem_addr(smem + S * spmv_stage_bytes<T>());
-  const int ntiles = (nslices + SPMV_TILE_SLICES - 1) / SPMV_TILE_SLICES;
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  if (threadIdx.x < S) mbar_init(bar0 + 8 * threadIdx.x, 1);
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  __syncthreads();
-  // thread 0: copy tile t into stage st
-  auto issue = [&](int t, int st) {
-    const int s0 = t * SPMV_TILE_SLICES, s1 = min(s0 + SPMV_TILE_SLICES, nslices);
-    const int e0 = sb[s0], cnt = sb[s1] - e0;
-    unsigned char* base = smem + st * spmv_stage_bytes<T>();
-    const unsigned vb = (unsigned)(cnt * sizeof(T)), cb = (unsigned)(cnt * sizeof(int));
-    mbar_arm(bar0 + 8 * st, vb + cb);
-    if (cnt > 0) {
-      bulk_g2s(smem_addr(base), val + e0, vb, bar0 + 8 * st);
-      bulk_g2s(smem_addr(base + SPMV_CAP * sizeof(T)), col + e0, cb, bar0 + 8 * st);
-    }
-  };
-  if (threadIdx.x == 0)
-    for (int j = 0; j < S; ++j) {
-      const int t = blockIdx.x + j * (int)gridDim.x;
-      if (t < ntiles) issue(t, j);
-    }
-  double v[K];
-#pragma unroll
-  for (int q = 0; q < K; ++q) v[q] = 0;
-  int j = 0;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++j) {
-    const int st = j % S;
-    const int late = threadIdx.x == 0 ? !mbar_wait(bar0 + 8 * st, (unsigned)((j / S) & 1)) : 0;
-    if (__syncthreads_or(late)) {
-      // a copy did not land: report it and leave this tile and the rest
-      // (copies still in flight target this CTA's own shared memory only)
-      if (threadIdx.x == 0) atomicCAS(err, 0, 0x40000000);
-      for (int i = 0; i < 64; ++i) __nanosleep(1000);
-      break;
-    }
-    const unsigned char* base = smem + st * spmv_stage_bytes<T>();
-    const T* sval = reinterpret_cast<const T*>(base);
-    const int* scol = reinterpret_cast<const int*>(base + SPMV_CAP * sizeof(T));
-    const int slice = t * SPMV_TILE_SLICES + wp, row = slice * 32 + lane;
-    if (slice < nslices && row < n) {
-      const int off = sb[slice] - sb[t * SPMV_TILE_SLICES] + lane, len = rl[row];
-      T d = 0;
-      for (int k0 = 0; k0 < len; k0 += 16) {
-        T xv[16];
-#pragma unroll
-        for (int k = 0; k < 16; ++k)
-          if (k0 + k < len) xv[k] = __ldg(x + scol[off + 32 * (k0 + k)]);
-#pragma unroll
-        for (int k = 0; k < 16; ++k)
-          if (k0 + k < len) {
-            if constexpr (sizeof(T) == 8) d = __fma_rn(sval[off + 32 * (k0 + k)], xv[k], d);
-            else d = fmaf(sval[off + 32 * (k0 + k)], xv[k], d);
-          }
-      }
-      if constexpr (sizeof(T) == 8) {
-        const double yi = (d != 0) ? d : 0.0;
-        y[row] = yi;
-        if (K == 1) v[0] = __fma_rn(w[row], yi, v[0]);
-        if (K == 2) {
-          v[0] = __fma_rn(yi, w[row], v[0]);
-          v[K - 1] = __fma_rn(yi, yi, v[K - 1]);
-        }
-      } else {
-        y[row] = d;
-        if (K == 1) v[0] += (double)w[row] * d;
-        if (K == 2) {
-          v[0] += (double)d * w[row];
-          v[K - 1] += (double)d * d;
-        }
-      }
-    }
-    __syncthreads();  // every warp is done with this stage
-    const int tn = t + S * (int)gridDim.x;
-    if (threadIdx.x == 0 && tn < ntiles) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(tn, st);
-    }
-  }
-  reduce_finish<K>(v, ra.part, ra.ticket, epi, ra.s, ra.hist, ra.g, 0);
-}
-
-// The staged kernel when every slice fits a stage (and RSG_SPMV_TMA is not
-// 0); false: the caller launches the plain kernel.
-static bool spmv_tma_enabled() {
-  static const bool on = [] {
-    const char* e = getenv("RSG_SPMV_TMA");
-    return !(e && std::string(e) == "0");
-  }();
-  return on;
-}
-
-template <typename T, int K>
-static bool launch_spmv_dot_tma(Context& ctx, const Csr& A, const T* val, const T* x, T* y, const T* w, RedArgs ra,
-                                int epi) {
-  if (!spmv_tma_enabled() || A.sell_wmax > SPMV_WMAX || A.nslices == 0 || ctx.num_sms <= 0) return false;
-  static bool attr = false;  // one attribute call per kernel instantiation
-  if (!attr) {
-    RSG_CUDA(cudaFuncSetAttribute(k_spmv_dot_tma<T, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)spmv_smem_bytes<T>()));
-    attr = true;
-  }
-  const int ntiles = (A.nslices + SPMV_TILE_SLICES - 1) / SPMV_TILE_SLICES;
-  const int grid = std::min(ntiles, ctx.num_sms);
-  RSG_LAUNCH(ctx, sizeof(T) == 8 ? "spmv_dot_tma" : "inner_spmv_dot_tma", (k_spmv_dot_tma<T, K>), grid, RT,
-             spmv_smem_bytes<T>(), A.n, A.nslices, A.slice_base.get(), A.row_len.get(), A.sell_col.get(), val, x, y,
-             w, ra, epi, ctx.dev_err.get());
-  return true;
-}
-
 __global__ void __launch_bounds__(RT) k_f32_bicg_s(int n, const float* __restrict__ r, const float* __restrict__ v,
                                                    float* __restrict__ sv, RedArgs ra) {
   if (stopped(ra.s)) return;
@@ -873,16 +716,14 @@ struct Solver {
       for (int it = 0; it < batch(); ++it) {
         RSG_LAUNCH(*ctx, "bicg_p", k_bicg_p, eb, 256, 0, n, r, v, p, state.get());
         pc->apply(p, ph, act);
-        if (!launch_spmv_dot_tma<double, 1>(*ctx, A, A.sell_val.get(), ph, v, rt, red(), (int)EPI_BICG_ALPHA))
-          RSG_LAUNCH(*ctx, "spmv_dot", k_spmv_dot<1>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
-                     A.sell_col.get(), A.sell_val.get(), ph, v, rt, red(), (int)EPI_BICG_ALPHA);
+        RSG_LAUNCH(*ctx, "spmv_dot", k_spmv_dot<1>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
+                   A.sell_col.get(), A.sell_val.get(), ph, v, rt, red(), (int)EPI_BICG_ALPHA);
         RSG_LAUNCH(*ctx, "bicg_s", k_bicg_s, nblk, RT, 0, n, r, v, s, red());
         RSG_LAUNCH(*ctx, "bicg_xfinal", k_bicg_xfinal, eb, 256, 0, n, ph, x, state.get());
         RSG_LAUNCH(*ctx, "status_fix", k_status_fix, 1, 1, 0, state.get());
         pc->apply(s, sh, act);
-        if (!launch_spmv_dot_tma<double, 2>(*ctx, A, A.sell_val.get(), sh, t, s, red(), (int)EPI_BICG_OMEGA))
-          RSG_LAUNCH(*ctx, "spmv_dot", k_spmv_dot<2>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
-                     A.sell_col.get(), A.sell_val.get(), sh, t, s, red(), (int)EPI_BICG_OMEGA);
+        RSG_LAUNCH(*ctx, "spmv_dot", k_spmv_dot<2>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
+                   A.sell_col.get(), A.sell_val.get(), sh, t, s, red(), (int)EPI_BICG_OMEGA);
         RSG_LAUNCH(*ctx, "bicg_update", k_bicg_update, nblk, RT, 0, n, ph, sh, s, t, rt, x, r, red());
       }
     }
@@ -901,9 +742,8 @@ struct Solver {
         pc->apply(r, z, act);
         RSG_LAUNCH(*ctx, "dot", k_dot, nblk, RT, 0, n, r, z, red(), (int)EPI_CG_RHO, 0);
         RSG_LAUNCH(*ctx, "cg_p", k_cg_p, eb, 256, 0, n, z, p, state.get());
-        if (!launch_spmv_dot_tma<double, 1>(*ctx, A, A.sell_val.get(), p, q, p, red(), (int)EPI_CG_ALPHA))
-          RSG_LAUNCH(*ctx, "spmv_dot", k_spmv_dot<1>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
-                     A.sell_col.get(), A.sell_val.get(), p, q, p, red(), (int)EPI_CG_ALPHA);
+        RSG_LAUNCH(*ctx, "spmv_dot", k_spmv_dot<1>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
+                   A.sell_col.get(), A.sell_val.get(), p, q, p, red(), (int)EPI_CG_ALPHA);
         RSG_LAUNCH(*ctx, "cg_update", k_cg_update, nblk, RT, 0, n, p, q, x, r, red());
       }
     }
@@ -959,16 +799,14 @@ struct Solver {
         for (int q = 0; q < inner_iters; ++q) {
           RSG_LAUNCH(*ctx, "inner_p", k_f32_bicg_p, eb, 256, 0, n, ir, iv, ip, sin);
           pc->apply_f32(ip, iph, act_in);
-          if (!launch_spmv_dot_tma<float, 1>(*ctx, A, A.sell_valf.get(), iph, iv, irt, ri, (int)EPI_BICG_ALPHA))
-            RSG_LAUNCH(*ctx, "inner_spmv_dot", k_f32_spmv_dot<1>, nblk, RT, 0, n, A.slice_base.get(),
-                       A.row_len.get(), A.sell_col.get(), A.sell_valf.get(), iph, iv, irt, ri, (int)EPI_BICG_ALPHA);
+          RSG_LAUNCH(*ctx, "inner_spmv_dot", k_f32_spmv_dot<1>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
+                     A.sell_col.get(), A.sell_valf.get(), iph, iv, irt, ri, (int)EPI_BICG_ALPHA);
           RSG_LAUNCH(*ctx, "inner_s", k_f32_bicg_s, nblk, RT, 0, n, ir, iv, is, ri);
           RSG_LAUNCH(*ctx, "inner_xfinal", k_f32_bicg_xfinal, eb, 256, 0, n, iph, ix, sin);
           RSG_LAUNCH(*ctx, "status_fix", k_status_fix, 1, 1, 0, sin);
           pc->apply_f32(is, ish, act_in);
-          if (!launch_spmv_dot_tma<float, 2>(*ctx, A, A.sell_valf.get(), ish, it, is, ri, (int)EPI_BICG_OMEGA))
-            RSG_LAUNCH(*ctx, "inner_spmv_dot", k_f32_spmv_dot<2>, nblk, RT, 0, n, A.slice_base.get(),
-                       A.row_len.get(), A.sell_col.get(), A.sell_valf.get(), ish, it, is, ri, (int)EPI_BICG_OMEGA);
+          RSG_LAUNCH(*ctx, "inner_spmv_dot", k_f32_spmv_dot<2>, nblk, RT, 0, n, A.slice_base.get(), A.row_len.get(),
+                     A.sell_col.get(), A.sell_valf.get(), ish, it, is, ri, (int)EPI_BICG_OMEGA);
           RSG_LAUNCH(*ctx, "inner_update", k_f32_bicg_update, nblk, RT, 0, n, iph, ish, is, it, irt, ix, ir, ri);
         }
         RSG_LAUNCH(*ctx, "to_f64", k_f32_to_f64, eb, 256, 0, n, ix, zcol(i), (const KState*)sin, state.get());

@@ -72,7 +72,6 @@ struct Csr {
   DeviceBuffer<double> val;
   // SELL-32 copy used by SpMV
   int nslices = 0;
-  int sell_wmax = 0;  // widest slice (entries per row slot)
   int64_t sell_size = 0;
   DeviceBuffer<int> slice_base, row_len, sell_col, sell_src;
   DeviceBuffer<double> sell_val;

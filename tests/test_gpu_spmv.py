@@ -1,7 +1,7 @@
-"""The SpMV + dot kernels of the Krylov solvers: the shared-memory staged
-kernel (k_spmv_dot_tma, tiles of the SELL-32 matrix copied with
-cp.async.bulk) against the oracle's solves, on tile-aligned, ragged and
-empty-row patterns, and the plain kernel for slices wider than a stage."""
+"""The SELL-32 SpMV + dot kernels of the Krylov solvers (k_spmv_dot,
+k_f32_spmv_dot) inside BiCGstab and the mixed-precision solver, against
+the oracle's solves on 27-point, ragged (slices of mixed row lengths, n
+not a multiple of 32), empty-row and wide-row patterns."""
 import os
 import sys
 
@@ -52,11 +52,10 @@ def _solve(ctx, rp, col, val, b, cls=api.BiCGstab):
 @pytest.mark.parametrize("case", ["27pt", "ragged", "empty_rows", "wide"])
 def test_spmv_kernels_in_bicgstab(ctx, case):
     """BiCGstab + ILU(0) to 1e-10 against the oracle: iteration counts within
-    two, solutions within 1e-8 of the largest entry.  Patterns up to 32
-    entries per row run the staged kernel (its profile entry), wider ones
-    the plain kernel."""
+    two, solutions within 1e-8 of the largest entry, the fused SpMV + dot
+    kernel on every pattern."""
     if case == "27pt":
-        rp, col, val = pattern27(24, 20, 9, seed=4)  # 4,320 rows: 16.9 tiles of 256
+        rp, col, val = pattern27(24, 20, 9, seed=4)
     elif case == "ragged":
         rp, col, val = random_pattern(1000, 32, 5)
     elif case == "empty_rows":
@@ -70,20 +69,17 @@ def test_spmv_kernels_in_bicgstab(ctx, case):
     assert info.reason == 0
     assert abs(info.iterations - it) <= 2, (info.iterations, it)
     assert np.max(np.abs(x - xo)) <= 1e-8 * np.max(np.abs(xo))
-    wmax = max(int(np.max(np.diff(rp)[s:s + 32])) for s in range(0, n, 32))
-    staged = "spmv_dot_tma" in prof
-    assert staged == (wmax <= 32), (wmax, sorted(prof))
-    assert staged != ("spmv_dot" in prof)
+    assert "spmv_dot" in prof, sorted(prof)
 
 
-def test_staged_fp32_spmv_in_mixed_solver(ctx):
-    """The FP32 staged kernel inside the mixed-precision solver: the FP64
-    outer iteration meets 1e-10 on the true residual."""
+def test_fp32_spmv_in_mixed_solver(ctx):
+    """The FP32 SpMV + dot inside the mixed-precision solver: the FP64 outer
+    iteration meets 1e-10 on the true residual."""
     rp, col, val = pattern27(40, 36, 10, seed=9)
     n = len(rp) - 1
     b = np.random.Generator(np.random.PCG64(10)).standard_normal(n)
     x, info, prof, A = _solve(ctx, rp, col, val, b, cls=api.MixedFGMRES)
     assert info.reason == 0
-    assert "inner_spmv_dot_tma" in prof and "inner_spmv_dot" not in prof
+    assert "inner_spmv_dot" in prof
     r = b - A.mult(x)
     assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
