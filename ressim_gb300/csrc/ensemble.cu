@@ -175,7 +175,8 @@ __device__ __forceinline__ void cluster_sum(double (&v)[EnsShape<CTAS>::VPT][K],
 }
 
 // A walk as a called function: its registers are allocated apart from the
-// solver loop's, which keeps both free of spills.
+// solver loop's, which keeps both free of spills.  FP64 rows are summed with
+// fused multiply-adds, as the stream path's solver applies do.
 // (13 entries of a row in registers, as for the 27-point stencil; longer
 // rows read the rest from memory)
 // The schedule and vectors are copied into local variables first: through
@@ -185,7 +186,7 @@ template <int KIND, typename T, int CTAS>
 __device__ __noinline__ bool walk(const RingArgs& g, const RingVals<T>& a, unsigned char* smem) {
   const RingArgs gl = g;
   const RingVals<T> al = a;
-  return ring_walk<KIND, T, 13, CTAS, ENS_THREADS>(gl, al, smem);
+  return ring_walk<KIND, T, 13, CTAS, ENS_THREADS, true>(gl, al, smem);
 }
 
 // out = M^-1 in (ILU(0): L y = in, U out = y, FP64 factors) on the cluster;
@@ -807,11 +808,13 @@ void ensemble_solve(const std::vector<EnsSystem>& sys, int precision, std::vecto
   std::vector<EnsMember> h;
   int C = 0, R = 0, mr = 0;
   size_t nw = 0, nf = 0;
-  // 8-CTA clusters when planned: twice as many members in flight as with
-  // 16-CTA clusters (measured on 152 SMs: with 16-CTA clusters one to four
-  // members took the same time and eight took twice as long, so about six
-  // such clusters were resident at once)
-  const int prefer = 8;
+  // 8-CTA clusters when planned and there are more members than 16-CTA
+  // clusters run at once: twice as many members in flight (measured on 152
+  // SMs: with 16-CTA clusters one to four members took the same time and
+  // eight took twice as long; with 8-CTA clusters one to nine took the same
+  // time).  A few members alone are faster on 16 SMs each (a 96x96x24 member:
+  // 3.6 against 4.7 ms per iteration).
+  const int prefer = count > 4 ? 8 : 16;
   for (int i = 0; i < count; ++i) {
     const EnsSystem& q = sys[i];
     SolverView sv = solver_view(*q.solver);

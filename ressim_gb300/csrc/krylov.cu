@@ -1027,7 +1027,7 @@ static rsg_status precond_host(rsg_solver* s, const double* b, double* x, bool t
     RSG_CUDA(cudaMemcpyAsync(db.get(), b, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     RSG_CUDA(cudaMemcpyAsync(dx.get(), x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     if (trans) s->s->pc->trans_apply(db.get(), dx.get(), nullptr);
-    else s->s->pc->apply(db.get(), dx.get(), nullptr);
+    else s->s->pc->apply_exact(db.get(), dx.get());
     RSG_CUDA(cudaMemcpyAsync(x, dx.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
     ctx->check_device_error();

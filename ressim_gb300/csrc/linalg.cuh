@@ -109,6 +109,9 @@ struct Precond {
   // x := M^{-1} b (x may be read as the starting iterate, as SSOR does)
   virtual void apply(const double* b, double* x, const int* active) = 0;
   virtual void trans_apply(const double* b, double* x, const int* active) = 0;
+  // Preconditioner.apply with MTJ's rounding (the solvers' applies may fuse
+  // multiply-adds)
+  virtual void apply_exact(const double* b, double* x) { apply(b, x, nullptr); }
   // FP32 variant for the mixed-precision inner solver
   virtual void apply_f32(const float* b, float* x, const int* active) {
     throw Error(RSG_UNSUPPORTED, "preconditioner has no FP32 variant");

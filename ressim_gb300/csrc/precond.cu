@@ -869,9 +869,9 @@ static bool ring_schedulable(Kernel kern, int ctas, size_t smem) {
 // issue slots whether its lanes are active or not, so the kernel is built
 // for 13 entries (the 27-point stencil's triangles) and for 16; longer rows
 // read their remaining entries from memory.
-template <int KIND, typename T, int CTAS, int MAXW>
+template <int KIND, typename T, int CTAS, int MAXW, bool FMA>
 static bool launch_ring_n(Context& ctx, const char* name, const RingPlan& G, const RingVals<T>& a, size_t smem) {
-  auto kern = k_sweep_ring<KIND, T, MAXW, CTAS>;
+  auto kern = k_sweep_ring<KIND, T, MAXW, CTAS, FMA>;
   static std::atomic<int> ok{0};  // per instantiation: 0 not probed, 1 schedulable, -1 not
   if (!ok) {
     std::lock_guard<std::mutex> lk(g_probe_mu);
@@ -911,7 +911,7 @@ struct RingPick<float> {
   static const float* diag(const RingPlan& G) { return G.diagf.get(); }
 };
 
-template <int KIND, typename T>
+template <int KIND, typename T, bool FMA>
 static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, const T* val, const T* diag, const T* b,
                         T* x, const int* active) {
   const RingPlan& G = P.ring(sizeof(T) == 4 ? 1 : 0);
@@ -921,23 +921,25 @@ static bool launch_ring(Context& ctx, const char* name, const SweepPlan& P, cons
   const RingVals<T> a{val, diag, b, x, active};
   const bool narrow = G.maxlen <= 13;
   if (G.C == 16)
-    return narrow ? launch_ring_n<KIND, T, 16, 13>(ctx, name, G, a, smem)
-                  : launch_ring_n<KIND, T, 16, 16>(ctx, name, G, a, smem);
+    return narrow ? launch_ring_n<KIND, T, 16, 13, FMA>(ctx, name, G, a, smem)
+                  : launch_ring_n<KIND, T, 16, 16, FMA>(ctx, name, G, a, smem);
   if (G.C == 8)
-    return narrow ? launch_ring_n<KIND, T, 8, 13>(ctx, name, G, a, smem)
-                  : launch_ring_n<KIND, T, 8, 16>(ctx, name, G, a, smem);
+    return narrow ? launch_ring_n<KIND, T, 8, 13, FMA>(ctx, name, G, a, smem)
+                  : launch_ring_n<KIND, T, 8, 16, FMA>(ctx, name, G, a, smem);
   return false;
 }
 
-template <int KIND, typename T>
+// FMA: the ring walk sums each row with fused multiply-adds (the Krylov
+// solvers' applies); otherwise every path rounds as MTJ does.
+template <int KIND, typename T, bool FMA = false>
 static void run_sweep(Context& ctx, const char* name, const SweepPlan& P, const T* val, const T* diag, const T* b,
                       T* x, T* xx, T omega, const int* active) {
   SweepArgs<T> a{P.nlev, P.level_slices.get(), P.slice_base.get(), P.row.get(), P.len.get(), P.col.get(), val, diag,
                  b, x, xx, omega, active};
   if constexpr (KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER) {
     const RingPlan& G = P.ring(sizeof(T) == 4 ? 1 : 0);
-    const bool ring = launch_ring<KIND, T>(ctx, name, P, RingPick<T>::val(G),
-                                           KIND == SW_ILU_UPPER ? RingPick<T>::diag(G) : nullptr, b, x, active);
+    const bool ring = launch_ring<KIND, T, FMA>(ctx, name, P, RingPick<T>::val(G),
+                                                KIND == SW_ILU_UPPER ? RingPick<T>::diag(G) : nullptr, b, x, active);
     if (ring) return;
   }
   if ((KIND == SW_ILU_LOWER || KIND == SW_ILU_UPPER) && P.nlev <= SWEEP_MAX_LEVELS) {
@@ -1056,8 +1058,8 @@ struct ILUPrecond : Precond {
 
   // Walk autotuner: the first setup on a pattern times each sweep's ring
   // schedules (16 CTAs of 4 warps, 8 CTAs of 8 warps) on the factor values,
-  // for the FP64 and the FP32 walks, and keeps the faster per sweep and
-  // precision.  Every schedule sums each row in CSR order, so the choice
+  // for the FP64 and the FP32 walks as the solvers run them (FP64 with fused
+  // multiply-adds), and keeps the faster per sweep and precision.  Every schedule sums each row in CSR order, so the choice
   // never changes a result bit.  force_ctas (rsg_solver_set_walk_shape)
   // replaces the timing by a fixed shape.
   int force_ctas = 0;
@@ -1092,17 +1094,21 @@ struct ILUPrecond : Precond {
           float ms;
           if (prec == 0) {
             ms = time_ms([&] {
-              if (lower) run_sweep<SW_ILU_LOWER, double>(*ctx, "ilu_tune", Lp, Lp.val.get(), nullptr, bd.get(),
-                                                          xd.get(), nullptr, 0.0, nullptr);
-              else run_sweep<SW_ILU_UPPER, double>(*ctx, "ilu_tune", Up, Up.val.get(), Up.diag.get(), bd.get(),
-                                                   xd.get(), nullptr, 0.0, nullptr);
+              if (lower)
+                run_sweep<SW_ILU_LOWER, double, true>(*ctx, "ilu_tune", Lp, Lp.val.get(), nullptr, bd.get(), xd.get(),
+                                                      nullptr, 0.0, nullptr);
+              else
+                run_sweep<SW_ILU_UPPER, double, true>(*ctx, "ilu_tune", Up, Up.val.get(), Up.diag.get(), bd.get(),
+                                                      xd.get(), nullptr, 0.0, nullptr);
             });
           } else {
             ms = time_ms([&] {
-              if (lower) run_sweep<SW_ILU_LOWER, float>(*ctx, "ilu_tune", Lp, Lp.valf.get(), nullptr, bf.get(),
-                                                         xf.get(), nullptr, 0.0f, nullptr);
-              else run_sweep<SW_ILU_UPPER, float>(*ctx, "ilu_tune", Up, Up.valf.get(), Up.diagf.get(), bf.get(),
-                                                  xf.get(), nullptr, 0.0f, nullptr);
+              if (lower)
+                run_sweep<SW_ILU_LOWER, float, true>(*ctx, "ilu_tune", Lp, Lp.valf.get(), nullptr, bf.get(), xf.get(),
+                                                     nullptr, 0.0f, nullptr);
+              else
+                run_sweep<SW_ILU_UPPER, float, true>(*ctx, "ilu_tune", Up, Up.valf.get(), Up.diagf.get(), bf.get(),
+                                                     xf.get(), nullptr, 0.0f, nullptr);
             });
           }
           if (ms < best_ms) {
@@ -1119,17 +1125,25 @@ struct ILUPrecond : Precond {
     ctx->check_device_error();
   }
 
+  // the Krylov solvers' applies: FP64 rows summed with fused multiply-adds
   void apply(const double* b, double* x, const int* active) override {
     // L.solve(b, y); U.solve(y, x)
-    run_sweep<SW_ILU_LOWER, double>(*ctx, "ilu_lower", Lp, Lp.val.get(), nullptr, b, y.get(), nullptr, 0.0, active);
+    run_sweep<SW_ILU_LOWER, double, true>(*ctx, "ilu_lower", Lp, Lp.val.get(), nullptr, b, y.get(), nullptr, 0.0,
+                                          active);
+    run_sweep<SW_ILU_UPPER, double, true>(*ctx, "ilu_upper", Up, Up.val.get(), Up.diag.get(), y.get(), x, nullptr,
+                                          0.0, active);
+  }
+  // Preconditioner.apply as MTJ rounds it (ILU.java:64-70)
+  void apply_exact(const double* b, double* x) override {
+    run_sweep<SW_ILU_LOWER, double>(*ctx, "ilu_lower", Lp, Lp.val.get(), nullptr, b, y.get(), nullptr, 0.0, nullptr);
     run_sweep<SW_ILU_UPPER, double>(*ctx, "ilu_upper", Up, Up.val.get(), Up.diag.get(), y.get(), x, nullptr, 0.0,
-                                    active);
+                                    nullptr);
   }
   void apply_f32(const float* b, float* x, const int* active) override {
-    run_sweep<SW_ILU_LOWER, float>(*ctx, "ilu_lower_f32", Lp, Lp.valf.get(), nullptr, b, yf.get(), nullptr, 0.0f,
-                                   active);
-    run_sweep<SW_ILU_UPPER, float>(*ctx, "ilu_upper_f32", Up, Up.valf.get(), Up.diagf.get(), yf.get(), x, nullptr,
-                                   0.0f, active);
+    run_sweep<SW_ILU_LOWER, float, true>(*ctx, "ilu_lower_f32", Lp, Lp.valf.get(), nullptr, b, yf.get(), nullptr,
+                                         0.0f, active);
+    run_sweep<SW_ILU_UPPER, float, true>(*ctx, "ilu_upper_f32", Up, Up.valf.get(), Up.diagf.get(), yf.get(), x,
+                                         nullptr, 0.0f, active);
   }
   void trans_apply(const double* b, double* x, const int* active) override;
 };

@@ -210,11 +210,22 @@ __device__ __forceinline__ int bar_red_or(int pred) {
   return r;
 }
 
+// One term of a row's sum: sum + v x, rounded after the product and after
+// the sum (MTJ's arithmetic) or, for FP64 with FMA, once (a fused
+// multiply-add: half the FP64 instructions of a level, which set about half
+// its cost).  FP32 walks always round twice: their arithmetic is cheap, and
+// fusing them made the mixed-precision step 9% slower.
+template <bool FMA, typename T>
+__device__ __forceinline__ T row_term(T sum, T v, T x) {
+  if constexpr (FMA && sizeof(T) == 8) return __fma_rn(v, x, sum);
+  else return sum + v * x;
+}
+
 // The level loop of ring_walk, run by the walking warps only (the first
 // RING_SLICES / RING_CTAS warps of each CTA; their barrier is the CTA barrier
 // when they are the whole CTA, else named barrier 1).  Ends when everything
 // owed to this CTA has landed; false when a wait ran out (g.err is set).
-template <int KIND, typename T, int MAXW, int RING_CTAS, int CTA_THREADS>
+template <int KIND, typename T, int MAXW, int RING_CTAS, int CTA_THREADS, bool FMA>
 __device__ __forceinline__ bool ring_levels(const RingArgs& g, const RingVals<T>& a, T* ring, unsigned ring0,
                                             unsigned bar0, unsigned tok0, unsigned rank) {
   constexpr int RING_WARPS = RING_SLICES / RING_CTAS;
@@ -265,10 +276,10 @@ __device__ __forceinline__ bool ring_levels(const RingArgs& g, const RingVals<T>
       T sum = 0;
 #pragma unroll
       for (int k = 0; k < MAXW; ++k)
-        if (k < cur.len) sum += cur.v[k] * ring[cur.c[k]];
+        if (k < cur.len) sum = row_term<FMA>(sum, cur.v[k], ring[cur.c[k]]);
       for (int k = MAXW; k < cur.len; ++k) {
         const int q = cur.base + 32 * k;
-        sum += a.val[q] * ring[g.ridx[q]];
+        sum = row_term<FMA>(sum, a.val[q], ring[g.ridx[q]]);
       }
       v = (KIND == SW_ILU_LOWER) ? cur.b - sum : (cur.b - sum) / cur.d;
       ring[own] = v;
@@ -314,8 +325,10 @@ __device__ __forceinline__ bool ring_levels(const RingArgs& g, const RingVals<T>
 // ring_smem_bytes<T>(g.R).  Returns false when a wait ran out (g.err is
 // set); the caller must then stop using the cluster's shared memory for
 // walks.  On success every mbarrier is invalidated again, so the same memory
-// can hold the next walk.
-template <int KIND, typename T, int MAXW, int RING_CTAS, int CTA_THREADS = RING_SLICES / RING_CTAS * 32>
+// can hold the next walk.  FMA: an FP64 row's terms as fused multiply-adds
+// instead of MTJ's product-then-sum rounding.
+template <int KIND, typename T, int MAXW, int RING_CTAS, int CTA_THREADS = RING_SLICES / RING_CTAS * 32,
+          bool FMA = false>
 __device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& a, unsigned char* smem) {
   constexpr int RING_WARPS = RING_SLICES / RING_CTAS;
   constexpr int WALK_THREADS = RING_WARPS * 32;
@@ -331,7 +344,7 @@ __device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& 
   cluster.sync();  // every replica's barriers exist before the first push
   bool ok = true;
   if (CTA_THREADS == WALK_THREADS || threadIdx.x < WALK_THREADS)
-    ok = ring_levels<KIND, T, MAXW, RING_CTAS, CTA_THREADS>(g, a, ring, ring0, bar0, tok0, rank);
+    ok = ring_levels<KIND, T, MAXW, RING_CTAS, CTA_THREADS, FMA>(g, a, ring, ring0, bar0, tok0, rank);
   cluster.sync();
   if (*(volatile int*)g.err != 0) {
     // a wait ran out somewhere: give pushes still in flight time to land
@@ -345,11 +358,11 @@ __device__ __forceinline__ bool ring_walk(const RingArgs& g, const RingVals<T>& 
   return ok;
 }
 
-template <int KIND, typename T, int MAXW, int RING_CTAS>
+template <int KIND, typename T, int MAXW, int RING_CTAS, bool FMA>
 __global__ void __launch_bounds__(RING_SLICES / RING_CTAS * 32) k_sweep_ring(RingArgs g, RingVals<T> a) {
   if (a.active && *a.active != 0) return;  // uniform over the cluster
   extern __shared__ __align__(16) unsigned char smem[];
-  ring_walk<KIND, T, MAXW, RING_CTAS>(g, a, smem);
+  ring_walk<KIND, T, MAXW, RING_CTAS, RING_SLICES / RING_CTAS * 32, FMA>(g, a, smem);
 }
 
 
