@@ -41,8 +41,8 @@ def _sim(ctx, case, perm, spec_kw=TIGHT, corey=None):
     return gs
 
 
-def _objective(ctx, case, perm, dts):
-    gs = _sim(ctx, case, perm)
+def _objective(ctx, case, perm, dts, spec_kw=TIGHT):
+    gs = _sim(ctx, case, perm, spec_kw)
     J, _ = gs.forward(dts, len(dts), case["producer"], [0.0, 1.0])
     return J
 
@@ -266,3 +266,25 @@ def test_adjoint_with_capillary_pressure(ctx):
             vals.append(sim.forward(dts, 1, case["producer"], [0.0, 1.0])[0])
         fd = (vals[0] - vals[1]) / (2 * H_FINE)
         assert abs(fd - grad[e]) <= FD_NOISE * J / H_FINE + 1e-5 * scale, (e, fd, grad[e], scale)
+
+
+def test_adjoint_gpu_fd_headline_grid(ctx):
+    """The adjoint on the 128 x 128 x 32 headline grid (524,288 parameters),
+    2 steps: central differences (h = 1e-6) of the GPU forward on two seeded
+    cells, one beside the producer, within the noise bound of the module
+    docstring.  The absolute Krylov tolerance is 1e-17 here: on this grid a
+    converged Newton iteration's residual stops near 1e-18, where BiCGstab
+    breaks down before reaching the small grids' 1e-24."""
+    spec = dict(TIGHT, atol=1e-17)
+    case = W.two_phase_case(ni=128, nj=128, nk=32, seed=3, dt=8640.0)
+    dts = [case["dt"]] * 2
+    gs = _sim(ctx, case, case["perm"], spec)
+    J, _ = gs.forward(dts, 1, case["producer"], [0.0, 1.0])
+    grad, _, _, _ = gs.backward(rtol=1e-13)
+    assert np.all(np.isfinite(grad))
+    n = case["ni"] * case["nj"] * case["nk"]
+    cells = [int(case["producer"][0]) + 1, int(np.random.Generator(np.random.PCG64(7)).integers(n))]
+    for e in cells:
+        fd = (_objective(ctx, case, _scaled(case["perm"], e, H), dts, spec) -
+              _objective(ctx, case, _scaled(case["perm"], e, -H), dts, spec)) / (2 * H)
+        assert abs(fd - grad[e]) <= FD_NOISE_H * abs(J) / H + 1e-4 * abs(fd), (e, fd, grad[e], J)
