@@ -250,6 +250,17 @@ rsg_status rsg_mesh_compute_mpfa(rsg_mesh* m, double continuity);
  * reference's two-point alternative, on the GPU: two MD entries per
  * connection, (here, t) and (there, -t), with TPFA's distance weighting. */
 rsg_status rsg_mesh_compute_tpfa(rsg_mesh* m);
+/* L_MPFA.calculateTransmissibilities (geometry/flux/L_MPFA.java:52-74), the
+ * L-method, on the GPU (3-D meshes; RSG_UNSUPPORTED in 2-D): at every
+ * interior corner point each connection takes the L interaction region (its
+ * here or there element and that element's three face neighbours at the
+ * point) whose primary coefficient is smaller in magnitude; boundary points
+ * take a two-point flux over the sub-face.  The reference orders a list's
+ * entries through hash sets; here they follow the corner points in
+ * ascending order, a region's elements primary first.  The discrete adjoint
+ * (rsg_mesh_transmissibility_adjoint, rsg_sim_backward) is not built for
+ * L-method lists and returns RSG_UNSUPPORTED. */
+rsg_status rsg_mesh_compute_lmpfa(rsg_mesh* m);
 /* counts[0] elements, [1] connections, [2] MD entries, [3] corner points,
  * [4] pressure-pattern nnz (valid after MPFA) */
 rsg_status rsg_mesh_get_counts(rsg_mesh* m, int64_t* counts);

@@ -170,7 +170,8 @@ void orc_mesh_destroy(void* h) { delete (Mesh*)h; }
 
 int orc_mesh_mpfa(void* h, double continuity, int tpfa, char* err, int errlen) {
   try {
-    if (tpfa) compute_tpfa(*(Mesh*)h);
+    if (tpfa == 1) compute_tpfa(*(Mesh*)h);
+    else if (tpfa == 2) compute_mpfa_l(*(Mesh*)h);
     else compute_mpfa_o(*(Mesh*)h, continuity);
   } catch (Failure& f) {
     put_err(err, errlen, f.what());

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <set>
 #include <unordered_map>
 
@@ -399,6 +400,8 @@ int neighbour_interface(const Mesh& m, int intf) {
 
 }  // namespace
 
+static void finish_md(Mesh& m, std::vector<std::vector<MDEntry>>& M);
+
 void compute_mpfa_o(Mesh& m, double continuity) {
   if (continuity > 1 || continuity <= 0) throw Failure(ST_BAD_ARG, "continuity must be in (0,1]");
   std::vector<std::vector<MDEntry>> M(m.numConnections());
@@ -503,7 +506,11 @@ void compute_mpfa_o(Mesh& m, double continuity) {
       }
     }
   }
-  // Connection.setDarcyTransmissibilities / check (geometry/Connection.java:61-107)
+  finish_md(m, M);
+}
+
+// Connection.setDarcyTransmissibilities / check (geometry/Connection.java:61-107)
+static void finish_md(Mesh& m, std::vector<std::vector<MDEntry>>& M) {
   for (int c = 0; c < m.numConnections(); ++c) {
     double sum = 0;
     bool hasHere = false, hasThere = false;
@@ -519,6 +526,204 @@ void compute_mpfa_o(Mesh& m, double continuity) {
     for (auto& t : M[c]) t.k *= m.connMult[c];
   }
   m.MD = std::move(M);
+}
+
+namespace {
+
+// MPFA.getHalfEdgePoints (geometry/flux/MPFA.java:165-201): the midpoints of
+// the two edges of interface intf at corner point p, next one first
+void half_edge_points(const Mesh& m, int p, int intf, Vec3& cp1, Vec3& cp2) {
+  const auto& pts = m.interfacePoints[intf];
+  const int n = (int)pts.size();
+  int i = 0;
+  while (i < n && pts[i] != p) ++i;
+  const int j = (i + 1) % n, k = i == 0 ? n - 1 : i - 1;
+  const Vec3 c1 = m.point[p], c2 = m.point[pts[j]], c3 = m.point[pts[k]];
+  cp1 = mul(add(c1, c2), 0.5);
+  cp2 = mul(add(c1, c3), 0.5);
+}
+
+// MPFA.computeSubFaceArea (geometry/flux/MPFA.java:131-160)
+double sub_face_area(const Mesh& m, int intf, int p) {
+  Vec3 c, d;
+  half_edge_points(m, p, intf, c, d);
+  const Vec3 a = m.icenter[intf], b = m.point[p];
+  const Vec3 ab = sub(b, a), ac = sub(c, a), ad = sub(d, a);
+  const double A1 = 0.5 * vnorm(cross(ab, ac));
+  const double A2 = 0.5 * vnorm(cross(ab, ad));
+  return A1 + A2;
+}
+
+// A linear function c1 + c2 x + c3 y + c4 z through four points (one basis
+// function per point, the columns of A^-1; L_MPFA.java:406-447, 659-758)
+struct Basis4 {
+  double c[4][4];  // c[i] = (c1, c2, c3, c4) of basis function i
+  Vec3 grad(int i) const { return {c[i][1], c[i][2], c[i][3]}; }
+  double psi(int i, const Vec3& q) const { return c[i][0] + c[i][1] * q.x + c[i][2] * q.y + c[i][3] * q.z; }
+};
+
+Basis4 basis4(const Vec3* q) {
+  double Ab[16] = {0}, Psi[16] = {0};
+  int piv[4];
+  for (int r = 0; r < 4; ++r) {
+    Ab[r + 0 * 4] = 1;
+    Ab[r + 1 * 4] = q[r].x;
+    Ab[r + 2 * 4] = q[r].y;
+    Ab[r + 3 * 4] = q[r].z;
+  }
+  for (int i = 0; i < 4; ++i) Psi[i + i * 4] = 1;
+  if (dgesv(4, 4, Ab, 4, piv, Psi, 4) != 0) throw Failure(ST_SINGULAR, "Error computing basis functions");
+  Basis4 b;
+  for (int i = 0; i < 4; ++i)
+    for (int r = 0; r < 4; ++r) b.c[i][r] = Psi[r + i * 4];
+  return b;
+}
+
+// LmethodInteractionRegion(p, primary) and calculateT (L_MPFA.java:495-657,
+// 760-866): T (3 x 4, column major) over the region's elements, primary
+// first, then the neighbours across the primary's three interfaces at p, in
+// their order.  prim: the primary's interfaces at p.
+void l_region_T(const Mesh& m, int p, int primary, const std::vector<int>& prim, int* els, double* T) {
+  double A[9] = {0}, B[12] = {0}, C[9] = {0}, D[12] = {0};
+  els[0] = primary;
+  int sec_intf[3];
+  for (int i = 0; i < 3; ++i) {
+    sec_intf[i] = neighbour_interface(m, prim[i]);
+    els[i + 1] = m.interfaceElement[sec_intf[i]];
+  }
+  // primary element: basis through its centre and its three interface centres
+  Vec3 q[4] = {m.ecenter[primary], m.icenter[prim[0]], m.icenter[prim[1]], m.icenter[prim[2]]};
+  const Basis4 pp = basis4(q);
+  for (int i = 0; i < 3; ++i) {
+    const Vec3 kn = kmult(&m.K6[6 * (size_t)primary], normal_area(m, prim[i], p));
+    double f = vdot(kn, pp.grad(0));
+    B[i + 0 * 3] += -f;
+    for (int j = 1; j < 4; ++j) {
+      f = vdot(kn, pp.grad(j));
+      A[i + (j - 1) * 3] += f;
+    }
+  }
+  // secondary elements: basis through the centre, the interface centre, the
+  // corner point and the interface's first half-edge point
+  for (int i = 0; i < 3; ++i) {
+    const int el = els[i + 1], jntf = sec_intf[i];
+    Vec3 e1, e2;
+    half_edge_points(m, p, jntf, e1, e2);
+    Vec3 qs[4] = {m.ecenter[el], m.icenter[jntf], m.point[p], e1};
+    const Basis4 ps = basis4(qs);
+    const Vec3 kn = kmult(&m.K6[6 * (size_t)el], normal_area(m, jntf, p));
+    double f = vdot(kn, ps.grad(0));
+    B[i + (i + 1) * 3] += -f;
+    D[i + (i + 1) * 3] += -f;
+    f = vdot(kn, ps.grad(1));
+    A[i + i * 3] += f;
+    C[i + i * 3] += f;
+    // assembleFullPotentialContribution at the corner point, then the edge point
+    const Vec3 at[2] = {m.point[p], e1};
+    for (int w = 0; w < 2; ++w) {
+      f = vdot(kn, ps.grad(2 + w));
+      double psik = pp.psi(0, at[w]);
+      B[i + 0 * 3] += -f * psik;
+      D[i + 0 * 3] += -f * psik;
+      for (int k = 1; k < 4; ++k) {
+        psik = pp.psi(k, at[w]);
+        A[i + (k - 1) * 3] += f * psik;
+        C[i + (k - 1) * 3] += f * psik;
+      }
+    }
+  }
+  // MPFA.calculateTmatrix: T = C (A \ B) - D
+  double AiB[12];
+  int piv[3];
+  for (int a = 0; a < 12; ++a) AiB[a] = B[a];
+  if (dgesv(3, 4, A, 3, piv, AiB, 3) != 0)
+    throw Failure(ST_SINGULAR, "Conductivity tensor does not appear to be symmetrical, positive definite");
+  for (int a = 0; a < 12; ++a) T[a] = D[a] * -1;
+  dgemm_nn_add(3, 4, 3, C, 3, AiB, 3, T, 3);
+}
+
+void md_add(std::vector<MDEntry>& Mi, int el, double tk, bool keep_zero) {
+  for (auto& tp : Mi)
+    if (tp.element == el) {
+      tp.k += tk;
+      return;
+    }
+  if (tk != 0 || keep_zero) Mi.push_back({el, tk});
+}
+
+}  // namespace
+
+// L_MPFA.calculateTransmissibilities (geometry/flux/L_MPFA.java:52-74) on
+// 3-D hexahedral meshes.  The reference iterates a point's connections and a
+// region's elements through hash sets, whose order Java leaves open; here
+// connections go in ascending index and a region's elements primary first,
+// which fixes the order of each MD list (the values do not depend on it).
+void compute_mpfa_l(Mesh& m) {
+  if (m.dim != 3) throw Failure(ST_UNSUPPORTED, "the L-method is built for 3-D hexahedral meshes");
+  std::vector<std::vector<MDEntry>> M(m.numConnections());
+  for (int p = 0; p < m.numPoints(); ++p) {
+    const auto& pints = m.pointInterfaces[p];
+    bool onBoundary = false;
+    std::set<int> conns;
+    for (int f : pints) {
+      if (m.iboundary[f]) onBoundary = true;
+      else conns.insert(m.interfaceConnection[f]);
+    }
+    if (onBoundary) {
+      // calculateBoundaryTransmissibilities (:77-126): two-point fluxes over
+      // the sub-faces at p, with TPFA's distance weighting
+      for (int c : conns) {
+        const int is = m.connHereIntf[c], js = m.connThereIntf[c];
+        const int ei = m.interfaceElement[is], ej = m.interfaceElement[js];
+        const Vec3 ki = kmult(&m.K6[6 * (size_t)ei], m.inormal[is]);
+        const Vec3 kj = kmult(&m.K6[6 * (size_t)ej], m.inormal[js]);
+        const double Kin = std::sqrt(ki.x * ki.x + ki.y * ki.y + ki.z * ki.z);
+        const double Kjn = std::sqrt(kj.x * kj.x + kj.y * kj.y + kj.z * kj.z);
+        const double A = sub_face_area(m, is, p);
+        double t = 0;
+        if (Kin != 0 && Kjn != 0)
+          t = Kin * Kjn * A /
+              (Kjn * vnorm(sub(m.icenter[is], m.ecenter[ei])) + Kjn * vnorm(sub(m.icenter[js], m.ecenter[ej])));
+        md_add(M[c], m.connHere[c], t, false);
+        md_add(M[c], m.connThere[c], -t, false);
+      }
+      continue;
+    }
+    // getElementInterfaces: each element's interfaces at p, in p's order
+    std::map<int, std::vector<int>> elIntf;
+    for (int el : m.pointElements[p]) elIntf[el];
+    for (int f : pints) elIntf[m.interfaceElement[f]].push_back(f);
+    for (int c : conns) {
+      const int here = m.connHere[c], there = m.connThere[c], hi = m.connHereIntf[c];
+      const int nuHere = (int)elIntf[here].size(), nuThere = (int)elIntf[there].size();
+      int prim[2], np = 0;
+      if (nuHere == 3) prim[np++] = here;
+      if (nuThere == 3) prim[np++] = there;
+      if (np == 0) throw Failure(ST_BAD_ARG, "Illegal local vertex degree for point");
+      int els[2][4], row[2];
+      double T[2][12];
+      for (int r = 0; r < np; ++r) {
+        const auto& pi = elIntf[prim[r]];
+        l_region_T(m, p, prim[r], pi, els[r], T[r]);
+        // the row of c's here interface: the primary's interface or its neighbour
+        row[r] = -1;
+        for (int i = 0; i < 3; ++i)
+          if (pi[i] == hi || neighbour_interface(m, pi[i]) == hi) row[r] = i;
+      }
+      // chooseTransmissibilities (:170-212): the smaller |t| of the primary's
+      // coefficient on c's sub-face; the second candidate on a tie
+      int pick = 0;
+      if (np == 2) pick = std::fabs(T[0][row[0]]) < std::fabs(T[1][row[1]]) ? 0 : 1;
+      // storeLTransmissibilities (:218-249)
+      for (int j = 0; j < 4; ++j) {
+        const int el = els[pick][j];
+        double tk = T[pick][row[pick] + j * 3];
+        if (prim[pick] == here) tk *= -1;
+        md_add(M[c], el, tk, el == here || el == there);
+      }
+    }
+  }
+  finish_md(m, M);
 }
 
 void compute_tpfa(Mesh& m) {

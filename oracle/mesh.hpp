@@ -67,6 +67,11 @@ Mesh build_structured_mesh(int dim, int ni, int nj, int nk, const double* coords
 // Connection.setDarcyTransmissibilities for every neighbour connection.
 void compute_mpfa_o(Mesh& mesh, double continuity);
 
+// L_MPFA.calculateTransmissibilities (geometry/flux/L_MPFA.java:52-74, the
+// L-method of L interaction regions with a two-point flux on boundary
+// points), 3-D, then Connection.setDarcyTransmissibilities.
+void compute_mpfa_l(Mesh& mesh);
+
 // TPFA (geometry/flux/TPFA.java:50-72), including its quirk of using the
 // "there" normal conductivity twice in the harmonic mean.
 void compute_tpfa(Mesh& mesh);

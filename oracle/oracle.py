@@ -197,9 +197,10 @@ class Mesh:
             lib().orc_mesh_destroy(self.h)
             self.h = None
 
-    def mpfa(self, continuity=1.0, tpfa=False):
+    def mpfa(self, continuity=1.0, tpfa=False, lmethod=False):
+        """O-method MPFA (default), TPFA, or the L-method (3-D)."""
         err = C.create_string_buffer(512)
-        st = lib().orc_mesh_mpfa(self.h, continuity, int(tpfa), err, 512)
+        st = lib().orc_mesh_mpfa(self.h, continuity, 2 if lmethod else int(tpfa), err, 512)
         if st != 0:
             raise OracleError(st, err.value.decode())
 

@@ -106,6 +106,7 @@ def _declare(L):
         "rsg_mesh_get_transmissibilities": (i32, [vp, P(i32), P(i32), P(d)]),
         "rsg_mesh_get_pattern": (i32, [vp, i32, P(i32), P(i32), P(i64)]),
         "rsg_mesh_assemble_potential": (i32, [vp, vp]),
+        "rsg_mesh_compute_lmpfa": (i32, [vp]),
         "rsg_mesh_connection_flux": (i32, [vp, P(d), P(d)]),
         "rsg_mesh_get_interface_centers": (i32, [vp, P(d)]),
         "rsg_upscale_pressure": (i32, [vp, i32, P(i32), P(d), P(d), P(abi.rsg_solve_info)]),
@@ -462,6 +463,10 @@ class Mesh:
     def compute_tpfa(self):
         """TPFA.calculateTransmissibilities: the two-point alternative to MPFA-O."""
         self.ctx.check(lib().rsg_mesh_compute_tpfa(self.h), "compute_tpfa")
+
+    def compute_lmpfa(self):
+        """L_MPFA.calculateTransmissibilities: the L-method (3-D)."""
+        self.ctx.check(lib().rsg_mesh_compute_lmpfa(self.h), "compute_lmpfa")
 
     def counts(self):
         c = (C.c_int64 * 5)()

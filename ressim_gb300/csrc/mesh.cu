@@ -786,6 +786,288 @@ __global__ void k_mpfa_gather(Grid g, int maxmd, const double* __restrict__ Tsto
   }
 }
 
+// ------------------------------------------------------------ L-method ----
+// MPFA.getHalfEdgePoints (MPFA.java:165-201) for the face at position f of
+// point p: the midpoints of the face's two edges at p, the one towards the
+// next point of the face's circular point list first.
+__device__ void half_edge_points(const Grid& g, const PointTopo& t, int f, int p, const double* pts, V3& e1,
+                                 V3& e2) {
+  int cp[8], ip[4];
+  const int a = t.fel[f];
+  elem_points(g, t.eijk[a][0], t.eijk[a][1], t.eijk[a][2], cp);
+  face_points(g, cp, t.fo[f], ip);
+  int i = 0;
+  for (int q = 0; q < 4; ++q)
+    if (ip[q] == p) {
+      i = q;
+      break;
+    }
+  const V3 c1 = ld3(pts, p), c2 = ld3(pts, ip[(i + 1) % 4]), c3 = ld3(pts, ip[i == 0 ? 3 : i - 1]);
+  e1 = vmul(vadd(c1, c2), 0.5);
+  e2 = vmul(vadd(c1, c3), 0.5);
+}
+
+// position in t of the face across face position f (the other side of its connection)
+__device__ int across(const Grid& g, const PointTopo& t, int f) {
+  const int a = t.fel[f];
+  int ne_, no_;
+  if (!face_neighbour(g, t.eijk[a][0], t.eijk[a][1], t.eijk[a][2], t.fo[f], ne_, no_)) return -1;
+  const int nb = ne_ * (g.dim == 3 ? 6 : 4) + no_;
+  for (int q = 0; q < t.nf; ++q)
+    if (t.face[q] == nb) return q;
+  return -1;
+}
+
+// Linear basis functions through four points: column i of A^-1 holds
+// c1..c4 of the function that is 1 at point i (L_MPFA.java:406-447, 659-758)
+__device__ bool basis4(const V3* q, double* Psi) {
+  double Ab[16];
+  for (int r = 0; r < 4; ++r) {
+    Ab[r] = 1;
+    Ab[r + 4] = q[r].x;
+    Ab[r + 8] = q[r].y;
+    Ab[r + 12] = q[r].z;
+  }
+  for (int k = 0; k < 16; ++k) Psi[k] = 0;
+  for (int i = 0; i < 4; ++i) Psi[i + i * 4] = 1;
+  return d_dgesv(4, 4, Ab, 4, Psi, 4) == 0;
+}
+__device__ __forceinline__ V3 bgrad(const double* Psi, int i) { return {Psi[1 + i * 4], Psi[2 + i * 4], Psi[3 + i * 4]}; }
+__device__ __forceinline__ double bval(const double* Psi, int i, V3 x) {
+  return Psi[0 + i * 4] + Psi[1 + i * 4] * x.x + Psi[2 + i * 4] * x.y + Psi[3 + i * 4] * x.z;
+}
+__device__ __forceinline__ V3 kmult6(const double* K, V3 v) {
+  return {K[0] * v.x + K[3] * v.y + K[4] * v.z, K[3] * v.x + K[1] * v.y + K[5] * v.z,
+          K[4] * v.x + K[5] * v.y + K[2] * v.z};
+}
+
+// L_MPFA per interior corner point of a 3-D grid: for each of the 8 elements
+// at the point, the T matrix (3 x 4, column major, at slot 12 a) of its L
+// interaction region (LmethodInteractionRegion.calculateT, L_MPFA.java:580-657
+// and 760-866): rows are the element's faces at the point in the point's
+// face order, columns the element, then the elements across those faces.
+// Boundary points keep no T (their sub-faces take a two-point flux).
+__global__ void __launch_bounds__(128) k_lmpfa_point(Grid g, const double* __restrict__ pts,
+                                                     const double* __restrict__ perm,
+                                                     const double* __restrict__ ecenter,
+                                                     const double* __restrict__ icenter,
+                                                     const double* __restrict__ inormal,
+                                                     const double* __restrict__ iarea, double* __restrict__ Tstore,
+                                                     int* flag) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  PointTopo t;
+  point_topology(g, p, t);
+  for (int f = 0; f < t.nf; ++f)
+    if (t.boundary[f]) return;
+  const V3 corner = ld3(pts, p);
+  for (int a = 0; a < t.ne; ++a) {
+    const int el = t.el[a], f0 = 3 * a;
+    double A[9] = {0}, B[12] = {0}, C[9] = {0}, D[12] = {0}, Pp[16], Ps[16];
+    // primary: basis through its centre and its three face centres
+    V3 q[4] = {ld3(ecenter, el), ld3(icenter, t.face[f0]), ld3(icenter, t.face[f0 + 1]), ld3(icenter, t.face[f0 + 2])};
+    if (!basis4(q, Pp)) {
+      atomicCAS(flag, 0, 1);
+      return;
+    }
+    for (int i = 0; i < 3; ++i) {
+      const V3 kn = kmult6(perm + 6 * (int64_t)el, normal_area(g, t, f0 + i, p, pts, inormal, iarea));
+      double fl = vdot(kn, bgrad(Pp, 0));
+      B[i] += -fl;
+      for (int j = 1; j < 4; ++j) {
+        fl = vdot(kn, bgrad(Pp, j));
+        A[i + (j - 1) * 3] += fl;
+      }
+    }
+    // secondaries: basis through the centre, the face centre, the corner
+    // point and the face's first half-edge point
+    for (int i = 0; i < 3; ++i) {
+      const int fs = across(g, t, f0 + i);
+      if (fs < 0) {
+        atomicCAS(flag, 0, 5);
+        return;
+      }
+      const int es = t.el[t.fel[fs]];
+      V3 e1, e2;
+      half_edge_points(g, t, fs, p, pts, e1, e2);
+      V3 qs[4] = {ld3(ecenter, es), ld3(icenter, t.face[fs]), corner, e1};
+      if (!basis4(qs, Ps)) {
+        atomicCAS(flag, 0, 1);
+        return;
+      }
+      const V3 kn = kmult6(perm + 6 * (int64_t)es, normal_area(g, t, fs, p, pts, inormal, iarea));
+      double fl = vdot(kn, bgrad(Ps, 0));
+      B[i + (i + 1) * 3] += -fl;
+      D[i + (i + 1) * 3] += -fl;
+      fl = vdot(kn, bgrad(Ps, 1));
+      A[i + i * 3] += fl;
+      C[i + i * 3] += fl;
+      const V3 at[2] = {corner, e1};
+      for (int w = 0; w < 2; ++w) {
+        fl = vdot(kn, bgrad(Ps, 2 + w));
+        double psik = bval(Pp, 0, at[w]);
+        B[i] += -fl * psik;
+        D[i] += -fl * psik;
+        for (int k = 1; k < 4; ++k) {
+          psik = bval(Pp, k, at[w]);
+          A[i + (k - 1) * 3] += fl * psik;
+          C[i + (k - 1) * 3] += fl * psik;
+        }
+      }
+    }
+    // T = C (A \ B) - D (MPFA.java:43-54)
+    if (d_dgesv(3, 4, A, 3, B, 3) != 0) {
+      atomicCAS(flag, 0, 2);
+      return;
+    }
+    double* T = Tstore + (int64_t)p * TSZ + 12 * a;
+    for (int k = 0; k < 12; ++k) T[k] = D[k] * -1;
+    for (int j = 0; j < 4; ++j)
+      for (int l = 0; l < 3; ++l) {
+        const double bl = B[l + j * 3];
+        if (bl != 0.0) {
+          const double temp = 1.0 * bl;
+          for (int i = 0; i < 3; ++i) T[i + j * 3] += temp * C[i + l * 3];
+        }
+      }
+  }
+}
+
+// The L-method's MD lists gathered per connection over its corner points in
+// ascending point order: at an interior point the L region (here or there
+// element as primary) whose primary coefficient on the connection's sub-face
+// is smaller in magnitude, the second on a tie (chooseTransmissibilities,
+// L_MPFA.java:170-212), stored with storeLTransmissibilities' sign and
+// zero rules (:218-249); at a boundary point the two-point flux over the
+// sub-face (calculateBoundaryTransmissibilities, :77-126).  Then
+// Connection.check.
+__global__ void k_lmpfa_gather(Grid g, int maxmd, const double* __restrict__ Tstore, const int* __restrict__ conn,
+                               const double* __restrict__ pts, const double* __restrict__ perm,
+                               const double* __restrict__ ecenter, const double* __restrict__ icenter,
+                               const double* __restrict__ inormal, int* md_len, int* md_elem, double* md_k,
+                               int* flag) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nconn) return;
+  const int here = conn[2 * c], there = conn[2 * c + 1];
+  int i, j, k;
+  el_ijk(g, here, i, j, k);
+  int o = -1, ot = -1;
+  for (int q = 1; q < 6; q += 2) {
+    int ne_, no_;
+    if (face_neighbour(g, i, j, k, q, ne_, no_) && ne_ == there) {
+      o = q;
+      ot = no_;
+      break;
+    }
+  }
+  const int fh = here * 6 + o, ft = there * 6 + ot;
+  int cp[8], ip[4];
+  elem_points(g, i, j, k, cp);
+  face_points(g, cp, o, ip);
+  for (int a = 1; a < 4; ++a)
+    for (int b = a; b > 0 && ip[b] < ip[b - 1]; --b) {
+      const int tmp = ip[b];
+      ip[b] = ip[b - 1];
+      ip[b - 1] = tmp;
+    }
+  int el[18];
+  double kk[18];
+  int n = 0;
+  auto add = [&](int e, double tk, bool keep) {
+    for (int q = 0; q < n; ++q)
+      if (el[q] == e) {
+        kk[q] += tk;
+        return true;
+      }
+    if (tk != 0 || keep) {
+      if (n >= maxmd) return false;
+      el[n] = e;
+      kk[n] = tk;
+      n++;
+    }
+    return true;
+  };
+  PointTopo t;
+  for (int a = 0; a < 4; ++a) {
+    const int p = ip[a];
+    point_topology(g, p, t);
+    bool onb = false;
+    for (int f = 0; f < t.nf; ++f) onb |= t.boundary[f] != 0;
+    int ph = -1, pt = -1;
+    for (int f = 0; f < t.nf; ++f) {
+      if (t.face[f] == fh) ph = f;
+      if (t.face[f] == ft) pt = f;
+    }
+    if (ph < 0 || pt < 0) {
+      atomicCAS(flag, 0, 5);
+      return;
+    }
+    if (onb) {
+      const V3 ki = kmult6(perm + 6 * (int64_t)here, ld3(inormal, fh));
+      const V3 kj = kmult6(perm + 6 * (int64_t)there, ld3(inormal, ft));
+      const double Kin = sqrt(ki.x * ki.x + ki.y * ki.y + ki.z * ki.z);
+      const double Kjn = sqrt(kj.x * kj.x + kj.y * kj.y + kj.z * kj.z);
+      // MPFA.computeSubFaceArea (MPFA.java:131-160)
+      V3 e1, e2;
+      half_edge_points(g, t, ph, p, pts, e1, e2);
+      const V3 fa = ld3(icenter, fh), fb = ld3(pts, p);
+      const V3 ab = vsub(fb, fa), ac = vsub(e1, fa), ad = vsub(e2, fa);
+      const double A1 = 0.5 * vnorm(vcross(ab, ac));
+      const double A2 = 0.5 * vnorm(vcross(ab, ad));
+      const double A = A1 + A2;
+      double tt = 0;
+      if (Kin != 0 && Kjn != 0)
+        tt = Kin * Kjn * A /
+             (Kjn * vnorm(vsub(fa, ld3(ecenter, here))) + Kjn * vnorm(vsub(ld3(icenter, ft), ld3(ecenter, there))));
+      if (!add(here, tt, false) || !add(there, -tt, false)) {
+        atomicCAS(flag, 0, 3);
+        return;
+      }
+      continue;
+    }
+    // the two candidate regions: here and there element as primary; the
+    // sub-face's row is the primary's own face on the connection
+    const int aH = t.fel[ph], aT = t.fel[pt];
+    const int rH = ph - 3 * aH, rT = pt - 3 * aT;
+    const double* TH = Tstore + (int64_t)p * TSZ + 12 * aH;
+    const double* TT = Tstore + (int64_t)p * TSZ + 12 * aT;
+    const bool pickH = fabs(TH[rH]) < fabs(TT[rT]);
+    const int ap = pickH ? aH : aT, row = pickH ? rH : rT;
+    const double* T = pickH ? TH : TT;
+    const int prim = t.el[ap];
+    for (int jj = 0; jj < 4; ++jj) {
+      int e = prim;
+      if (jj > 0) {
+        const int fs = across(g, t, 3 * ap + jj - 1);
+        if (fs < 0) {
+          atomicCAS(flag, 0, 5);
+          return;
+        }
+        e = t.el[t.fel[fs]];
+      }
+      double tk = T[row + jj * 3];
+      if (prim == here) tk *= -1;
+      if (!add(e, tk, e == here || e == there)) {
+        atomicCAS(flag, 0, 3);
+        return;
+      }
+    }
+  }
+  double sum = 0;
+  bool hasHere = false, hasThere = false;
+  for (int q = 0; q < n; ++q) {
+    sum += kk[q];
+    hasHere |= el[q] == here;
+    hasThere |= el[q] == there;
+  }
+  if (fabs(sum) > 1.0e-6 || !hasHere || !hasThere) atomicCAS(flag, 0, 4);
+  md_len[c] = n;
+  for (int q = 0; q < n; ++q) {
+    md_elem[(int64_t)c * maxmd + q] = el[q];
+    md_k[(int64_t)c * maxmd + q] = kk[q] * 1.0;  // connection multiplier (1 on structured grids)
+  }
+}
+
 __global__ void k_md_compact(int nconn, int maxmd, const int* __restrict__ ptr, const int* __restrict__ el_in,
                              const double* __restrict__ k_in, int* el_out, double* k_out) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1014,9 +1296,44 @@ static void scan_lengths(const std::vector<int>& len, std::vector<int>& ptr) {
   for (size_t i = 0; i < len.size(); ++i) ptr[i + 1] = ptr[i] + len[i];
 }
 
+// MD lists gathered per connection (fixed stride maxmd) into the mesh's CSR
+// form, after the gather kernel's status flag is checked
+static void install_md(Mesh& m, DeviceBuffer<int>& flag, DeviceBuffer<int>& mdlen, DeviceBuffer<int>& mdel,
+                       DeviceBuffer<double>& mdk) {
+  Context& c = *m.ctx;
+  const Grid& g = m.g;
+  int hf = 0;
+  std::vector<int> hl(g.nconn);
+  RSG_CUDA(cudaMemcpyAsync(&hf, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  if (g.nconn > 0)
+    RSG_CUDA(cudaMemcpyAsync(hl.data(), mdlen.get(), sizeof(int) * g.nconn, cudaMemcpyDeviceToHost, c.stream));
+  c.sync();
+  if (hf == 1) throw Error(RSG_SINGULAR, "Severe grid distortion (singular basis system)");
+  if (hf == 2) throw Error(RSG_SINGULAR, "Conductivity tensor does not appear to be symmetrical, positive definite");
+  if (hf == 3) throw Error(RSG_BAD_ARG, "too many transmissibilities on a connection");
+  if (hf == 4) throw Error(RSG_BAD_ARG, "Transmissibilities on a connection fail the consistency check");
+  if (hf == 5) throw Error(RSG_BAD_ARG, "interaction region lookup failed");
+  scan_lengths(hl, m.h_md_ptr);
+  m.nmd = m.h_md_ptr[g.nconn];
+  m.md_ptr.resize(g.nconn + 1);
+  m.md_elem.resize(std::max<int64_t>(m.nmd, 1));
+  m.md_k.resize(std::max<int64_t>(m.nmd, 1));
+  RSG_CUDA(cudaMemcpyAsync(m.md_ptr.get(), m.h_md_ptr.data(), sizeof(int) * (g.nconn + 1), cudaMemcpyHostToDevice,
+                           c.stream));
+  RSG_LAUNCH(c, "md_compact", k_md_compact, blocks_for(std::max(g.nconn, 1), 256), 256, 0, g.nconn, m.maxmd,
+             m.md_ptr.get(), mdel.get(), mdk.get(), m.md_elem.get(), m.md_k.get());
+  m.h_md_elem.resize(m.nmd);
+  RSG_CUDA(cudaMemcpyAsync(m.h_md_elem.data(), m.md_elem.get(), sizeof(int) * m.nmd, cudaMemcpyDeviceToHost,
+                           c.stream));
+  c.sync();
+  m.have_md = true;
+  m.build_patterns();
+}
+
 void mpfa_adjoint(Mesh& m, int npairs, const double* mu, const double* phi, double scale, bool accumulate,
                   double* out) {
   if (!m.have_md) throw Error(RSG_BAD_ARG, "transmissibilities have not been computed");
+  if (m.lmethod) throw Error(RSG_UNSUPPORTED, "the adjoint is built for MPFA-O and TPFA transmissibilities");
   Context& c = *m.ctx;
   const Grid& g = m.g;
   if (m.tpfa) {
@@ -1162,32 +1479,32 @@ rsg_status rsg_mesh_compute_mpfa(rsg_mesh* mh, double continuity) {
                m.ecenter.get(), m.icenter.get(), m.inormal.get(), m.iarea.get(), continuity, T.get(), flag.get());
     RSG_LAUNCH(c, "mpfa_gather", rsg::k_mpfa_gather, rsg::blocks_for(g.nconn, 128), 128, 0, g, m.maxmd, T.get(),
                m.conn.get(), mdlen.get(), mdel.get(), mdk.get(), flag.get());
-    int hf = 0;
-    std::vector<int> hl(g.nconn);
-    RSG_CUDA(cudaMemcpyAsync(&hf, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    RSG_CUDA(cudaMemcpyAsync(hl.data(), mdlen.get(), sizeof(int) * g.nconn, cudaMemcpyDeviceToHost, c.stream));
-    c.sync();
-    if (hf == 1) throw rsg::Error(RSG_SINGULAR, "Severe grid distortion (singular basis system)");
-    if (hf == 2) throw rsg::Error(RSG_SINGULAR, "Conductivity tensor does not appear to be symmetrical, positive definite");
-    if (hf == 3) throw rsg::Error(RSG_BAD_ARG, "too many transmissibilities on a connection");
-    if (hf == 4) throw rsg::Error(RSG_BAD_ARG, "Transmissibilities on a connection fail the consistency check");
-    if (hf == 5) throw rsg::Error(RSG_BAD_ARG, "interaction region lookup failed");
-    rsg::scan_lengths(hl, m.h_md_ptr);
-    m.nmd = m.h_md_ptr[g.nconn];
-    m.md_ptr.resize(g.nconn + 1);
-    m.md_elem.resize(std::max<int64_t>(m.nmd, 1));
-    m.md_k.resize(std::max<int64_t>(m.nmd, 1));
-    RSG_CUDA(cudaMemcpyAsync(m.md_ptr.get(), m.h_md_ptr.data(), sizeof(int) * (g.nconn + 1), cudaMemcpyHostToDevice,
-                             c.stream));
-    RSG_LAUNCH(c, "md_compact", rsg::k_md_compact, rsg::blocks_for(g.nconn, 256), 256, 0, g.nconn, m.maxmd,
-               m.md_ptr.get(), mdel.get(), mdk.get(), m.md_elem.get(), m.md_k.get());
-    m.h_md_elem.resize(m.nmd);
-    RSG_CUDA(cudaMemcpyAsync(m.h_md_elem.data(), m.md_elem.get(), sizeof(int) * m.nmd, cudaMemcpyDeviceToHost,
-                             c.stream));
-    c.sync();
-    m.have_md = true;
+    rsg::install_md(m, flag, mdlen, mdel, mdk);
     m.tpfa = false;
-    m.build_patterns();
+    m.lmethod = false;
+  });
+}
+
+// L_MPFA.calculateTransmissibilities (geometry/flux/L_MPFA.java:52-74) on the GPU
+rsg_status rsg_mesh_compute_lmpfa(rsg_mesh* mh) {
+  if (!mh) return RSG_BAD_ARG;
+  rsg::Mesh& m = mh->m;
+  if (m.g.dim != 3) return RSG_UNSUPPORTED;
+  return guarded(m.ctx, [&] {
+    rsg::Context& c = *m.ctx;
+    const rsg::Grid& g = m.g;
+    rsg::DeviceBuffer<double> T((size_t)g.npts * rsg::TSZ);
+    rsg::DeviceBuffer<int> flag(1), mdlen(g.nconn), mdel((size_t)g.nconn * m.maxmd);
+    rsg::DeviceBuffer<double> mdk((size_t)g.nconn * m.maxmd);
+    RSG_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), c.stream));
+    RSG_LAUNCH(c, "lmpfa_point", rsg::k_lmpfa_point, rsg::blocks_for(g.npts, 128), 128, 0, g, m.pts.get(),
+               m.perm.get(), m.ecenter.get(), m.icenter.get(), m.inormal.get(), m.iarea.get(), T.get(), flag.get());
+    RSG_LAUNCH(c, "lmpfa_gather", rsg::k_lmpfa_gather, rsg::blocks_for(std::max(g.nconn, 1), 128), 128, 0, g,
+               m.maxmd, T.get(), m.conn.get(), m.pts.get(), m.perm.get(), m.ecenter.get(), m.icenter.get(),
+               m.inormal.get(), mdlen.get(), mdel.get(), mdk.get(), flag.get());
+    rsg::install_md(m, flag, mdlen, mdel, mdk);
+    m.tpfa = false;
+    m.lmethod = true;
   });
 }
 
@@ -1213,6 +1530,7 @@ rsg_status rsg_mesh_compute_tpfa(rsg_mesh* mh) {
     c.sync();
     m.have_md = true;
     m.tpfa = true;
+    m.lmethod = false;
     m.build_patterns();
   });
 }

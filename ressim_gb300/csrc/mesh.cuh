@@ -28,6 +28,7 @@ struct Mesh {
   bool have_md = false;
   double continuity = 1.0;           // continuity point used by the last MPFA-O computation
   bool tpfa = false;                 // MD lists from the two-point approximation
+  bool lmethod = false;              // MD lists from the L-method
   // pressure pattern (LinearSolver) and potential pattern (PotentialCalculator)
   std::vector<int> h_prow, h_pcol, h_qrow, h_qcol;
   // per MD entry: CSR position in the here row and in the there row of the
