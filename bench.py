@@ -117,7 +117,7 @@ def build_case(args):
 # one ncu capture of this workload (dram__bytes_read.sum +
 # dram__bytes_write.sum); keyed by grid size and kernel family.  ncu cannot
 # run inside the timed benchmark, so the line labels these as a capture's.
-NCU_TRAFFIC = {(128, 128, 32): {"ilu_lower": 91_788_288, "ilu_upper": 95_744_256}}
+NCU_TRAFFIC = {(128, 128, 32): {"ilu_lower": 103_740_416, "ilu_upper": 107_909_632}}
 NCU_TRAFFIC_SOURCE = "ncu capture of the same kernel on the same workload (not measured in this run)"
 
 
@@ -840,8 +840,8 @@ def main():
                     help="cells of the Peng-Robinson flash leg (0: skip)")
     ap.add_argument("--comp-steps", type=int, default=1, help="timed steps of the compositional leg (0: skip)")
     ap.add_argument("--comp-grid", type=int, nargs=3, default=[64, 64, 16])
-    ap.add_argument("--adj-steps", type=int, default=4, help="steps of the adjoint leg (0: skip)")
-    ap.add_argument("--adj-every", type=int, default=2, help="adjoint leg: steps per checkpoint")
+    ap.add_argument("--adj-steps", type=int, default=50, help="steps of the adjoint leg (0: skip)")
+    ap.add_argument("--adj-every", type=int, default=10, help="adjoint leg: steps per checkpoint")
     ap.add_argument("--adj-rtol", type=float, default=1e-8, help="adjoint leg: transposed-solve tolerance")
     ap.add_argument("--inner", type=float, nargs=2, default=[10, 1e-3],
                     help="mixed solver: FP32 inner iterations and inner relative tolerance")
