@@ -1,5 +1,5 @@
 """The JNI shim (ressim_gb300/jni/rsg_jni.c) compiles against include/rsg.h,
-and INTEGRATION.md quotes it verbatim.  There is no JDK here, so a minimal
+and the integration guide quotes it verbatim.  There is no JDK here, so a minimal
 stand-in declares the few JNI types and JNIEnv functions the shim uses (with
 the JNI specification's signatures); the check is that the shim's calls into
 the C ABI match the header."""
