@@ -10,6 +10,7 @@
  */
 #include <jni.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "rsg.h"
 
@@ -70,5 +71,76 @@ JNIEXPORT jint JNICALL Java_no_uib_cipr_rs_gpu_RsgNative_simStep(JNIEnv* env, jc
   rsg_step_info info;
   rsg_status st = rsg_sim_step((rsg_sim*)(intptr_t)sim, dt, &info);
   (*env)->SetIntArrayRegion(env, newton, 0, 1, &info.newton_iterations);
+  return st;
+}
+
+/* Several fields stepped together (one persistent pressure-solver launch per
+ * Newton iteration); sims: handles, dt: one step length per field; per field
+ * newton[i] and statuses[i]. */
+JNIEXPORT jint JNICALL Java_no_uib_cipr_rs_gpu_RsgNative_ensembleStepBatched(JNIEnv* env, jclass cls,
+                                                                            jlongArray sims, jdoubleArray dt,
+                                                                            jint precision, jintArray newton,
+                                                                            jintArray statuses) {
+  (void)cls;
+  const jint count = (*env)->GetArrayLength(env, sims);
+  if (count <= 0) return RSG_BAD_ARG;
+  rsg_sim** hs = malloc(sizeof(rsg_sim*) * (size_t)count);
+  rsg_step_info* infos = malloc(sizeof(rsg_step_info) * (size_t)count);
+  int32_t* sts = malloc(sizeof(int32_t) * (size_t)count);
+  rsg_status st = RSG_BAD_ARG;
+  if (hs && infos && sts) {
+    jlong* ph = (*env)->GetPrimitiveArrayCritical(env, sims, 0);
+    for (jint i = 0; i < count; ++i) hs[i] = (rsg_sim*)(intptr_t)ph[i];
+    (*env)->ReleasePrimitiveArrayCritical(env, sims, ph, JNI_ABORT);
+    double* pdt = (*env)->GetPrimitiveArrayCritical(env, dt, 0);
+    st = rsg_ensemble_step_batched(count, hs, pdt, precision, infos, sts);
+    (*env)->ReleasePrimitiveArrayCritical(env, dt, pdt, JNI_ABORT);
+    for (jint i = 0; i < count; ++i) {
+      jint nt = infos[i].newton_iterations, s = sts[i];
+      (*env)->SetIntArrayRegion(env, newton, i, 1, &nt);
+      (*env)->SetIntArrayRegion(env, statuses, i, 1, &s);
+    }
+  }
+  free(hs);
+  free(infos);
+  free(sts);
+  return st;
+}
+
+/* L_MPFA.calculateTransmissibilities(mesh, K) in place of O_MPFA's */
+JNIEXPORT jint JNICALL Java_no_uib_cipr_rs_gpu_RsgNative_meshComputeLmpfa(JNIEnv* env, jclass cls, jlong mesh) {
+  (void)env;
+  (void)cls;
+  return rsg_mesh_compute_lmpfa((rsg_mesh*)(intptr_t)mesh);
+}
+
+/* new PressureDiscretisation(mesh, bc).getSolution(): bc as parallel arrays
+ * of element indices and pressures; x receives the solution */
+JNIEXPORT jint JNICALL Java_no_uib_cipr_rs_gpu_RsgNative_upscalePressure(JNIEnv* env, jclass cls, jlong mesh,
+                                                                        jintArray cells, jdoubleArray values,
+                                                                        jdoubleArray x, jintArray iters) {
+  (void)cls;
+  rsg_solve_info info;
+  const jint nbc = (*env)->GetArrayLength(env, cells);
+  jint* pc = (*env)->GetPrimitiveArrayCritical(env, cells, 0);
+  double* pv = (*env)->GetPrimitiveArrayCritical(env, values, 0);
+  double* px = (*env)->GetPrimitiveArrayCritical(env, x, 0);
+  rsg_status st = rsg_upscale_pressure((rsg_mesh*)(intptr_t)mesh, nbc, (const int32_t*)pc, pv, px, &info);
+  (*env)->ReleasePrimitiveArrayCritical(env, x, px, 0);
+  (*env)->ReleasePrimitiveArrayCritical(env, values, pv, JNI_ABORT);
+  (*env)->ReleasePrimitiveArrayCritical(env, cells, pc, JNI_ABORT);
+  (*env)->SetIntArrayRegion(env, iters, 0, 1, &info.iterations);
+  return st;
+}
+
+/* LocalFlowRateAverage.computeDarcyFlux: flux[c] = sum_k t_k p[k] per connection */
+JNIEXPORT jint JNICALL Java_no_uib_cipr_rs_gpu_RsgNative_connectionFlux(JNIEnv* env, jclass cls, jlong mesh,
+                                                                       jdoubleArray p, jdoubleArray flux) {
+  (void)cls;
+  double* pp = (*env)->GetPrimitiveArrayCritical(env, p, 0);
+  double* pf = (*env)->GetPrimitiveArrayCritical(env, flux, 0);
+  rsg_status st = rsg_mesh_connection_flux((rsg_mesh*)(intptr_t)mesh, pp, pf);
+  (*env)->ReleasePrimitiveArrayCritical(env, flux, pf, 0);
+  (*env)->ReleasePrimitiveArrayCritical(env, p, pp, JNI_ABORT);
   return st;
 }
