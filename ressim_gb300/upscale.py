@@ -250,7 +250,8 @@ class StructuredUpscaler:
     """Upscaling of a structured fine grid (dim 2 or 3, ni x nj x nk cells,
     corner coordinates in linear point order, 6 permeability components per
     cell) over the coarse domains of `partition2d`.  The fine mesh supplies
-    the geometry for the classification; each domain gets its own mesh."""
+    the geometry for the classification; each domain gets its own mesh with
+    MPFA-O ("mpfa"), TPFA ("tpfa") or L-method ("lmpfa", 3-D) lists."""
 
     def __init__(self, ctx, dim, ni, nj, nk, perm, coords=None, method="mpfa", continuity=1.0, **tensor):
         self.ctx, self.dim = ctx, dim
@@ -277,6 +278,8 @@ class StructuredUpscaler:
         m = api.Mesh(self.ctx, self.dim, *dims, perm, coords=pts)
         if self.method == "tpfa":
             m.compute_tpfa()
+        elif self.method == "lmpfa":
+            m.compute_lmpfa()
         else:
             m.compute_mpfa(self.continuity)
         return m, local

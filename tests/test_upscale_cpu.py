@@ -95,3 +95,18 @@ def test_uniform_tensor_is_reproduced_on_the_oracle(dim, nk):
     assert abs(res[0]["k21"] - K[3] * H) <= 1e-8 * H
     # the inner box is 4 x 4 cells: four connections per side and layer
     assert all(len(res[0]["inner"][o]) == 4 * max(nk, 1) for o in U.ORIENTATIONS_2D)
+
+
+def test_l_method_upscaling_of_a_diagonal_tensor_on_the_oracle():
+    """With the L-method lists (two-point fluxes at boundary corners, exact for
+    K-orthogonal grids) a homogeneous diagonal tensor on a box grid upscales
+    to itself times the thickness, with no cross term."""
+    from upscale_oracle import oracle_upscale
+    ni = nj = 12
+    nk = 2
+    K = (2.0, 0.5, 0.1, 0.0, 0.0, 0.0)
+    coords, perm = _grid(3, ni, nj, nk, K)
+    doms = U.partition2d(0.0, 0.0, [3], [4.0], [3], [4.0], border=2.0)
+    res, _ = oracle_upscale(3, ni, nj, nk, coords, perm, [doms[4]], method="lmpfa")
+    t = res[0]["tensor"]
+    assert np.allclose(t, [K[0] * nk, K[1] * nk, 0.0, 0.0, 0.0, 0.0], rtol=1e-8, atol=1e-9)

@@ -50,7 +50,7 @@ def oracle_upscale(dim, ni, nj, nk, coords, perm, domains, bc_type="Open", metho
         elements, bnd, innerc = U.classify(d, centers, conn, icen)
         dims, local, pts, pm = U.domain_box(dim, ni, nj, nk if dim == 3 else 0, coords, perm, elements)
         m = O.Mesh(dim, *dims, coords=pts, perm=pm)
-        m.mpfa(tpfa=(method == "tpfa"))
+        m.mpfa(tpfa=(method == "tpfa"), lmethod=(method == "lmpfa"))
         lbnd, lin = U.local_numbering(conn, local, m.connections(), bnd, innerc)
         bx, by = U.pressure_bc(d, centers[local], lbnd, bc_type)
         px, itx, _, _ = O.pressure_discretisation(m, bx)
