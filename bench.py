@@ -19,6 +19,13 @@ initial state through the public API with the state staged through
 page-locked host memory every step.  `--impl reference` times the CPU oracle
 (the C++ restatement of RS + MTJ, single-threaded like RS) on the same K
 steps with the same converged Newton loop.
+
+The same line carries the other measured legs as sub-objects: the
+mixed-precision solver on the same steps, the Peng-Robinson flash, the
+compositional line drive, the discrete adjoint of 50 steps with a checkpoint
+every 10, the ensemble of 64 members and the AMG preconditioner; with no
+flags the whole run takes about eight minutes on one GB300 (each leg has a
+flag to shorten or skip it).
 """
 import argparse
 import json
